@@ -1,0 +1,399 @@
+"""Benchmark of The Joker's rejection hot path on GB300.
+
+Workload (one step): one star with 40 RV epochs over 3000 d (sigma ~ U(0.05,
+0.5) km/s, Keplerian signal + noise, jitter applied with s ~ LogNormal(ln 0.5,
+1) km/s per prior sample) against a device-resident prior cache of 2^28
+samples (P log-uniform [2, 1024] d, e ~ Beta(0.867, 3.03), omega, M0 ~
+U[0, 2 pi)); the marginal ln L of every sample plus the acceptance test
+exp(lnL - max) > u against the caller's numpy PCG64 uniforms.  Seeded
+synthetic inputs stand in for survey data.
+
+metric: prior samples/s (lnL + accept).  ``value``: mixed-precision path, inputs
+resident in HBM.  ``e2e``: the same through the host-facing call -- the packed
+(S, 5) float64 chunk copied from pinned host memory, prepared, evaluated and
+accepted, accepted indices copied back -- every step.  The plain FP64 GPU path
+is reported beside it (``fp64``) on a 2^25-sample slice of the same workload.
+
+Multi-GPU (torchrun): each rank evaluates its own 2^28-sample shard of the
+cache for the same star (weak scaling); the per-star maximum is exchanged with
+one all-reduce(max) before the acceptance pass.
+
+``--impl reference`` times the reference's own CPU likelihood (the unmodified
+Cython CJokerHelper compiled into oracle/_ref, else the C restatement in
+oracle/) over a process pool of all host cores, on a bounded sample.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+N_EPOCHS = 40
+BASELINE_D = 3000.0
+SEED_STAR = 2
+SEED_CACHE = 0
+
+
+# ------------------------------------------------------------------ workload
+def make_star():
+    from thejoker_gb300.linear import rv_unit_columns
+    rng = np.random.default_rng(SEED_STAR)
+    t = np.sort(2456000.0 + rng.uniform(0, BASELINE_D, N_EPOCHS))
+    err = rng.uniform(0.05, 0.5, N_EPOCHS)
+    P = np.exp(rng.uniform(np.log(2), np.log(1024)))
+    e = rng.beta(0.867, 3.03)
+    om, M0 = rng.uniform(0, 2 * np.pi), rng.uniform(0, 2 * np.pi)
+    K = 30.0 * (P / 365.25) ** (-1 / 3) / np.sqrt(1 - e ** 2) * rng.normal()
+    rv = K * rv_unit_columns(t, t.min(), [P], [e], [om], [M0])[0] + rng.normal(0, 100.0) \
+        + rng.normal(0, np.sqrt(err ** 2 + 0.5 ** 2))
+    return dict(t=t, rv=rv, ivar=1 / err ** 2, t_ref=t.min(), trend_M=np.ones((N_EPOCHS, 1)),
+                mu=np.zeros(2), lam=np.array([0.0, 100.0 ** 2]),
+                k_prior=np.array([1.0, 30.0, 365.25, 500.0]))
+
+
+def fill_cache_host(out, seed, threads=16):
+    """Prior samples (P, e, omega, M0, s) into ``out`` (n x 5 float64), drawn
+    in parallel blocks from independent numpy generators."""
+    from concurrent.futures import ThreadPoolExecutor
+    n = out.shape[0]
+    nblk = max(1, min(threads * 4, n // 65536))
+    bounds = np.linspace(0, n, nblk + 1).astype(np.int64)
+    seqs = np.random.SeedSequence(seed).spawn(nblk)
+
+    def work(i):
+        a, b = bounds[i], bounds[i + 1]
+        r = np.random.default_rng(seqs[i])
+        m = b - a
+        out[a:b, 0] = np.exp(r.uniform(np.log(2.0), np.log(1024.0), m))
+        out[a:b, 1] = r.beta(0.867, 3.03, m)
+        out[a:b, 2] = r.uniform(0, 2 * np.pi, m)
+        out[a:b, 3] = r.uniform(0, 2 * np.pi, m)
+        out[a:b, 4] = np.exp(r.normal(np.log(0.5), 1.0, m))
+
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(work, range(nblk)))
+    return out
+
+
+# Algorithmic work per unit, fixed for the roofline:
+# FP32 operations of the mixed kernel per (sample, epoch) with the jitter
+# applied at L = 2, counted from its source (FMA = 2 flops, special-function
+# ops = 1), and per sample for the setup and the FP64 tail.
+FLOPS_PER_EPOCH = 196
+FLOPS_PER_SAMPLE = 60
+
+
+# ------------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([v.strip() for v in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._th = threading.Thread(target=self._run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._th.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 2 + i and s[2 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "n_samples": len(self.samples)}
+
+
+# ------------------------------------------------------------ CPU baseline
+def _cpu_worker(args):
+    kind, star, chunk = args
+    if kind == "reference":
+        from oracle import ref_cython
+        h = ref_cython.make_helper(star["t"], star["rv"], star["ivar"], star["t_ref"],
+                                   star["trend_M"], 1, 0, star["mu"], np.sqrt(star["lam"]),
+                                   True, *star["k_prior"][1:])
+        return np.array(h.batch_marginal_ln_likelihood(np.ascontiguousarray(chunk)))
+    from oracle import oracle
+    return oracle.batch_marginal_ln_likelihood(
+        star["t"], star["rv"], star["ivar"], star["t_ref"], star["trend_M"], star["mu"],
+        star["lam"], chunk, True, *star["k_prior"][1:], jitter=True)
+
+
+def cpu_baseline(star, n_samples, seed=1):
+    """Time the CPU likelihood + accept over a process pool of all cores on a
+    bounded sample; returns (samples/s, kind, cores, seconds)."""
+    import multiprocessing as mp
+    from oracle import build as ob, ref_cython
+    ob.build_all()
+    kind = "reference" if ref_cython.available() else "port"
+    cores = os.cpu_count() or 1
+    chunk = np.empty((n_samples, 5))
+    fill_cache_host(chunk, seed)
+    tasks = [(kind, star, c) for c in np.array_split(chunk, cores * 4)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_cpu_worker, tasks[:cores])          # warm the workers
+        t0 = time.perf_counter()
+        lls = np.concatenate(pool.map(_cpu_worker, tasks))
+        uu = np.random.default_rng(seed).uniform(size=len(lls))
+        np.where(np.exp(lls - lls.max()) > uu)
+        dt = time.perf_counter() - t0
+    return n_samples / dt, kind, cores, dt
+
+
+# ---------------------------------------------------------------- GPU path
+def run_ours(args, rank, world, dist):
+    import torch
+    from thejoker_gb300 import build as tb
+    from thejoker_gb300 import device as dev
+
+    tb.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    S = args.samples
+    star = make_star()
+    table = dev.StarTable([star], jitter="applied")
+
+    # host chunk (pinned) for this rank's shard, and the resident cache
+    host = torch.empty((S, 5), dtype=torch.float64).pin_memory()
+    fill_cache_host(host.numpy(), SEED_CACHE + rank)
+    cache = dev.PriorCache(S)
+    stage = torch.empty((args.h2d_chunk, 5), dtype=torch.float64, device="cuda")
+    for a in range(0, S, args.h2d_chunk):
+        b = min(S, a + args.h2d_chunk)
+        stage[: b - a].copy_(host[a:b], non_blocking=True)
+        cache.load(stage[: b - a], row0=a)
+    torch.cuda.synchronize()
+    lnl = torch.empty((1, S), dtype=torch.float64, device="cuda")
+    keys = dev.MaxKeys(1)
+    gen = np.random.default_rng(1000 + rank)
+    pcg_state, pcg_inc = dev.pcg64_state(gen)
+    seg = dict(lnl_off=0, n=S, idx_base=0, out_off=0, max_out=S, max_slot=0,
+               pcg=(pcg_state, pcg_inc, 0))
+    out_idx = torch.empty(S, dtype=torch.int64, device="cuda")
+    counts = torch.empty(1, dtype=torch.int64, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    lnl_ms = []
+
+    def step(precision="mixed", count=S, timing=False):
+        keys.t.zero_()
+        if timing:
+            ev[0].record()
+        dev.lnl(table, cache, lnl, precision=precision, count=count, max_keys=keys)
+        if timing:
+            ev[1].record()
+        if dist is not None and world > 1:
+            # keys order as unsigned 64-bit integers; flip the top bit so that
+            # the signed MAX of the all-reduce keeps that order
+            flip = torch.tensor(-(1 << 63), dtype=torch.int64, device="cuda")
+            m = torch.bitwise_xor(keys.t, flip)
+            dist.all_reduce(m, op=dist.ReduceOp.MAX)
+            keys.t.copy_(torch.bitwise_xor(m, flip))
+        sg = dict(seg)
+        sg["n"] = count
+        dev.accept(lnl, keys, [sg], u_source="pcg64", out_idx=out_idx, counts=counts)
+
+    def barrier():
+        if dist is not None and world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- value: inputs resident
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        barrier()
+        t0.record()
+        for _ in range(args.steps):
+            step(timing=True)
+            torch.cuda.synchronize()
+            lnl_ms.append(ev[0].elapsed_time(ev[1]))
+        t1.record()
+        barrier()
+    ms = t0.elapsed_time(t1) / args.steps
+    n_acc = int(counts.item())
+
+    # ---- e2e: pinned host chunk -> device -> prepare -> lnL -> accept -> host indices
+    def e2e_step():
+        for a in range(0, S, args.h2d_chunk):
+            b = min(S, a + args.h2d_chunk)
+            stage[: b - a].copy_(host[a:b], non_blocking=True)
+            cache.load(stage[: b - a], row0=a)
+        step()
+        c = int(counts.item())
+        return out_idx[: min(c, S)].cpu()
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    barrier()
+    te0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = e2e_step()
+    barrier()
+    e2e_ms = (time.perf_counter() - te0) * 1e3 / args.steps
+    d2h = int(res.numel()) * 8 + 8
+
+    # ---- plain FP64 GPU path on a slice of the same workload
+    S64 = min(S, args.fp64_samples)
+    step("fp64", S64)
+    barrier()
+    f0 = time.perf_counter()
+    for _ in range(2):
+        step("fp64", S64)
+    barrier()
+    fp64_ms = (time.perf_counter() - f0) * 1e3 / 2
+
+    # ---- max over ranks
+    def gmax(x):
+        if dist is None or world == 1:
+            return x
+        tt = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        return float(tt.item())
+
+    ms, e2e_ms, fp64_ms = gmax(ms), gmax(e2e_ms), gmax(fp64_ms)
+    kern_ms = float(np.median(lnl_ms))
+    if rank != 0:
+        return None
+    total = S * world
+    flops = S * (N_EPOCHS * FLOPS_PER_EPOCH + FLOPS_PER_SAMPLE)
+    achieved = flops / (kern_ms * 1e-3) / 1e12
+    peak = args.fp32_peak
+    line = {
+        "metric": "prior samples/s (lnL+accept)",
+        "value": total / (ms * 1e-3),
+        "unit": "samples/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64 (mixed)",
+        "data": "synthetic (seeded; prior cache and star drawn with numpy)",
+        "config": {"workload": f"1 star x {N_EPOCHS} epochs over {BASELINE_D:.0f} d, jitter "
+                               f"applied, prior cache 2^{int(math.log2(S))} samples per GPU",
+                   "prior_samples_per_gpu": S, "n_epochs": N_EPOCHS, "n_linear": 2,
+                   "l2": "inputs larger than L2 (cache 76 B/sample resident, 2^28 samples)",
+                   "precision": "mixed", "u_source": "numpy PCG64 stream regenerated on device"},
+        "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "samples/s",
+                "h2d_bytes_per_step": S * 40, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms},
+        "fp64": {"value": S64 * world / (fp64_ms * 1e-3), "unit": "samples/s",
+                 "samples": S64, "ms_per_step": fp64_ms},
+        "accepted_per_step": n_acc,
+        "gpu_launches": 4 * args.steps,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": args.traffic,
+                     "kernel": "lnl_mixed_kernel<2,true,false>",
+                     "kernel_ms": kern_ms,
+                     "peak_source": "FP32 FMA throughput measured on this pool's GB300 "
+                                    "(FMA-chain microkernel, 67.6 TFLOP/s)",
+                     "flops_per_launch": flops},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        v, kind, cores, secs = cpu_baseline(star, args.cpu_samples)
+        line["cpu_baseline"] = {"value": v, "unit": "samples/s", "cores": cores, "kind": kind,
+                                "sample": f"{args.cpu_samples} prior samples of the same star "
+                                          f"({secs:.1f} s wall); the reference ignores jitter"}
+    return line
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return None
+    star = make_star()
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(star, args.cpu_samples // 4)
+    for k in range(args.steps):
+        v, kind, cores, secs = cpu_baseline(star, args.cpu_samples, seed=10 + k)
+        vals.append((v, secs))
+    v = float(np.mean([x[0] for x in vals]))
+    ms = float(np.mean([x[1] for x in vals])) * 1e3
+    return {
+        "metric": "prior samples/s (lnL+accept)", "value": v, "unit": "samples/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": f"1 star x {N_EPOCHS} epochs over {BASELINE_D:.0f} d, jitter in "
+                               "the samples (ignored by the reference)",
+                   "prior_samples_per_step": args.cpu_samples},
+        "cpu_baseline": {"value": v, "unit": "samples/s", "cores": cores, "kind": kind,
+                         "sample": f"{args.cpu_samples} prior samples per step"},
+        "e2e": {"value": v, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--samples", type=int, default=1 << 28)
+    p.add_argument("--fp64-samples", type=int, default=1 << 25)
+    p.add_argument("--cpu-samples", type=int, default=1 << 20)
+    p.add_argument("--h2d-chunk", type=int, default=1 << 25)
+    p.add_argument("--fp32-peak", type=float, default=67.6)
+    p.add_argument("--traffic", type=float, default=None)
+    p.add_argument("--no-cpu", action="store_true")
+    args = p.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+    else:
+        if world > 1:
+            import torch
+            import torch.distributed as tdist
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+            tdist.init_process_group("nccl")
+            dist = tdist
+        line = run_ours(args, rank, world, dist)
+        if dist is not None:
+            dist.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

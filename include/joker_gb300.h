@@ -1,0 +1,172 @@
+/*
+ * joker_gb300.h -- C ABI of the GB300 (sm_103a) marginal-likelihood and
+ * rejection-sampling hot path of The Joker.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int status (JOKER_OK or one of the JOKER_E* codes below; never aborts) and,
+ * for device work, a cudaStream_t passed as void*.  A failing call leaves a
+ * one-line message readable through joker_last_error().
+ *
+ * Pointers named d_* are device pointers owned by the caller; every other
+ * array argument is host memory, read during the call and not retained.
+ *
+ * Reference interfaces replaced (paths inside the adrn/thejoker project):
+ *   joker_stars_create                    CJokerHelper.__init__
+ *                                         thejoker/src/fast_likelihood.pyx:125-253
+ *   joker_batch_marginal_ln_likelihood    CJokerHelper.batch_marginal_ln_likelihood
+ *                                         thejoker/src/fast_likelihood.pyx:428-469
+ *   joker_lnl                             the same loop over many stars and a
+ *                                         shared prior cache (the pool map of
+ *                                         marginal_ln_likelihood_worker,
+ *                                         thejoker/multiproc_helpers.py:63-120)
+ *   joker_accept                          exp(lls - lls.max()) > uu and the
+ *                                         index list truncated to
+ *                                         max_posterior_samples,
+ *                                         thejoker/likelihood_helpers.py:107-109,
+ *                                         thejoker/multiproc_helpers.py:256-258
+ */
+#ifndef JOKER_GB300_H
+#define JOKER_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JOKER_ABI_VERSION 1
+
+/* status codes */
+#define JOKER_OK 0
+#define JOKER_EINVAL 1      /* bad argument, shape or size */
+#define JOKER_ECUDA 2       /* a CUDA runtime call failed */
+#define JOKER_ENOMEM 3      /* device or host allocation failed */
+#define JOKER_ERANGE 4      /* a size above a documented maximum */
+
+/* limits */
+#define JOKER_MAX_LINEAR 6  /* K + poly_trend + n_offsets */
+
+/* precision of the likelihood kernels */
+#define JOKER_FP64 0        /* plain FP64 throughout */
+#define JOKER_MIXED 1       /* FP64-accurate phase, FP32 Kepler, compensated
+                               FP32 epoch sums, FP64 small solve; sin/cos of
+                               the Kepler starter on the special-function unit */
+#define JOKER_MIXED_ACCURATE 2  /* as JOKER_MIXED with correctly rounded sincosf */
+
+/* jitter handling (the reference Cython computes the jittered inverse variance
+   but never reads it, fast_likelihood.pyx:458; its NumPy test oracle applies
+   it, thejoker/src/tests/py_likelihood.py:168-170) */
+#define JOKER_JITTER_REFERENCE 0   /* s ignored, as CJokerHelper */
+#define JOKER_JITTER_APPLIED 1     /* ivar / (1 + s^2 ivar) per sample */
+
+/* source of the acceptance uniforms */
+#define JOKER_U_ARRAY 0     /* d_u[u_off + i] */
+#define JOKER_U_PCG64 1     /* numpy PCG64 stream, reproduced on the device */
+
+typedef struct joker_stars joker_stars;   /* opaque, device-resident star table */
+typedef struct joker_cache joker_cache;   /* opaque, device-resident prior cache */
+
+/* One segment of the acceptance pass: the ln L values of one star over a
+ * contiguous run of samples, the uniforms to test them against, and where the
+ * accepted indices go.  Plain C layout, 96 bytes. */
+typedef struct {
+    int64_t lnl_off;       /* first ln L of the segment in d_lnl */
+    int64_t n;             /* number of samples */
+    int64_t idx_base;      /* added to the in-segment position of each accepted sample */
+    int64_t out_off;       /* first output slot in d_out_idx / d_out_lnl */
+    int64_t max_out;       /* output capacity; acceptance beyond it is counted, not written */
+    int64_t u_off;         /* JOKER_U_ARRAY: first uniform in d_u */
+    uint64_t pcg_state_hi; /* JOKER_U_PCG64: PCG64 state and increment, positioned */
+    uint64_t pcg_state_lo; /*   so that the next draw is the segment's first uniform */
+    uint64_t pcg_inc_hi;
+    uint64_t pcg_inc_lo;
+    int32_t max_slot;      /* which running maximum (d_max_key) the segment uses */
+    int32_t reserved;
+    int64_t reserved2;
+} joker_accept_seg;
+
+int joker_abi_version(void);
+const char *joker_last_error(void);
+
+/* ---- star table -----------------------------------------------------------
+ * Mirrors CJokerHelper.__init__ (fast_likelihood.pyx:125-253) for n_stars
+ * stars at once.  Star k owns epochs [epoch_offsets[k], epoch_offsets[k+1]).
+ *   t, rv, ivar     times (days), velocities and inverse variances per epoch
+ *   t_ref           reference time per star (the reference's _t_ref_bmjd)
+ *   trend_M         total_epochs x (n_linear-1), row-major: the columns of
+ *                   CJokerHelper's trend_M (v0 / offset indicators, then
+ *                   (t - t_ref)^k), fast_likelihood.pyx:174-184
+ *   mu, lambda      n_stars x n_linear prior means / variances in the
+ *                   CJokerHelper index order K, v0, offsets..., v1, ...
+ *   k_prior         n_stars x 4: {scaled, sigma_K0, P0, max_K}; scaled != 0 is
+ *                   the FixedCompanionMass prior (the reference's
+ *                   fixed_K_prior == 0, :225-228, :461-464), whose variance
+ *                   min(max_K^2, sigma_K0^2 / (1 - e^2) (P / P0)^(-2/3))
+ *                   replaces lambda[k][0] per sample
+ *   jitter_mode     JOKER_JITTER_REFERENCE or JOKER_JITTER_APPLIED
+ * Errors: JOKER_EINVAL for n_linear outside [1, JOKER_MAX_LINEAR], a star
+ * without epochs, non-increasing offsets or a non-positive ivar or lambda. */
+int joker_stars_create(joker_stars **out, int n_stars, int n_linear,
+                       const int64_t *epoch_offsets, const double *t,
+                       const double *rv, const double *ivar, const double *t_ref,
+                       const double *trend_M, const double *mu,
+                       const double *lambda, const double *k_prior,
+                       int jitter_mode);
+int joker_stars_destroy(joker_stars *stars);
+int joker_stars_info(const joker_stars *stars, int *n_stars, int *n_linear,
+                     int64_t *total_epochs, int *max_epochs);
+
+/* ---- prior cache ----------------------------------------------------------
+ * A device-resident copy of packed prior samples (JokerSamples.pack order
+ * P, e, omega, M0, s in internal units, thejoker/samples.py:404-445) kept both
+ * as FP64 columns and in the prepared form the mixed kernel reads.
+ * joker_cache_load converts rows [row0, row0 + n) from a device n x 5
+ * row-major FP64 array; it rejects e outside [0, 1) or P <= 0 lazily (the
+ * result for such rows is NaN, as the reference's arithmetic would give). */
+int joker_cache_create(joker_cache **out, int64_t capacity);
+int joker_cache_destroy(joker_cache *cache);
+int joker_cache_load(joker_cache *cache, const double *d_chunk, int64_t n,
+                     int64_t row0, void *stream);
+int64_t joker_cache_capacity(const joker_cache *cache);
+
+/* ---- likelihood -----------------------------------------------------------
+ * Drop-in for CJokerHelper.batch_marginal_ln_likelihood on star `star`:
+ * d_chunk is n_samples x 5 row-major FP64 (the reference's chunk, :428-451),
+ * d_lnl receives n_samples FP64 ln L values computed in FP64. */
+int joker_batch_marginal_ln_likelihood(const joker_stars *stars, int star,
+                                       const double *d_chunk, int64_t n_samples,
+                                       double *d_lnl, void *stream);
+
+/* ln L of stars [star0, star0 + n_sel) over cache rows [row0, row0 + count).
+ * d_lnl is n_sel x count with row stride ld.  When d_max_key is not NULL,
+ * d_max_key[k] holds an order-preserving integer image of the running
+ * maximum of star star0+k and is raised atomically (it must be zeroed, or hold
+ * a previous maximum, before the call).  precision: JOKER_FP64, JOKER_MIXED or
+ * JOKER_MIXED_ACCURATE.  block (threads per CTA, 0 = 128) and chunk (samples
+ * per work item, a multiple of block, 0 = 1024) tune the launch.  Calls that
+ * share one joker_stars handle must be ordered on one stream. */
+int joker_lnl(const joker_stars *stars, const joker_cache *cache, int star0,
+              int n_sel, int64_t row0, int64_t count, int precision,
+              double *d_lnl, int64_t ld, uint64_t *d_max_key, int block,
+              int64_t chunk, void *stream);
+
+/* Decode an order-preserving key back to the double it encodes. */
+double joker_key_to_double(uint64_t key);
+
+/* ---- acceptance -----------------------------------------------------------
+ * For each segment: keep_i = exp(lnl_i - max) > u_i with max the decoded
+ * d_max_key[seg.max_slot]; the indices (idx_base + i) of kept samples are
+ * written in ascending order to d_out_idx[out_off ...] (at most max_out of
+ * them), their ln L to d_out_lnl (if not NULL), and the total number kept to
+ * d_count[segment].  segs is a host array of n_segs segments.  d_work must
+ * hold joker_accept_workspace(segs, n_segs) bytes. */
+int64_t joker_accept_workspace(const joker_accept_seg *segs, int n_segs);
+int joker_accept(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
+                 const uint64_t *d_max_key, int u_source, const double *d_u,
+                 int64_t *d_out_idx, double *d_out_lnl, int64_t *d_count,
+                 void *d_work, int64_t work_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JOKER_GB300_H */

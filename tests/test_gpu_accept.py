@@ -1,0 +1,142 @@
+"""GPU acceptance pass and the sampler API against the reference's rules
+(likelihood_helpers.py:91-229) restated with NumPy (GB300 only)."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import oracle_lnl, synth_chunk, synth_star
+
+pytestmark = pytest.mark.gpu
+
+
+def _keys_for(values):
+    from thejoker_gb300 import device as dev
+    import struct
+    mk = dev.MaxKeys(len(values))
+    keys = []
+    for m in values:
+        b = struct.unpack("<q", struct.pack("<d", m))[0]
+        k = (~b) & 0xFFFFFFFFFFFFFFFF if b < 0 else (b | (1 << 63))
+        keys.append(np.array(k, dtype=np.uint64).view(np.int64))
+    mk.t.copy_(torch.tensor(np.array(keys, dtype=np.int64)))
+    return mk
+
+
+@pytest.mark.parametrize("n", [1, 31, 32, 1000, 8192, 8193, 100000])
+def test_pcg64_stream_matches_numpy_uniform(cuda, n):
+    """With lnl = log(x) and max 0 the pass keeps exactly x > u: the device
+    regenerates rng.uniform(size=n) bit for bit."""
+    from thejoker_gb300 import device as dev
+    rng = np.random.default_rng(1234 + n)
+    x = rng.uniform(size=n)
+    lnl = np.log(x)
+    lnl[0] = 0.0
+    gen = np.random.default_rng(99)
+    gen.uniform(size=17)                       # arbitrary position in the stream
+    st, inc = dev.pcg64_state(gen)
+    uu = np.random.Generator(np.random.PCG64())
+    uu.bit_generator.state = gen.bit_generator.state
+    expect = np.where(np.exp(lnl - lnl.max()) > uu.uniform(size=n))[0]
+    d = torch.from_numpy(lnl).cuda()
+    idx, out_lnl, counts = dev.accept(d, _keys_for([0.0]), [dict(
+        lnl_off=0, n=n, out_off=0, max_out=n, max_slot=0, pcg=(st, inc, 0))],
+        out_lnl=torch.empty(n, dtype=torch.float64, device="cuda"))
+    c = int(counts[0])
+    assert c == len(expect)
+    np.testing.assert_array_equal(idx[:c].cpu().numpy(), expect)
+    np.testing.assert_array_equal(out_lnl[:c].cpu().numpy(), lnl[expect])
+
+
+def test_array_source_truncation_and_segments(cuda):
+    from thejoker_gb300 import device as dev
+    rng = np.random.default_rng(5)
+    lnl = np.concatenate([rng.normal(0, 3, 20000), rng.normal(-2, 1, 9000)])
+    u = rng.uniform(size=lnl.size)
+    segs = [dict(lnl_off=0, n=20000, idx_base=0, out_off=0, max_out=50, max_slot=0, u_off=0),
+            dict(lnl_off=20000, n=9000, idx_base=100, out_off=50, max_out=10000, max_slot=1,
+                 u_off=20000)]
+    m0, m1 = lnl[:20000].max(), lnl[20000:].max()
+    idx, _, counts = dev.accept(torch.from_numpy(lnl).cuda(), _keys_for([m0, m1]), segs,
+                                u_source="array", u=torch.from_numpy(u).cuda())
+    idx = idx.cpu().numpy()
+    e0 = np.where(np.exp(lnl[:20000] - m0) > u[:20000])[0]
+    e1 = np.where(np.exp(lnl[20000:] - m1) > u[20000:])[0]
+    assert int(counts[0]) == len(e0) and int(counts[1]) == len(e1)
+    np.testing.assert_array_equal(idx[:min(50, len(e0))], e0[:50])
+    np.testing.assert_array_equal(idx[50:50 + len(e1)], e1 + 100)
+
+
+def test_accept_extremes(cuda):
+    """u == 0 accepts anything above exp underflow; NaN max keeps nothing."""
+    from thejoker_gb300 import device as dev
+    lnl = np.array([0.0, -100.0, -700.0, -800.0, -5.0])
+    u = np.array([0.5, 0.0, 0.0, 0.0, 0.999999])
+    idx, _, counts = dev.accept(torch.from_numpy(lnl).cuda(), _keys_for([0.0]),
+                                [dict(lnl_off=0, n=5, out_off=0, max_out=5, max_slot=0, u_off=0)],
+                                u_source="array", u=torch.from_numpy(u).cuda())
+    expect = np.where(np.exp(lnl) > u)[0]
+    np.testing.assert_array_equal(idx[:int(counts[0])].cpu().numpy(), expect)
+    idx, _, counts = dev.accept(torch.from_numpy(lnl).cuda(), _keys_for([float("nan")]),
+                                [dict(lnl_off=0, n=5, out_off=0, max_out=5, max_slot=0, u_off=0)],
+                                u_source="array", u=torch.from_numpy(u).cuda())
+    assert int(counts[0]) == 0
+
+
+def _reference_rejection(star, chunk, rng, max_post, n_lin, prior):
+    """likelihood_helpers.rejection_sample_inmem restated with the oracle."""
+    from thejoker_gb300.linear import posterior_linear_samples
+    lls = oracle_lnl(star, chunk)
+    uu = rng.uniform(size=len(lls))
+    good = np.where(np.exp(lls - lls.max()) > uu)[0][:max_post]
+    raw, _, _ = posterior_linear_samples(chunk[good], n_lin, rng, star["t"], star["rv"],
+                                         star["ivar"], star["t_ref"], star["trend_M"],
+                                         star["mu"], star["lam"], star["k_prior"])
+    return good, raw, lls
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_thejoker_rejection_sample_matches_reference_pipeline(cuda, precision):
+    from thejoker_gb300 import JokerPrior, RVData, TheJoker
+    rng = np.random.default_rng(21)
+    st = synth_star(rng, 12, K=5.0)
+    prior = JokerPrior.default(P_min=2, P_max=1024, sigma_K0=30.0, sigma_v=100.0)
+    data = RVData(st["t"], st["rv"], 1 / np.sqrt(st["ivar"]))
+    samples = prior.sample(20000, rng=np.random.default_rng(3))
+    chunk = samples.pack()[0]
+    joker = TheJoker(prior, rng=np.random.default_rng(42), precision=precision)
+    out = joker.rejection_sample(data, samples, max_posterior_samples=300, return_logprobs=True)
+    good, raw, lls = _reference_rejection(st, chunk, np.random.default_rng(42), 300, 1, prior)
+    assert len(out) == len(good) > 0
+    np.testing.assert_array_equal(out["P"], chunk[good, 0])
+    np.testing.assert_allclose(out["K"], raw[:, 5], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(out["v0"], raw[:, 6], rtol=1e-6, atol=1e-6)
+    # the generator ends in the same state as the reference's
+    r2 = np.random.default_rng(42)
+    _reference_rejection(st, chunk, r2, 300, 1, prior)
+    assert joker.rng.bit_generator.state == r2.bit_generator.state
+
+
+def test_thejoker_iterative_matches_reference_loop(cuda):
+    from thejoker_gb300 import JokerPrior, RVData, TheJoker
+    rng = np.random.default_rng(22)
+    st = synth_star(rng, 10, K=20.0)
+    prior = JokerPrior.default(P_min=2, P_max=1024, sigma_K0=30.0, sigma_v=100.0)
+    data = RVData(st["t"], st["rv"], 1 / np.sqrt(st["ivar"]))
+    chunk = prior.sample(200000, rng=np.random.default_rng(4)).pack()[0]
+    joker = TheJoker(prior, rng=np.random.default_rng(7), precision="fp64")
+    out = joker.iterative_rejection_sample(data, chunk, n_requested_samples=8,
+                                           init_batch_size=2000)
+    # likelihood_helpers.iterative_rejection_inmem restated
+    r = np.random.default_rng(7)
+    lls_all = oracle_lnl(st, chunk[:200000])
+    n_process, start, allm = 2000, 0, np.array([])
+    for _ in range(128):
+        allm = np.concatenate([allm, lls_all[start:start + n_process]])
+        uu = r.uniform(size=len(allm))
+        good = np.where(np.exp(allm - allm.max()) > uu)[0]
+        if len(good) >= 8:
+            break
+        start += n_process
+        n_process = int(1 * (8 - len(good)) / len(good) * len(allm))
+        n_process = min(n_process, 200000 - start)
+    np.testing.assert_array_equal(out["P"], chunk[good[:8], 0])

@@ -1,0 +1,187 @@
+"""GPU parity: the CUDA kernels against the reference's outputs and the CPU
+oracle, called through the C ABI (GB300 only).
+
+Tolerances, as stated for this path:
+* FP64 kernel: |dlnL| <= 1e-9 * max(1, |lnL|) against the reference's Cython
+  output, and against 50-digit values; where the reference's own FP64 error
+  is larger (quadratic trend: 3.7e-9) the comparison with it uses 1e-8.
+* mixed kernel: |dlnL| <= 3e-4 + 2e-7 |lnL| for samples within 40 of the best
+  ln L of the batch (the only ones an acceptance test can keep), and 2e-5
+  relative for all samples.  The FP32 velocity column carries ~1e-7 absolute
+  error; its effect on chi2 is 2 K_hat sum w res dm, so the error grows with
+  the residuals of the fit (poor fits, few epochs).
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import oracle_lnl, rel_err, star_from_fixture, synth_chunk, synth_star
+
+pytestmark = pytest.mark.gpu
+
+MIXED_ABS, MIXED_REL_NEAR, MIXED_REL = 3e-4, 2e-7, 2e-5
+
+
+def mixed_ok(got, ref):
+    near = ref >= ref.max() - 40.0
+    d = np.abs(got - ref)
+    return (np.all(d[near] <= MIXED_ABS + MIXED_REL_NEAR * np.abs(ref[near]))
+            and rel_err(got, ref).max() <= MIXED_REL)
+
+
+CASES = ["againstpy", "scalevark", "config1", "trend3", "offsets", "jitter"]
+
+
+def _dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def _table(stars, jitter="reference"):
+    from thejoker_gb300.device import StarTable
+    return StarTable(stars, jitter=jitter)
+
+
+def _drop_in(table, star, chunk):
+    from thejoker_gb300 import _native as nat
+    d = _dev(chunk)
+    out = torch.full((chunk.shape[0],), float("nan"), dtype=torch.float64, device="cuda")
+    nat.check(nat.lib().joker_batch_marginal_ln_likelihood(
+        table.handle, star, ctypes.c_void_p(d.data_ptr()), chunk.shape[0],
+        ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return out.cpu().numpy()
+
+
+def _lnl(table, chunk, precision, star0=0, n_sel=None, max_keys=None):
+    from thejoker_gb300 import device as dev
+    cache = dev.PriorCache.from_samples(chunk)
+    n_sel = table.n_stars - star0 if n_sel is None else n_sel
+    out = torch.full((n_sel, chunk.shape[0]), float("nan"), dtype=torch.float64, device="cuda")
+    dev.lnl(table, cache, out, precision=precision, star0=star0, n_sel=n_sel, max_keys=max_keys)
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_fp64_drop_in_matches_reference(cuda, golden_dir, case):
+    z = np.load(os.path.join(golden_dir, f"ref_lnl_{case}.npz"))
+    table = _table([star_from_fixture(z)])
+    got = _drop_in(table, 0, z["chunk"])
+    ref = z["lnl_ref"]
+    tol_ref = 1e-8 if case == "trend3" else 1e-9
+    assert rel_err(got, ref).max() <= tol_ref
+    assert rel_err(got[z["idx_hp"]], z["lnl_hp"]).max() <= 1e-9
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_fp64_cache_path_equals_drop_in(cuda, golden_dir, case):
+    z = np.load(os.path.join(golden_dir, f"ref_lnl_{case}.npz"))
+    table = _table([star_from_fixture(z)])
+    a = _drop_in(table, 0, z["chunk"])
+    b = _lnl(table, z["chunk"], "fp64")[0]
+    np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("precision", ["mixed", "mixed_accurate"])
+def test_mixed_error_bound(cuda, golden_dir, case, precision):
+    z = np.load(os.path.join(golden_dir, f"ref_lnl_{case}.npz"))
+    table = _table([star_from_fixture(z)])
+    got = _lnl(table, z["chunk"], precision)[0]
+    ref = z["lnl_ref"]
+    near = ref >= ref.max() - 40.0
+    d = np.abs(got - ref)
+    print(case, precision, "max |dlnL| near max", d[near].max(), "max rel", rel_err(got, ref).max())
+    assert mixed_ok(got, ref)
+
+
+def test_jitter_applied_fp64_and_mixed(cuda, golden_dir):
+    z = np.load(os.path.join(golden_dir, "ref_lnl_jitter.npz"))
+    table = _table([star_from_fixture(z)], jitter="applied")
+    ref = z["lnl_py_jitter"]
+    got64 = _lnl(table, z["chunk"], "fp64")[0]
+    assert rel_err(got64, ref).max() <= 1e-9
+    gotm = _lnl(table, z["chunk"], "mixed")[0]
+    assert mixed_ok(gotm, ref)
+
+
+def test_many_stars_ragged_epochs_and_tiles(cuda):
+    """Stars with 3..300 epochs (300 > one 256-epoch shared-memory tile),
+    different trends, in one persistent launch."""
+    rng = np.random.default_rng(11)
+    stars = [synth_star(rng, n, poly=2) for n in (3, 300, 17, 64, 5, 256, 257)]
+    chunk = synth_chunk(rng, 3000)
+    table = _table(stars)
+    keys = None
+    from thejoker_gb300 import device as dev
+    keys = dev.MaxKeys(len(stars))
+    got64 = _lnl(table, chunk, "fp64", max_keys=keys)
+    gotm = _lnl(table, chunk, "mixed")
+    for k, st in enumerate(stars):
+        ref = oracle_lnl(st, chunk)
+        # the (t - t_ref) trend column makes the oracle's N x N LU lose ~1e-8
+        assert rel_err(got64[k], ref).max() <= 2e-8, k
+        assert mixed_ok(gotm[k], ref), k
+    np.testing.assert_array_equal(keys.values(), got64.max(axis=1))
+
+
+def test_subset_of_stars_and_rows(cuda):
+    rng = np.random.default_rng(12)
+    stars = [synth_star(rng, n) for n in (8, 9, 10, 11)]
+    chunk = synth_chunk(rng, 5000)
+    table = _table(stars)
+    from thejoker_gb300 import device as dev
+    cache = dev.PriorCache.from_samples(chunk)
+    out = torch.full((2, 1200), float("nan"), dtype=torch.float64, device="cuda")
+    dev.lnl(table, cache, out, precision="fp64", star0=1, n_sel=2, row0=777, count=1100)
+    o = out.cpu().numpy()
+    for k in range(2):
+        ref = oracle_lnl(stars[1 + k], chunk[777:1877])
+        assert rel_err(o[k, :1100], ref).max() <= 1e-9
+        assert np.all(np.isnan(o[k, 1100:]))
+
+
+def test_deterministic_replay(cuda, golden_dir):
+    z = np.load(os.path.join(golden_dir, "ref_lnl_config1.npz"))
+    table = _table([star_from_fixture(z)])
+    for prec in ("fp64", "mixed"):
+        a = _lnl(table, z["chunk"], prec)
+        b = _lnl(table, z["chunk"], prec)
+        np.testing.assert_array_equal(a, b)
+
+
+def test_edge_cases(cuda):
+    rng = np.random.default_rng(13)
+    st = synth_star(rng, 7)
+    table = _table([st])
+    # empty chunk
+    assert _drop_in(table, 0, np.zeros((0, 5))).shape == (0,)
+    # one sample
+    ch = synth_chunk(rng, 1)
+    assert rel_err(_drop_in(table, 0, ch), oracle_lnl(st, ch)).max() <= 1e-9
+    # eccentricity outside [0, 1) gives NaN like the reference's arithmetic
+    bad = synth_chunk(rng, 4)
+    bad[2, 1] = 1.5
+    out = _drop_in(table, 0, bad)
+    assert np.isnan(out[2]) and np.all(np.isfinite(out[[0, 1, 3]]))
+    # circular orbits and e close to 1
+    ch = synth_chunk(rng, 64)
+    ch[:32, 1] = 0.0
+    ch[32:, 1] = 0.999
+    assert rel_err(_drop_in(table, 0, ch), oracle_lnl(st, ch)).max() <= 1e-9
+
+
+def test_errors_raise(cuda):
+    from thejoker_gb300 import _native as nat
+    from thejoker_gb300 import device as dev
+    rng = np.random.default_rng(14)
+    table = _table([synth_star(rng, 5)])
+    cache = dev.PriorCache.from_samples(synth_chunk(rng, 10))
+    out = torch.empty((1, 20), dtype=torch.float64, device="cuda")
+    with pytest.raises(nat.JokerError):
+        dev.lnl(table, cache, out, row0=5, count=10)     # beyond the cache
+    with pytest.raises(nat.JokerError):
+        dev.lnl(table, cache, out, star0=1, n_sel=1)     # no such star
+    with pytest.raises(nat.JokerError):
+        cache.load(synth_chunk(rng, 11))                  # above capacity

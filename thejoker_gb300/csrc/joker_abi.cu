@@ -1,0 +1,469 @@
+// C ABI of libjoker_gb300 (declared in include/joker_gb300.h): handle
+// management, the per-star FP64 preparation done once on the host, and the
+// launchers.  No torch types cross this boundary.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include "joker_internal.cuh"
+
+namespace joker {
+cudaError_t launch_lnl(int precision, int L, bool jit, const LnlArgs &a, int block,
+                       cudaStream_t st);
+cudaError_t launch_prepare(const double *chunk, int64_t n, int64_t row0, double *P, double *E,
+                           double *OM, double *M0, double *S, float4 *mx_a, float4 *mx_b,
+                           float *mx_s2, cudaStream_t st);
+cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st);
+int64_t accept_blocks(const joker_accept_seg *segs, int n_segs, int64_t *blk_base_host);
+}  // namespace joker
+
+using namespace joker;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                     \
+    do {                                                                                   \
+        cudaError_t e_ = (expr);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(JOKER_ECUDA, "%s: %s", #expr, cudaGetErrorString(e_));             \
+    } while (0)
+
+struct joker_stars {
+    int n_stars = 0, L = 0, jitter = 0, max_epochs = 0;
+    int64_t total_epochs = 0;
+    std::vector<int64_t> off;
+    StarRec *d_stars = nullptr;
+    double *d_ep64 = nullptr;
+    float *d_ep32 = nullptr;
+    int *d_queue = nullptr;
+    int *d_order = nullptr;      // stars sorted by epoch count, largest first
+};
+
+struct joker_cache {
+    int64_t cap = 0;
+    double *P = nullptr, *E = nullptr, *OM = nullptr, *M0 = nullptr, *S = nullptr;
+    float4 *mx_a = nullptr, *mx_b = nullptr;
+    float *mx_s2 = nullptr;
+};
+
+extern "C" int joker_abi_version(void) { return JOKER_ABI_VERSION; }
+extern "C" const char *joker_last_error(void) { return g_err.c_str(); }
+
+extern "C" double joker_key_to_double(uint64_t key) { return key_to_double(key); }
+
+// ---------------------------------------------------------------- star table
+static void split_ff(double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// Inverse and log-determinant of a small symmetric positive-definite matrix
+// (Cholesky, long double).  Returns false if not positive definite.
+static bool spd_inverse(int n, const long double *A, long double *Ainv, long double &logdet) {
+    std::vector<long double> Lc(n * n, 0.0L);
+    logdet = 0.0L;
+    for (int j = 0; j < n; ++j) {
+        long double d = A[j * n + j];
+        for (int k = 0; k < j; ++k) d -= Lc[j * n + k] * Lc[j * n + k];
+        if (!(d > 0.0L)) return false;
+        const long double ljj = sqrtl(d);
+        Lc[j * n + j] = ljj;
+        logdet += 2.0L * logl(ljj);
+        for (int i = j + 1; i < n; ++i) {
+            long double v = A[i * n + j];
+            for (int k = 0; k < j; ++k) v -= Lc[i * n + k] * Lc[j * n + k];
+            Lc[i * n + j] = v / ljj;
+        }
+    }
+    // inverse column by column
+    std::vector<long double> col(n);
+    for (int c = 0; c < n; ++c) {
+        for (int i = 0; i < n; ++i) {
+            long double v = (i == c) ? 1.0L : 0.0L;
+            for (int k = 0; k < i; ++k) v -= Lc[i * n + k] * col[k];
+            col[i] = v / Lc[i * n + i];
+        }
+        for (int i = n - 1; i >= 0; --i) {
+            long double v = col[i];
+            for (int k = i + 1; k < n; ++k) v -= Lc[k * n + i] * col[k];
+            col[i] = v / Lc[i * n + i];
+        }
+        for (int i = 0; i < n; ++i) Ainv[i * n + c] = col[i];
+    }
+    return true;
+}
+
+extern "C" int joker_stars_create(joker_stars **out, int n_stars, int n_linear,
+                                  const int64_t *epoch_offsets, const double *t,
+                                  const double *rv, const double *ivar, const double *t_ref,
+                                  const double *trend_M, const double *mu,
+                                  const double *lambda, const double *k_prior,
+                                  int jitter_mode) {
+    if (!out) return fail(JOKER_EINVAL, "joker_stars_create: out is NULL");
+    *out = nullptr;
+    if (n_stars <= 0) return fail(JOKER_EINVAL, "joker_stars_create: n_stars must be > 0");
+    if (n_linear < 1 || n_linear > JOKER_MAX_LINEAR)
+        return fail(JOKER_EINVAL, "joker_stars_create: n_linear=%d outside [1, %d]", n_linear,
+                    JOKER_MAX_LINEAR);
+    if (jitter_mode != JOKER_JITTER_REFERENCE && jitter_mode != JOKER_JITTER_APPLIED)
+        return fail(JOKER_EINVAL, "joker_stars_create: unknown jitter_mode %d", jitter_mode);
+    if (!epoch_offsets || !t || !rv || !ivar || !t_ref || !mu || !lambda || !k_prior ||
+        (n_linear > 1 && !trend_M))
+        return fail(JOKER_EINVAL, "joker_stars_create: NULL array argument");
+    if (epoch_offsets[0] != 0) return fail(JOKER_EINVAL, "epoch_offsets[0] must be 0");
+    const int L = n_linear, T = n_linear - 1;
+    int max_ep = 0;
+    for (int k = 0; k < n_stars; ++k) {
+        const int64_t n = epoch_offsets[k + 1] - epoch_offsets[k];
+        if (n <= 0) return fail(JOKER_EINVAL, "star %d has no epochs", k);
+        if (n > (int64_t)1 << 30) return fail(JOKER_ERANGE, "star %d: too many epochs", k);
+        max_ep = std::max<int>(max_ep, (int)n);
+    }
+    const int64_t NE = epoch_offsets[n_stars];
+    for (int64_t i = 0; i < NE; ++i)
+        if (!(ivar[i] > 0.0) || !std::isfinite(ivar[i]) || !std::isfinite(t[i]) ||
+            !std::isfinite(rv[i]))
+            return fail(JOKER_EINVAL, "epoch %lld: ivar must be positive and finite, t and rv finite",
+                        (long long)i);
+    std::vector<StarRec> recs(n_stars);
+    std::vector<double> ep64((size_t)NE * REC64, 0.0);
+    std::vector<float> ep32((size_t)NE * REC32, 0.0f);
+    const long double LOG2PI = logl(2.0L * 3.141592653589793238462643383279502884L);
+    for (int k = 0; k < n_stars; ++k) {
+        const double *muk = mu + (size_t)k * L, *lamk = lambda + (size_t)k * L;
+        const double *kp = k_prior + (size_t)k * 4;
+        for (int j = 0; j < L; ++j)
+            if (!(lamk[j] > 0.0) && !(j == 0 && kp[0] != 0.0))
+                return fail(JOKER_EINVAL, "star %d: prior variance lambda[%d] must be > 0", k, j);
+        if (kp[0] != 0.0 && !(kp[1] > 0.0 && kp[2] > 0.0 && kp[3] > 0.0))
+            return fail(JOKER_EINVAL, "star %d: scaled K prior needs sigma_K0, P0, max_K > 0", k);
+        StarRec &r = recs[k];
+        memset(&r, 0, sizeof r);
+        const int64_t e0 = epoch_offsets[k];
+        const int n = (int)(epoch_offsets[k + 1] - e0);
+        r.epoch_off = (int32_t)e0;
+        r.n_epochs = n;
+        r.k_scaled = kp[0] != 0.0;
+        r.mu0 = muk[0];
+        r.lam0 = lamk[0];
+        r.sigK0sq = kp[1] * kp[1];
+        r.P0 = kp[2];
+        r.maxK2 = kp[3] * kp[3];
+        r.log_kscale = r.k_scaled ? std::log(r.sigK0sq) + 2.0 / 3.0 * std::log(r.P0) : 0.0;
+        r.log_maxK2 = r.k_scaled ? std::log(r.maxK2) : 0.0;
+        for (int j = 0; j < L; ++j) r.lam[j] = lamk[j];
+        // sums in long double
+        std::vector<long double> C(T * T, 0.0L), c(T, 0.0L), Cinv(T * T, 0.0L);
+        long double Syy = 0.0L, slog_ivar = 0.0L, slog_lam = 0.0L;
+        for (int j = 1; j < L; ++j) slog_lam += logl((long double)lamk[j]);
+        for (int i = 0; i < n; ++i) {
+            const int64_t g = e0 + i;
+            const double dt = t[g] - t_ref[k];
+            long double yp = rv[g];
+            for (int j = 1; j < L; ++j) yp -= (long double)muk[j] * trend_M[g * T + (j - 1)];
+            const long double w = ivar[g];
+            Syy += w * yp * yp;
+            slog_ivar += logl(w);
+            for (int j = 0; j < T; ++j) {
+                const long double Tj = trend_M[g * T + j];
+                c[j] += w * Tj * yp;
+                for (int m = 0; m < T; ++m) C[j * T + m] += w * Tj * trend_M[g * T + m];
+            }
+            // FP64 record: dt, y', ivar, T_1..T_{L-1}
+            double *r64 = &ep64[(size_t)g * REC64];
+            r64[0] = dt;
+            r64[1] = (double)yp;
+            r64[2] = ivar[g];
+            for (int j = 0; j < T; ++j) r64[3 + j] = trend_M[g * T + j];
+            // mixed record
+            float *r32 = &ep32[(size_t)g * REC32];
+            split_ff(dt, r32[0], r32[1]);
+            if (jitter_mode == JOKER_JITTER_REFERENCE) {
+                split_ff(ivar[g], r32[2], r32[3]);
+                split_ff((double)(w * yp), r32[4], r32[5]);
+                for (int j = 0; j < T; ++j)
+                    split_ff((double)(w * (long double)trend_M[g * T + j]), r32[6 + 2 * j],
+                             r32[7 + 2 * j]);
+            } else {
+                r32[2] = (float)ivar[g];
+                r32[3] = 0.0f;
+                split_ff((double)yp, r32[4], r32[5]);
+                for (int j = 0; j < T; ++j)
+                    split_ff(trend_M[g * T + j], r32[6 + 2 * j], r32[7 + 2 * j]);
+            }
+        }
+        for (int j = 0; j < T; ++j) C[j * T + j] += 1.0L / (long double)lamk[j + 1];
+        long double logdetC = 0.0L;
+        if (T > 0 && !spd_inverse(T, C.data(), Cinv.data(), logdetC))
+            return fail(JOKER_EINVAL, "star %d: trend block of the linear system is not positive definite", k);
+        long double cCc = 0.0L;
+        for (int j = 0; j < T; ++j) {
+            long double v = 0.0L;
+            for (int m = 0; m < T; ++m) v += Cinv[j * T + m] * c[m];
+            r.cC[j + 1] = (double)v;
+            cCc += c[j] * v;
+            for (int m = 0; m < T; ++m) r.Cinv[(j + 1) * MAXL + (m + 1)] = (double)Cinv[j * T + m];
+        }
+        r.chi2_0 = (double)(Syy - cCc);
+        r.logdet_const = (double)(n * LOG2PI - slog_ivar + slog_lam + logdetC);
+        r.log_norm_rest = (double)(n * LOG2PI + slog_lam);
+        r.sum_log_ivar = (double)slog_ivar;
+    }
+    std::vector<int> order(n_stars);
+    for (int k = 0; k < n_stars; ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return recs[a].n_epochs > recs[b].n_epochs;
+    });
+
+    joker_stars *s = new joker_stars();
+    s->n_stars = n_stars;
+    s->L = L;
+    s->jitter = jitter_mode;
+    s->max_epochs = max_ep;
+    s->total_epochs = NE;
+    s->off.assign(epoch_offsets, epoch_offsets + n_stars + 1);
+    auto cleanup = [&]() { joker_stars_destroy(s); };
+    cudaError_t e;
+    if ((e = cudaMalloc(&s->d_stars, sizeof(StarRec) * n_stars)) != cudaSuccess ||
+        (e = cudaMalloc(&s->d_ep64, sizeof(double) * ep64.size())) != cudaSuccess ||
+        (e = cudaMalloc(&s->d_ep32, sizeof(float) * ep32.size())) != cudaSuccess ||
+        (e = cudaMalloc(&s->d_queue, sizeof(int) * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&s->d_order, sizeof(int) * n_stars)) != cudaSuccess) {
+        cleanup();
+        return fail(JOKER_ENOMEM, "joker_stars_create: cudaMalloc: %s", cudaGetErrorString(e));
+    }
+    if ((e = cudaMemcpy(s->d_stars, recs.data(), sizeof(StarRec) * n_stars,
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(s->d_ep64, ep64.data(), sizeof(double) * ep64.size(),
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(s->d_ep32, ep32.data(), sizeof(float) * ep32.size(),
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(s->d_order, order.data(), sizeof(int) * n_stars,
+                        cudaMemcpyHostToDevice)) != cudaSuccess) {
+        cleanup();
+        return fail(JOKER_ECUDA, "joker_stars_create: cudaMemcpy: %s", cudaGetErrorString(e));
+    }
+    *out = s;
+    return JOKER_OK;
+}
+
+extern "C" int joker_stars_destroy(joker_stars *s) {
+    if (!s) return JOKER_OK;
+    cudaFree(s->d_stars);
+    cudaFree(s->d_ep64);
+    cudaFree(s->d_ep32);
+    cudaFree(s->d_queue);
+    cudaFree(s->d_order);
+    delete s;
+    return JOKER_OK;
+}
+
+extern "C" int joker_stars_info(const joker_stars *s, int *n_stars, int *n_linear,
+                                int64_t *total_epochs, int *max_epochs) {
+    if (!s) return fail(JOKER_EINVAL, "joker_stars_info: NULL handle");
+    if (n_stars) *n_stars = s->n_stars;
+    if (n_linear) *n_linear = s->L;
+    if (total_epochs) *total_epochs = s->total_epochs;
+    if (max_epochs) *max_epochs = s->max_epochs;
+    return JOKER_OK;
+}
+
+// ---------------------------------------------------------------- prior cache
+extern "C" int joker_cache_create(joker_cache **out, int64_t capacity) {
+    if (!out) return fail(JOKER_EINVAL, "joker_cache_create: out is NULL");
+    *out = nullptr;
+    if (capacity <= 0) return fail(JOKER_EINVAL, "joker_cache_create: capacity must be > 0");
+    joker_cache *c = new joker_cache();
+    c->cap = capacity;
+    cudaError_t e;
+    const size_t n = (size_t)capacity;
+    if ((e = cudaMalloc(&c->P, 8 * n)) != cudaSuccess || (e = cudaMalloc(&c->E, 8 * n)) != cudaSuccess ||
+        (e = cudaMalloc(&c->OM, 8 * n)) != cudaSuccess || (e = cudaMalloc(&c->M0, 8 * n)) != cudaSuccess ||
+        (e = cudaMalloc(&c->S, 8 * n)) != cudaSuccess ||
+        (e = cudaMalloc(&c->mx_a, 16 * n)) != cudaSuccess ||
+        (e = cudaMalloc(&c->mx_b, 16 * n)) != cudaSuccess ||
+        (e = cudaMalloc(&c->mx_s2, 4 * n)) != cudaSuccess) {
+        joker_cache_destroy(c);
+        return fail(JOKER_ENOMEM, "joker_cache_create(%lld): %s", (long long)capacity,
+                    cudaGetErrorString(e));
+    }
+    *out = c;
+    return JOKER_OK;
+}
+
+extern "C" int joker_cache_destroy(joker_cache *c) {
+    if (!c) return JOKER_OK;
+    cudaFree(c->P); cudaFree(c->E); cudaFree(c->OM); cudaFree(c->M0); cudaFree(c->S);
+    cudaFree(c->mx_a); cudaFree(c->mx_b); cudaFree(c->mx_s2);
+    delete c;
+    return JOKER_OK;
+}
+
+extern "C" int64_t joker_cache_capacity(const joker_cache *c) { return c ? c->cap : -1; }
+
+extern "C" int joker_cache_load(joker_cache *c, const double *d_chunk, int64_t n, int64_t row0,
+                                void *stream) {
+    if (!c || (!d_chunk && n > 0)) return fail(JOKER_EINVAL, "joker_cache_load: NULL argument");
+    if (n < 0 || row0 < 0 || row0 + n > c->cap)
+        return fail(JOKER_ERANGE, "joker_cache_load: rows [%lld, %lld) exceed capacity %lld",
+                    (long long)row0, (long long)(row0 + n), (long long)c->cap);
+    CUDA_TRY(launch_prepare(d_chunk, n, row0, c->P, c->E, c->OM, c->M0, c->S, c->mx_a, c->mx_b,
+                            c->mx_s2, (cudaStream_t)stream));
+    return JOKER_OK;
+}
+
+// ---------------------------------------------------------------- likelihood
+static int run_lnl(const joker_stars *s, int precision, LnlArgs a, int block,
+                   cudaStream_t st) {
+    CUDA_TRY(cudaMemsetAsync(s->d_queue, 0, sizeof(int), st));
+    CUDA_TRY(launch_lnl(precision, s->L, s->jitter == JOKER_JITTER_APPLIED, a, block, st));
+    return JOKER_OK;
+}
+
+extern "C" int joker_batch_marginal_ln_likelihood(const joker_stars *s, int star,
+                                                  const double *d_chunk, int64_t n_samples,
+                                                  double *d_lnl, void *stream) {
+    if (!s) return fail(JOKER_EINVAL, "joker_batch_marginal_ln_likelihood: NULL handle");
+    if (star < 0 || star >= s->n_stars)
+        return fail(JOKER_EINVAL, "star %d outside [0, %d)", star, s->n_stars);
+    if (n_samples < 0) return fail(JOKER_EINVAL, "n_samples must be >= 0");
+    if (n_samples == 0) return JOKER_OK;
+    if (!d_chunk || !d_lnl) return fail(JOKER_EINVAL, "NULL device pointer");
+    LnlArgs a;
+    memset(&a, 0, sizeof a);
+    a.stars = s->d_stars;
+    a.ep64 = s->d_ep64;
+    a.ep32 = s->d_ep32;
+    a.P = d_chunk; a.e = d_chunk + 1; a.om = d_chunk + 2; a.M0 = d_chunk + 3; a.s = d_chunk + 4;
+    a.stride = 5;
+    a.queue = s->d_queue;
+    a.lnl = d_lnl;
+    a.star0 = star;
+    a.n_sel = 1;
+    a.row0 = 0;
+    a.count = n_samples;
+    a.ld = n_samples;
+    a.chunk = 1024;
+    a.ips = (n_samples + a.chunk - 1) / a.chunk;
+    a.n_items = (int)std::min<int64_t>(a.ips, INT32_MAX);
+    if (a.ips > INT32_MAX) return fail(JOKER_ERANGE, "n_samples too large for one call");
+    return run_lnl(s, JOKER_FP64, a, 128, (cudaStream_t)stream);
+}
+
+extern "C" int joker_lnl(const joker_stars *s, const joker_cache *c, int star0, int n_sel,
+                         int64_t row0, int64_t count, int precision, double *d_lnl, int64_t ld,
+                         uint64_t *d_max_key, int block, int64_t chunk, void *stream) {
+    if (!s || !c) return fail(JOKER_EINVAL, "joker_lnl: NULL handle");
+    if (precision != JOKER_FP64 && precision != JOKER_MIXED && precision != JOKER_MIXED_ACCURATE)
+        return fail(JOKER_EINVAL, "joker_lnl: unknown precision %d", precision);
+    if (star0 < 0 || n_sel < 0 || star0 + n_sel > s->n_stars)
+        return fail(JOKER_EINVAL, "joker_lnl: stars [%d, %d) outside [0, %d)", star0,
+                    star0 + n_sel, s->n_stars);
+    if (row0 < 0 || count < 0 || row0 + count > c->cap)
+        return fail(JOKER_ERANGE, "joker_lnl: rows [%lld, %lld) outside the cache (%lld)",
+                    (long long)row0, (long long)(row0 + count), (long long)c->cap);
+    if (n_sel == 0 || count == 0) return JOKER_OK;
+    if (!d_lnl) return fail(JOKER_EINVAL, "joker_lnl: d_lnl is NULL");
+    if (ld < count) return fail(JOKER_EINVAL, "joker_lnl: ld < count");
+    if (block == 0) block = 128;
+    if (block != 128) return fail(JOKER_EINVAL, "joker_lnl: block must be 128");
+    if (chunk <= 0) chunk = 1024;
+    if (chunk % block) return fail(JOKER_EINVAL, "joker_lnl: chunk must be a multiple of block");
+    LnlArgs a;
+    memset(&a, 0, sizeof a);
+    a.stars = s->d_stars;
+    a.ep64 = s->d_ep64;
+    a.ep32 = s->d_ep32;
+    a.P = c->P; a.e = c->E; a.om = c->OM; a.M0 = c->M0; a.s = c->S;
+    a.stride = 1;
+    a.mx_a = c->mx_a; a.mx_b = c->mx_b; a.mx_s2 = c->mx_s2;
+    a.queue = s->d_queue;
+    a.lnl = d_lnl;
+    a.max_key = (unsigned long long *)d_max_key;
+    a.star0 = star0;
+    a.n_sel = n_sel;
+    a.row0 = row0;
+    a.count = count;
+    a.ld = ld;
+    a.chunk = (int)chunk;
+    a.ips = (count + chunk - 1) / chunk;
+    a.order = (star0 == 0 && n_sel == s->n_stars) ? s->d_order : nullptr;
+    const int64_t items = a.ips * n_sel;
+    if (items > INT32_MAX) return fail(JOKER_ERANGE, "joker_lnl: too many work items; use a larger chunk");
+    a.n_items = (int)items;
+    return run_lnl(s, precision, a, block, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------- acceptance
+
+
+static int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
+
+extern "C" int64_t joker_accept_workspace(const joker_accept_seg *segs, int n_segs) {
+    if (!segs || n_segs <= 0) return 0;
+    const int64_t nb = accept_blocks(segs, n_segs, nullptr);
+    return align256(sizeof(joker_accept_seg) * (int64_t)n_segs) +
+           align256(8 * (int64_t)(n_segs + 1)) + align256(8 * nb) + align256(4 * 256 * nb);
+}
+
+extern "C" int joker_accept(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
+                            const uint64_t *d_max_key, int u_source, const double *d_u,
+                            int64_t *d_out_idx, double *d_out_lnl, int64_t *d_count,
+                            void *d_work, int64_t work_bytes, void *stream) {
+    if (n_segs <= 0) return JOKER_OK;
+    if (!segs || !d_lnl || !d_max_key || !d_out_idx || !d_count || !d_work)
+        return fail(JOKER_EINVAL, "joker_accept: NULL argument");
+    if (u_source != JOKER_U_ARRAY && u_source != JOKER_U_PCG64)
+        return fail(JOKER_EINVAL, "joker_accept: unknown u_source %d", u_source);
+    if (u_source == JOKER_U_ARRAY && !d_u) return fail(JOKER_EINVAL, "joker_accept: d_u is NULL");
+    for (int i = 0; i < n_segs; ++i)
+        if (segs[i].n < 0 || segs[i].max_out < 0 || segs[i].lnl_off < 0 || segs[i].max_slot < 0)
+            return fail(JOKER_EINVAL, "joker_accept: segment %d has a negative field", i);
+    const int64_t need = joker_accept_workspace(segs, n_segs);
+    if (work_bytes < need)
+        return fail(JOKER_EINVAL, "joker_accept: workspace %lld < %lld bytes", (long long)work_bytes,
+                    (long long)need);
+    std::vector<int64_t> base(n_segs + 1);
+    const int64_t nb = accept_blocks(segs, n_segs, base.data());
+    if (nb > 0x7fffffffLL) return fail(JOKER_ERANGE, "joker_accept: too many samples in one call");
+    char *w = (char *)d_work;
+    joker_accept_seg *d_segs = (joker_accept_seg *)w;
+    w += align256(sizeof(joker_accept_seg) * (int64_t)n_segs);
+    int64_t *d_base = (int64_t *)w;
+    w += align256(8 * (int64_t)(n_segs + 1));
+    int64_t *d_blk = (int64_t *)w;
+    w += align256(8 * nb);
+    uint32_t *d_words = (uint32_t *)w;
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemcpyAsync(d_segs, segs, sizeof(joker_accept_seg) * n_segs, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_base, base.data(), 8 * (n_segs + 1), cudaMemcpyHostToDevice, st));
+    AcceptArgs a;
+    a.segs = d_segs;
+    a.blk_base = d_base;
+    a.n_segs = n_segs;
+    a.lnl = d_lnl;
+    a.max_key = (const unsigned long long *)d_max_key;
+    a.u_source = u_source;
+    a.u = d_u;
+    a.words = d_words;
+    a.blk_count = d_blk;
+    a.out_idx = d_out_idx;
+    a.out_lnl = d_out_lnl;
+    a.count = d_count;
+    // pageable host sources are staged before cudaMemcpyAsync returns
+    CUDA_TRY(launch_accept(a, nb, st));
+    return JOKER_OK;
+}

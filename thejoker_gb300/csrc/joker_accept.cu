@@ -1,0 +1,183 @@
+// Acceptance pass of libjoker_gb300: the reference's rejection step
+//   uu = rng.uniform(size=len(lls))
+//   good = np.where(np.exp(lls - lls.max()) > uu)[0][:max_posterior_samples]
+// (thejoker/likelihood_helpers.py:107-109, multiproc_helpers.py:256-258),
+// applied to many independent segments (stars / sample runs) at once.
+//
+// Three kernels, all bandwidth-bound scans over the ln L buffer:
+//   mark  -- one warp per 1024 samples, lanes on consecutive samples (coalesced
+//            loads); the test of 32 samples becomes one 32-bit word by ballot;
+//            per-CTA accepted counts.
+//   scan  -- exclusive scan of the per-CTA counts of each segment.
+//   emit  -- per CTA, an in-block scan of word popcounts gives each accepted
+//            sample its rank; indices are written in ascending order, the
+//            first max_out of them only.
+// The uniforms come either from a device array or from numpy's PCG64 stream,
+// regenerated here from the generator state (joker_math.cuh), so the draws are
+// bit-identical to rng.uniform() on the host.
+#include "joker_internal.cuh"
+#include "joker_math.cuh"
+
+namespace joker {
+
+constexpr int ACC_THREADS = 256;                       // 8 warps
+constexpr int64_t ACC_BLOCK = ACC_THREADS * 32;        // samples per CTA
+
+
+__device__ __forceinline__ int find_seg(const int64_t *blk_base, int n_segs, int64_t b) {
+    int lo = 0, hi = n_segs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (blk_base[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// exp(d) > u, evaluated as numpy does in FP64 but with an FP32 pre-test that
+// settles all but the samples within 1e-4 of the boundary.
+__device__ __forceinline__ bool accept_test(double d, double u) {
+    if (!(d > -40.0)) {
+        // exp(d) <= 4.3e-18 < 2^-53 <= any nonzero u; only u == 0 can pass
+        return (u == 0.0) && (exp(d) > 0.0);
+    }
+    const float lf = __logf((float)u);
+    const float df = (float)d;
+    if (u > 0.0) {
+        if (df > lf + 1e-4f) return true;
+        if (df < lf - 1e-4f) return false;
+    }
+    return exp(d) > u;
+}
+
+__global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) {
+    const int64_t gblk = blockIdx.x;
+    const int si = find_seg(a.blk_base, a.n_segs, gblk);
+    const joker_accept_seg sg = a.segs[si];
+    const int64_t blk = gblk - a.blk_base[si];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t wbase = blk * ACC_BLOCK + (int64_t)warp * 1024;  // first sample of this warp
+    const double mx = key_to_double(a.max_key[sg.max_slot]);
+    const double *lnl = a.lnl + sg.lnl_off;
+
+    u128 st = 0, inc = 0, Am = 1, Cp = 0;
+    if (a.u_source == JOKER_U_PCG64) {
+        const u128 s0 = ((u128)sg.pcg_state_hi << 64) | (u128)sg.pcg_state_lo;
+        inc = ((u128)sg.pcg_inc_hi << 64) | (u128)sg.pcg_inc_lo;
+        // draw at position p is output(state after p + 1 steps)
+        st = pcg_advance(s0, inc, (uint64_t)(wbase + lane + 1));
+        // affine map for 32 steps: s -> Am s + Cp
+        u128 cm = pcg_mult(), cp = inc;
+#pragma unroll
+        for (int b = 0; b < 5; ++b) { cp = (cm + 1) * cp; cm *= cm; }
+        Am = cm;
+        Cp = cp;
+    }
+    uint32_t my_word = 0;
+    int my_count = 0;
+    for (int k = 0; k < 32; ++k) {
+        const int64_t i = wbase + (int64_t)k * 32 + lane;
+        bool keep = false;
+        if (i < sg.n) {
+            double u;
+            if (a.u_source == JOKER_U_PCG64) u = pcg_uniform(pcg_output(st));
+            else u = a.u[sg.u_off + i];
+            keep = accept_test(lnl[i] - mx, u);
+        }
+        if (a.u_source == JOKER_U_PCG64) st = Am * st + Cp;
+        const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+        if (lane == k) my_word = bal;
+        my_count += __popc(bal);
+    }
+    // word index within the CTA: warp * 32 + lane
+    a.words[gblk * ACC_THREADS + threadIdx.x] = my_word;
+    __shared__ int s_cnt[ACC_THREADS / 32];
+    if (lane == 0) s_cnt[warp] = my_count;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t c = 0;
+        for (int w = 0; w < ACC_THREADS / 32; ++w) c += s_cnt[w];
+        a.blk_count[gblk] = c;
+    }
+}
+
+// One CTA per segment: exclusive scan of that segment's per-CTA counts.
+__global__ void __launch_bounds__(ACC_THREADS) accept_scan_kernel(AcceptArgs a) {
+    const int si = blockIdx.x;
+    const int64_t b0 = a.blk_base[si], nb = a.blk_base[si + 1] - b0;
+    __shared__ int64_t s_part[ACC_THREADS];
+    int64_t carry = 0;
+    for (int64_t base = 0; base < nb; base += ACC_THREADS) {
+        const int64_t b = base + threadIdx.x;
+        const int64_t v = (b < nb) ? a.blk_count[b0 + b] : 0;
+        s_part[threadIdx.x] = v;
+        __syncthreads();
+        // Hillis-Steele inclusive scan
+        for (int off = 1; off < ACC_THREADS; off <<= 1) {
+            const int64_t add = (threadIdx.x >= off) ? s_part[threadIdx.x - off] : 0;
+            __syncthreads();
+            s_part[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (b < nb) a.blk_count[b0 + b] = carry + s_part[threadIdx.x] - v;
+        const int64_t tot = s_part[ACC_THREADS - 1];
+        __syncthreads();
+        carry += tot;
+    }
+    if (threadIdx.x == 0) a.count[si] = carry;
+}
+
+__global__ void __launch_bounds__(ACC_THREADS) accept_emit_kernel(AcceptArgs a) {
+    const int64_t gblk = blockIdx.x;
+    const int si = find_seg(a.blk_base, a.n_segs, gblk);
+    const joker_accept_seg sg = a.segs[si];
+    const int64_t blk = gblk - a.blk_base[si];
+    const int64_t boff = a.blk_count[gblk];
+    if (boff >= sg.max_out) return;
+    const uint32_t word = a.words[gblk * ACC_THREADS + threadIdx.x];
+    const int c = __popc(word);
+    __shared__ int s_scan[ACC_THREADS];
+    s_scan[threadIdx.x] = c;
+    __syncthreads();
+    for (int off = 1; off < ACC_THREADS; off <<= 1) {
+        const int add = (threadIdx.x >= off) ? s_scan[threadIdx.x - off] : 0;
+        __syncthreads();
+        s_scan[threadIdx.x] += add;
+        __syncthreads();
+    }
+    int64_t pos = boff + s_scan[threadIdx.x] - c;
+    const int64_t first = blk * ACC_BLOCK + (int64_t)threadIdx.x * 32;
+    uint32_t wm = word;
+    while (wm && pos < sg.max_out) {
+        const int b = __ffs(wm) - 1;
+        wm &= wm - 1;
+        const int64_t i = first + b;
+        a.out_idx[sg.out_off + pos] = sg.idx_base + i;
+        if (a.out_lnl) a.out_lnl[sg.out_off + pos] = a.lnl[sg.lnl_off + i];
+        ++pos;
+    }
+}
+
+int64_t accept_blocks(const joker_accept_seg *segs, int n_segs, int64_t *blk_base_host) {
+    int64_t tot = 0;
+    for (int s = 0; s < n_segs; ++s) {
+        if (blk_base_host) blk_base_host[s] = tot;
+        tot += (segs[s].n + ACC_BLOCK - 1) / ACC_BLOCK;
+    }
+    if (blk_base_host) blk_base_host[n_segs] = tot;
+    return tot;
+}
+
+cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st) {
+    if (total_blocks > 0) {
+        accept_mark_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    accept_scan_kernel<<<a.n_segs, ACC_THREADS, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || total_blocks == 0) return e;
+    accept_emit_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace joker

@@ -1,0 +1,127 @@
+// Internal types and device math shared by the kernels of libjoker_gb300.
+#pragma once
+#include <cstdint>
+#include <cstring>
+#include <cuda_runtime.h>
+#include "../../include/joker_gb300.h"
+
+namespace joker {
+
+constexpr int MAXL = JOKER_MAX_LINEAR;
+constexpr int TILE = 256;          // epochs staged in shared memory at a time
+constexpr int REC32 = 16;          // floats per epoch record of the mixed kernel
+constexpr int REC64 = 8;           // doubles per epoch record of the FP64 kernel
+
+// Per-star constants, built on the host in FP64 (joker_abi.cu).  Index 0 of
+// the linear parameters is K; 1.. are v0, the offsets and the trend terms.
+struct alignas(16) StarRec {
+    int32_t epoch_off;     // first epoch in the packed per-epoch arrays
+    int32_t n_epochs;
+    int32_t k_scaled;      // FixedCompanionMass K prior
+    int32_t pad;
+    double mu0;            // K prior mean
+    double lam0;           // K prior variance (not scaled)
+    double sigK0sq;        // sigma_K0^2
+    double P0;             // reference period of the scaled K prior
+    double maxK2;          // max_K^2
+    double log_kscale;     // log(sigma_K0^2 * P0^(2/3))
+    double log_maxK2;      // log(max_K^2)
+    // Sample-independent parts, jitter ignored.  With y'_n = y_n - sum_{j>=1}
+    // mu_j T_jn, W = diag(ivar) and C = Lambda_T^-1 + T W T^T (the trend block):
+    double chi2_0;              // y'^T W y' - c^T C^-1 c,  c = T W y'
+    double logdet_const;        // N log 2pi - sum log ivar + sum_{j>=1} log lambda_j + log det C
+    double cC[MAXL];            // C^-1 c          (entries 1..L-1)
+    double Cinv[MAXL * MAXL];   // C^-1            (entries 1..L-1)
+    // Jitter applied: everything is per sample.
+    double lam[MAXL];           // prior variances (lam[0] = lam0)
+    double log_norm_rest;       // N log 2pi + sum_{j>=1} log lambda_j
+    double sum_log_ivar;        // sum log ivar
+};
+
+// One unit of the persistent likelihood kernels: `count` samples of star
+// `star` starting at cache row `row0`; ln L goes to lnl[out_off + i].
+struct alignas(16) WorkItem {
+    int32_t star;
+    int32_t count;
+    int64_t row0;
+    int64_t out_off;
+    int32_t max_slot;
+    int32_t pad;
+};
+
+struct LnlArgs {
+    const StarRec *stars;
+    const double *ep64;      // FP64 epoch records: [epoch][REC64]
+    const float *ep32;       // mixed epoch records: [epoch][REC32]
+    // FP64 sample columns (stride in doubles between consecutive samples)
+    const double *P, *e, *om, *M0, *s;
+    int64_t stride;
+    // prepared mixed cache
+    const float4 *mx_a;      // (1/P hi, 1/P lo, M0/2pi hi, M0/2pi lo)
+    const float4 *mx_b;      // (e, cos w, sin w, log g) with g = P^(-2/3) / (1 - e^2)
+    const float *mx_s2;      // s^2
+    // Work items: explicit (items != nullptr) or implicit -- stars
+    // [star0, star0 + n_sel) x rows [row0, row0 + count) in chunks of `chunk`,
+    // star-major, stars visited in `order` (relative indices) when given.
+    const WorkItem *items;
+    int n_items;
+    int star0, n_sel, chunk;
+    int64_t row0, count, ld, ips;
+    const int *order;
+    int *queue;              // dynamic work counter, zeroed before launch
+    double *lnl;
+    unsigned long long *max_key;
+};
+
+__device__ __forceinline__ WorkItem get_item(const LnlArgs &a, int it) {
+    if (a.items) return a.items[it];
+    WorkItem w;
+    const int k = (int)(it / a.ips);
+    const int64_t c = (int64_t)it - (int64_t)k * a.ips;
+    const int sk = a.order ? a.order[k] : k;
+    w.star = a.star0 + sk;
+    w.row0 = a.row0 + c * a.chunk;
+    const int64_t rem = a.count - c * a.chunk;
+    w.count = (int)(rem < a.chunk ? rem : a.chunk);
+    w.out_off = (int64_t)sk * a.ld + c * a.chunk;
+    w.max_slot = sk;
+    w.pad = 0;
+    return w;
+}
+
+struct AcceptArgs {
+    const joker_accept_seg *segs;
+    const int64_t *blk_base;     // n_segs + 1 prefix of CTA counts
+    int n_segs;
+    const double *lnl;
+    const unsigned long long *max_key;
+    int u_source;
+    const double *u;
+    uint32_t *words;             // accepted masks, one word per 32 samples
+    int64_t *blk_count;          // per CTA accepted count, then its exclusive offset
+    int64_t *out_idx;
+    double *out_lnl;
+    int64_t *count;
+};
+
+// ---------------------------------------------------------------- helpers
+__host__ __device__ __forceinline__ unsigned long long double_to_key(double x) {
+#ifdef __CUDA_ARCH__
+    long long b = __double_as_longlong(x);
+#else
+    long long b; memcpy(&b, &x, 8);
+#endif
+    if (x != x) return 0xFFFFFFFFFFFFFFFFull;  // NaN dominates, as numpy's max
+    return (b < 0) ? ~(unsigned long long)b : ((unsigned long long)b | 0x8000000000000000ull);
+}
+
+__host__ __device__ __forceinline__ double key_to_double(unsigned long long k) {
+    unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double x; memcpy(&x, &b, 8); return x;
+#endif
+}
+
+}  // namespace joker

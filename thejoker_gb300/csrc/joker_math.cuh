@@ -1,0 +1,170 @@
+// Device math for the likelihood kernels: Kepler solvers (FP64 and FP32),
+// float-float (double-single) arithmetic, and numpy's PCG64 generator.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace joker {
+
+constexpr double PI_D = 3.141592653589793238462643383279502884;
+constexpr double TWO_PI_D = 6.283185307179586476925286766559005768;
+constexpr double TWO_PI_HI_D = 6.283185307179586;          // nearest double to 2 pi
+constexpr double TWO_PI_LO_D = 2.4492935982947064e-16;     // 2 pi - TWO_PI_HI_D
+constexpr double INV_TWO_PI_D = 0.15915494309189533577;
+constexpr float PI_F = 3.14159265358979f;
+constexpr float TWO_PI_HI_F = 6.28318548202514648f;         // nearest float to 2 pi
+constexpr float TWO_PI_LO_F = -1.7484556e-07f;              // 2 pi - TWO_PI_HI_F
+// Markley (1995) starter: alpha = (3 pi^2 + 1.6 pi (pi - |M|) / (1 + e)) / (pi^2 - 6)
+constexpr double MK_A0_D = 3.0 * PI_D * PI_D / (PI_D * PI_D - 6.0);
+constexpr double MK_A1_D = 1.6 * PI_D / (PI_D * PI_D - 6.0);
+
+// ----------------------------------------------------------------- FP64 Kepler
+// Eccentric anomaly by Markley's non-iterative method (F. L. Markley, 1995,
+// "Kepler equation solver", Celestial Mechanics and Dynamical Astronomy 63,
+// 101-111): a cubic-root starter followed by one fifth-order Householder-type
+// correction.  M must lie in [-pi, pi], 0 <= e < 1.  Returns sin E and cos E;
+// the correction is applied by rotating (sin E1, cos E1) through the small
+// angle delta with its Taylor series (|delta| < 4e-4).
+__device__ __forceinline__ void kepler_sincos_f64(double M, double e, double &sinE,
+                                                  double &cosE) {
+    const double x = fabs(M);
+    const double ome = 1.0 - e;
+    const double alpha = MK_A0_D + MK_A1_D * (PI_D - x) / (1.0 + e);
+    const double d = 3.0 * ome + alpha * e;
+    const double q = 2.0 * alpha * d * ome - x * x;
+    const double r = 3.0 * alpha * d * (d - ome) * x + x * x * x;
+    double w = cbrt(fabs(r) + sqrt(q * q * q + r * r));
+    w = w * w;
+    const double E1 = (2.0 * r * w / (w * w + w * q + q * q) + x) / d;
+    double s1, c1;
+    sincos(E1, &s1, &c1);
+    const double f0 = E1 - e * s1 - x;
+    const double f1 = 1.0 - e * c1;
+    const double f2 = e * s1;
+    const double f3 = 1.0 - f1;
+    const double f4 = -f2;
+    const double d3 = -f0 / (f1 - 0.5 * f0 * f2 / f1);
+    const double d4 = -f0 / (f1 + 0.5 * d3 * f2 + d3 * d3 * f3 * (1.0 / 6.0));
+    const double d5 = -f0 / (f1 + 0.5 * d4 * f2 + d4 * d4 * f3 * (1.0 / 6.0) +
+                             d4 * d4 * d4 * f4 * (1.0 / 24.0));
+    const double dd = d5 * d5;
+    const double cd = 1.0 - dd * (0.5 - dd * (1.0 / 24.0 - dd * (1.0 / 720.0)));
+    const double sd = d5 * (1.0 - dd * (1.0 / 6.0 - dd * (1.0 / 120.0 - dd * (1.0 / 5040.0))));
+    const double sE = s1 * cd + c1 * sd;
+    cosE = c1 * cd - s1 * sd;
+    sinE = (M < 0.0) ? -sE : sE;
+}
+
+// --------------------------------------------------------- float-float helpers
+// Error-free transformations (Knuth two-sum, FMA two-product).  The _rn
+// intrinsics keep the compiler from contracting them into FMAs.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &err) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// acc (hi, lo) += (c_hi + c_lo) * m, with the product c_hi * m exact.
+__device__ __forceinline__ void ff_acc(float &hi, float &lo, float c_hi, float c_lo, float m) {
+    const float p = __fmul_rn(c_hi, m);
+    float pe = __fmaf_rn(c_hi, m, -p);
+    pe = __fmaf_rn(c_lo, m, pe);
+    float s, e;
+    two_sum(hi, p, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(e, pe));
+}
+
+// acc += (c_hi + c_lo), exact high part.
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float c_hi, float c_lo) {
+    float s, e;
+    two_sum(hi, c_hi, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(e, c_lo));
+}
+
+// (hi, lo) = a * b as an unevaluated sum, exact.
+__device__ __forceinline__ void two_prod(float a, float b, float &hi, float &lo) {
+    hi = __fmul_rn(a, b);
+    lo = __fmaf_rn(a, b, -hi);
+}
+
+__device__ __forceinline__ double ff_to_double(float hi, float lo) {
+    return (double)hi + (double)lo;
+}
+
+__device__ __forceinline__ float fast_rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// ----------------------------------------------------------------- FP32 Kepler
+// The same Markley starter in FP32, followed by one Halley step; the starter's
+// error (< 4e-4 rad) leaves a Halley residual far below FP32 resolution.
+// a1 = 1.6 pi / ((1 + e)(pi^2 - 6)) is a per-sample constant.  M in [-pi, pi].
+template <bool ACCURATE_SINCOS>
+__device__ __forceinline__ void kepler_sincos_f32(float M, float e, float ome, float a1,
+                                                  float &sinE, float &cosE) {
+    const float x = fabsf(M);
+    const float alpha = __fmaf_rn(a1, PI_F - x, (float)MK_A0_D);
+    const float d = __fmaf_rn(alpha, e, 3.0f * ome);
+    const float x2 = x * x;
+    const float ad = alpha * d;
+    const float q = __fmaf_rn(2.0f * ad, ome, -x2);
+    const float r = x * __fmaf_rn(3.0f * ad, d - ome, x2);
+    const float disc = __fmaf_rn(q * q, q, r * r);
+    const float sq = disc * rsqrtf(disc);
+    float w = exp2f(0.6666667f * __log2f(fabsf(r) + sq));
+    const float den3 = __fmaf_rn(w, w + q, q * q);
+    const float E1 = __fmaf_rn(x, den3, 2.0f * r * w) * fast_rcp(den3 * d);
+    float s1, c1;
+    if (ACCURATE_SINCOS) sincosf(E1, &s1, &c1);
+    else __sincosf(E1, &s1, &c1);
+    const float es = e * s1;
+    const float f0 = (E1 - x) - es;
+    const float f1 = __fmaf_rn(-e, c1, 1.0f);
+    // Halley: delta = -f0 f1 / (f1^2 - f0 f2 / 2)
+    const float delta = -f0 * f1 * fast_rcp(__fmaf_rn(f1, f1, -0.5f * f0 * es));
+    const float hd2 = 0.5f * delta * delta;
+    const float sE = __fmaf_rn(delta, c1, __fmaf_rn(-hd2, s1, s1));
+    cosE = __fmaf_rn(-delta, s1, __fmaf_rn(-hd2, c1, c1));
+    sinE = (M < 0.0f) ? -sE : sE;
+}
+
+// ------------------------------------------------------------------- PCG64
+// numpy's PCG64 (128-bit LCG, XSL-RR output; M. E. O'Neill, "PCG: A family of
+// simple fast space-efficient statistically good algorithms for random number
+// generation", 2014).  Generator.uniform draws one 64-bit output per double:
+// u = (x >> 11) * 2^-53.  The state is stepped before each output.
+typedef unsigned __int128 u128;
+__device__ __forceinline__ u128 pcg_mult() {
+    return ((u128)0x2360ED051FC65DA4ull << 64) | (u128)0x4385DF649FCCF645ull;
+}
+
+__device__ __forceinline__ u128 pcg_step(u128 s, u128 inc) { return s * pcg_mult() + inc; }
+
+__device__ __forceinline__ uint64_t pcg_output(u128 s) {
+    const unsigned rot = (unsigned)(s >> 122);
+    const uint64_t x = (uint64_t)(s >> 64) ^ (uint64_t)s;
+    return (x >> rot) | (x << ((64u - rot) & 63u));
+}
+
+// Advance an LCG by delta steps in O(log delta) (F. B. Brown, 1994, "Random
+// number generation with arbitrary strides", Trans. Am. Nucl. Soc. 71, 202).
+__device__ __forceinline__ u128 pcg_advance(u128 s, u128 inc, uint64_t delta) {
+    u128 cm = pcg_mult(), cp = inc, am = 1, ap = 0;
+    while (delta) {
+        if (delta & 1) { am *= cm; ap = ap * cm + cp; }
+        cp = (cm + 1) * cp;
+        cm *= cm;
+        delta >>= 1;
+    }
+    return am * s + ap;
+}
+
+__device__ __forceinline__ double pcg_uniform(uint64_t x) {
+    return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+}
+
+}  // namespace joker

@@ -1,0 +1,251 @@
+"""Device-side objects over the C ABI: star tables, the prior cache, the
+acceptance pass, and numpy-PCG64 state handling.  PyTorch supplies device
+memory and streams only; all arithmetic runs in libjoker_gb300."""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native as nat
+
+__all__ = ["StarTable", "PriorCache", "accept", "stream_handle", "pcg64_state",
+           "pcg64_advance_generator", "MaxKeys"]
+
+_MASK128 = (1 << 128) - 1
+_PCG_MULT = 0x2360ED051FC65DA44385DF649FCCF645
+
+
+def stream_handle(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class StarTable:
+    """Device-resident table of one or more stars (``joker_stars``), the
+    many-star form of CJokerHelper.__init__ (fast_likelihood.pyx:125-253).
+
+    ``stars`` is a list of dicts with keys t, rv, ivar, t_ref, trend_M (N x
+    (L-1)), mu, lam (L), k_prior (4: scaled, sigma_K0, P0, max_K).
+    """
+
+    def __init__(self, stars, jitter="reference"):
+        if not stars:
+            raise ValueError("no stars")
+        L = len(stars[0]["mu"])
+        off = np.zeros(len(stars) + 1, dtype=np.int64)
+        for k, s in enumerate(stars):
+            off[k + 1] = off[k] + len(s["t"])
+            if len(s["mu"]) != L or len(s["lam"]) != L:
+                raise ValueError("all stars must share n_linear")
+        cat = lambda key: _f64(np.concatenate([np.asarray(s[key], dtype=np.float64) for s in stars]))
+        t, rv, ivar = cat("t"), cat("rv"), cat("ivar")
+        t_ref = _f64([s["t_ref"] for s in stars])
+        if L > 1:
+            trend = _f64(np.concatenate([np.asarray(s["trend_M"], dtype=np.float64).reshape(len(s["t"]), L - 1)
+                                         for s in stars]))
+        else:
+            trend = np.zeros(1)
+        mu = _f64(np.stack([s["mu"] for s in stars]))
+        lam = _f64(np.stack([s["lam"] for s in stars]))
+        kp = _f64(np.stack([s["k_prior"] for s in stars]))
+        jm = {"reference": nat.JOKER_JITTER_REFERENCE, "applied": nat.JOKER_JITTER_APPLIED}[jitter]
+        torch.cuda.init()
+        h = ctypes.c_void_p()
+        nat.check(nat.lib().joker_stars_create(
+            ctypes.byref(h), len(stars), L, nat.lptr(off), nat.dptr(t), nat.dptr(rv),
+            nat.dptr(ivar), nat.dptr(t_ref), nat.dptr(trend), nat.dptr(mu), nat.dptr(lam),
+            nat.dptr(kp), jm), "joker_stars_create")
+        self._h = h
+        self.n_stars = len(stars)
+        self.n_linear = L
+        self.jitter = jitter
+        self.epoch_offsets = off
+        self.n_epochs = np.diff(off)
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("StarTable is closed")
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            nat.lib().joker_stars_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PriorCache:
+    """Device-resident prior cache (``joker_cache``): the packed (n, 5) samples
+    kept as FP64 columns plus the prepared form of the mixed kernel."""
+
+    def __init__(self, capacity):
+        torch.cuda.init()
+        h = ctypes.c_void_p()
+        nat.check(nat.lib().joker_cache_create(ctypes.byref(h), int(capacity)), "joker_cache_create")
+        self._h = h
+        self.capacity = int(capacity)
+        self.size = 0
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("PriorCache is closed")
+        return self._h
+
+    def load(self, chunk, row0=0, stream=None):
+        """Load rows [row0, row0 + len(chunk)) from a (n, 5) float64 array
+        (numpy or a CUDA tensor)."""
+        if isinstance(chunk, np.ndarray):
+            chunk = torch.from_numpy(_f64(chunk)).pin_memory().to("cuda", non_blocking=True)
+        if chunk.dtype != torch.float64 or chunk.dim() != 2 or chunk.shape[1] != 5:
+            raise ValueError("chunk must be float64 with shape (n, 5)")
+        chunk = chunk.contiguous()
+        n = chunk.shape[0]
+        nat.check(nat.lib().joker_cache_load(self.handle, ctypes.c_void_p(chunk.data_ptr()), n,
+                                             int(row0), stream_handle(stream)), "joker_cache_load")
+        self.size = max(self.size, int(row0) + n)
+        return self
+
+    @classmethod
+    def from_samples(cls, chunk, stream=None):
+        c = cls(len(chunk))
+        return c.load(chunk, 0, stream)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            nat.lib().joker_cache_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+PRECISIONS = {"fp64": nat.JOKER_FP64, "mixed": nat.JOKER_MIXED,
+              "mixed_accurate": nat.JOKER_MIXED_ACCURATE}
+
+
+class MaxKeys:
+    """Running maxima of ln L (order-preserving uint64 images) on the device."""
+
+    def __init__(self, n):
+        self.t = torch.zeros(int(n), dtype=torch.int64, device="cuda")
+
+    def ptr(self):
+        return ctypes.c_void_p(self.t.data_ptr())
+
+    def values(self):
+        keys = self.t.cpu().numpy().view(np.uint64)
+        return np.array([nat.lib().joker_key_to_double(int(k)) for k in keys])
+
+
+def lnl(stars, cache, out, precision="fp64", star0=0, n_sel=None, row0=0, count=None,
+        max_keys=None, chunk=0, stream=None):
+    """ln L of stars [star0, star0 + n_sel) over cache rows [row0, row0 + count)
+    into ``out`` (a float64 CUDA tensor of shape (n_sel, ld))."""
+    n_sel = stars.n_stars - star0 if n_sel is None else n_sel
+    count = cache.size - row0 if count is None else count
+    if out.dtype != torch.float64 or out.dim() != 2 or out.shape[0] < n_sel or out.shape[1] < count:
+        raise ValueError("out must be float64 with shape (n_sel, >= count)")
+    if not out.is_contiguous():
+        raise ValueError("out must be contiguous")
+    nat.check(nat.lib().joker_lnl(
+        stars.handle, cache.handle, int(star0), int(n_sel), int(row0), int(count),
+        PRECISIONS[precision], ctypes.c_void_p(out.data_ptr()), out.shape[1],
+        max_keys.ptr() if max_keys is not None else None, 0, int(chunk),
+        stream_handle(stream)), "joker_lnl")
+    return out
+
+
+# --------------------------------------------------------------------- PCG64
+def pcg64_state(rng):
+    """(state, inc) of a numpy Generator backed by PCG64, else None."""
+    bg = rng.bit_generator
+    st = bg.state
+    if st.get("bit_generator") != "PCG64":
+        return None
+    return int(st["state"]["state"]), int(st["state"]["inc"])
+
+
+def _pcg_advance(state, inc, delta):
+    cm, cp, am, ap = _PCG_MULT, inc, 1, 0
+    while delta:
+        if delta & 1:
+            am = (am * cm) & _MASK128
+            ap = (ap * cm + cp) & _MASK128
+        cp = ((cm + 1) * cp) & _MASK128
+        cm = (cm * cm) & _MASK128
+        delta >>= 1
+    return (am * state + ap) & _MASK128
+
+
+def pcg64_advance_generator(rng, n_draws):
+    """Move a PCG64 Generator forward exactly as ``rng.uniform(size=n_draws)``
+    would, leaving its 32-bit buffer untouched."""
+    bg = rng.bit_generator
+    st = bg.state
+    s, inc = int(st["state"]["state"]), int(st["state"]["inc"])
+    st["state"]["state"] = _pcg_advance(s, inc, int(n_draws))
+    bg.state = st
+
+
+def pcg64_fields(state, inc, offset=0):
+    """Split a PCG64 state advanced by ``offset`` draws for joker_accept_seg."""
+    s = _pcg_advance(state, inc, int(offset)) if offset else state
+    return s >> 64, s & ((1 << 64) - 1), inc >> 64, inc & ((1 << 64) - 1)
+
+
+# ----------------------------------------------------------------- acceptance
+def accept(lnl_buf, max_keys, segments, u_source="pcg64", u=None, out_idx=None, out_lnl=None,
+           counts=None, stream=None):
+    """Run the acceptance pass (joker_accept) over ``segments``.
+
+    Each segment is a dict with lnl_off, n, idx_base, out_off, max_out,
+    max_slot and either u_off (u_source="array") or pcg=(state, inc, offset).
+    Returns (out_idx, out_lnl, counts) CUDA tensors.
+    """
+    ns = len(segments)
+    arr = (nat.AcceptSeg * ns)()
+    total_out = 0
+    for i, sg in enumerate(segments):
+        a = arr[i]
+        a.lnl_off, a.n, a.idx_base = int(sg["lnl_off"]), int(sg["n"]), int(sg.get("idx_base", 0))
+        a.out_off, a.max_out = int(sg["out_off"]), int(sg["max_out"])
+        a.u_off = int(sg.get("u_off", 0))
+        a.max_slot = int(sg.get("max_slot", 0))
+        if u_source == "pcg64":
+            st, inc, off = sg["pcg"]
+            a.pcg_state_hi, a.pcg_state_lo, a.pcg_inc_hi, a.pcg_inc_lo = pcg64_fields(st, inc, off)
+        total_out = max(total_out, a.out_off + a.max_out)
+    dev = lnl_buf.device
+    if out_idx is None:
+        out_idx = torch.empty(max(total_out, 1), dtype=torch.int64, device=dev)
+    if counts is None:
+        counts = torch.empty(ns, dtype=torch.int64, device=dev)
+    wbytes = nat.lib().joker_accept_workspace(arr, ns)
+    work = torch.empty(max(int(wbytes), 1), dtype=torch.uint8, device=dev)
+    usrc = nat.JOKER_U_PCG64 if u_source == "pcg64" else nat.JOKER_U_ARRAY
+    nat.check(nat.lib().joker_accept(
+        arr, ns, ctypes.c_void_p(lnl_buf.data_ptr()), max_keys.ptr(), usrc,
+        ctypes.c_void_p(u.data_ptr()) if u is not None else None,
+        ctypes.c_void_p(out_idx.data_ptr()),
+        ctypes.c_void_p(out_lnl.data_ptr()) if out_lnl is not None else None,
+        ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(work.data_ptr()), int(wbytes),
+        stream_handle(stream)), "joker_accept")
+    # torch's allocator reuses freed blocks in stream order, so the workspace
+    # may be released now; record a foreign stream so that it waits for it
+    if stream is not None:
+        work.record_stream(stream)
+    return out_idx, out_lnl, counts

@@ -1,0 +1,114 @@
+"""GPUJokerHelper: the GB300 drop-in for the reference's CJokerHelper.
+
+It exposes the surface the reference's sampling code uses
+(thejoker/src/fast_likelihood.pyx:70-576): ``packed_order``,
+``internal_units``, ``data``, ``prior``, ``batch_marginal_ln_likelihood``,
+``batch_get_posterior_samples`` and ``test_likelihood_worker``, and it pickles
+by its constructor arguments (``__reduce__``, :122-123).  The likelihood runs
+in libjoker_gb300 on the GPU; there is no CPU path.
+"""
+import numpy as np
+import torch
+
+from . import device as dev
+from .linear import posterior_linear_samples
+from .samples import PACKED_ORDER
+
+__all__ = ["GPUJokerHelper"]
+
+
+class GPUJokerHelper:
+    """Per-star likelihood helper.
+
+    Parameters
+    ----------
+    data : RVData
+    prior : JokerPrior
+    trend_M : (n_times, n_linear - 1) float64 design matrix of the linear
+        parameters other than K (as built by ``validate_prepare_data``).
+    precision : "fp64" (default; the drop-in), "mixed" or "mixed_accurate".
+    jitter : "reference" (default; s is ignored as in CJokerHelper) or
+        "applied" (ivar / (1 + s^2 ivar), as the reference's NumPy test oracle).
+    """
+
+    def __init__(self, data, prior, trend_M, precision="fp64", jitter="reference"):
+        self.prior = prior
+        self.data = data
+        self.precision = precision
+        self.jitter = jitter
+        unit = data.rv_unit
+        self.internal_units = {"P": "d", "e": "", "omega": "rad", "M0": "rad", "s": unit,
+                               "K": unit, "v0": unit}
+        for name in prior._offset_names:
+            self.internal_units[name] = unit
+        for i, name in enumerate(prior._v_trend_names):
+            self.internal_units.setdefault(name, f"{unit} / d^{i}")
+        self.packed_order = list(PACKED_ORDER)
+        self.n_times = len(data)
+        self.n_linear = prior.n_linear
+        trend_M = np.ascontiguousarray(trend_M, dtype=np.float64)
+        if trend_M.ndim != 2 or trend_M.shape[0] != self.n_times or \
+                trend_M.shape[1] != self.n_linear - 1:
+            raise ValueError("Invalid design matrix shape: {}, expected: {}".format(
+                trend_M.shape, (self.n_times, self.n_linear - 1)))
+        self.trend_M = trend_M
+        self.mu, self.lam, self.k_prior = prior.linear_prior_arrays()
+        self._stars = dev.StarTable([dict(
+            t=data._t_bmjd, rv=data.rv, ivar=data.ivar, t_ref=data._t_ref_bmjd,
+            trend_M=trend_M, mu=self.mu, lam=self.lam, k_prior=self.k_prior)], jitter=jitter)
+
+    def __reduce__(self):
+        return (GPUJokerHelper, (self.data, self.prior, self.trend_M, self.precision, self.jitter))
+
+    @property
+    def stars(self):
+        return self._stars
+
+    # ------------------------------------------------------------ likelihood
+    def batch_marginal_ln_likelihood_device(self, chunk, out=None, stream=None):
+        """ln L for a (S, 5) float64 CUDA tensor; returns a CUDA tensor."""
+        if chunk.dtype != torch.float64 or chunk.dim() != 2 or chunk.shape[1] != 5:
+            raise ValueError("chunk must be float64 with shape (n_samples, 5)")
+        chunk = chunk.contiguous()
+        S = chunk.shape[0]
+        if out is None:
+            out = torch.empty(S, dtype=torch.float64, device=chunk.device)
+        if self.precision == "fp64":
+            import ctypes
+            from . import _native as nat
+            nat.check(nat.lib().joker_batch_marginal_ln_likelihood(
+                self._stars.handle, 0, ctypes.c_void_p(chunk.data_ptr()), S,
+                ctypes.c_void_p(out.data_ptr()), dev.stream_handle(stream)),
+                "joker_batch_marginal_ln_likelihood")
+        else:
+            cache = dev.PriorCache.from_samples(chunk, stream=stream)
+            dev.lnl(self._stars, cache, out.view(1, S), precision=self.precision, stream=stream)
+        return out
+
+    def batch_marginal_ln_likelihood(self, chunk):
+        """Marginal ln-likelihood per row of ``chunk`` (S x 5: P, e, omega, M0, s),
+        the drop-in for CJokerHelper.batch_marginal_ln_likelihood (:428-469)."""
+        chunk = np.ascontiguousarray(chunk, dtype=np.float64)
+        if chunk.ndim != 2 or chunk.shape[1] != 5:
+            raise ValueError("chunk must have shape (n_samples, 5)")
+        if chunk.shape[0] == 0:
+            return np.zeros(0)
+        d = torch.from_numpy(chunk).pin_memory().to("cuda", non_blocking=True)
+        out = self.batch_marginal_ln_likelihood_device(d)
+        return out.cpu().numpy()
+
+    def test_likelihood_worker(self, chunk_row):
+        """ln L of one packed sample (fast_likelihood.pyx:547-576)."""
+        return float(self.batch_marginal_ln_likelihood(np.asarray(chunk_row)[None, :])[0])
+
+    # ------------------------------------------------------ linear parameters
+    def batch_get_posterior_samples(self, chunk, n_linear_samples_per, rng):
+        """(samples (S*n, n_pars), ll (S*n)) as fast_likelihood.pyx:471-545."""
+        chunk = np.ascontiguousarray(chunk, dtype=np.float64)
+        S = chunk.shape[0]
+        ll = np.repeat(self.batch_marginal_ln_likelihood(chunk) if S else np.zeros(0),
+                       n_linear_samples_per)
+        samples, _, _ = posterior_linear_samples(
+            chunk, n_linear_samples_per, rng, self.data._t_bmjd, self.data.rv, self.data.ivar,
+            self.data._t_ref_bmjd, self.trend_M, self.mu, self.lam, self.k_prior)
+        return samples, ll
