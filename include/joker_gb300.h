@@ -166,6 +166,28 @@ int joker_accept(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
                  int64_t *d_out_idx, double *d_out_lnl, int64_t *d_count,
                  void *d_work, int64_t work_bytes, void *stream);
 
+/* ---- acceptance without allocation ---------------------------------------
+ * No counterpart in the reference.  joker_accept_noalloc is joker_accept for
+ * callers that must not allocate device memory: a serving loop with
+ * per-request deadlines (cudaMalloc may synchronise the device and has
+ * unbounded latency), or a plugin inside a host framework whose caching
+ * allocator already holds the device's free memory.  It needs no workspace.
+ * Its scratch space is one fixed array of 2,220,288 bytes inside the
+ * library, held on every GPU that loads the library until the process exits.
+ * Limits: at most JOKER_NOALLOC_MAX_SEGS segments and
+ * JOKER_NOALLOC_MAX_BLOCKS blocks of 8192 samples (each segment rounded up;
+ * about 2^24 samples in all); larger calls return JOKER_ERANGE.  All calls
+ * share the array: calls that overlap on the GPU (another stream, another
+ * host thread) race and must not be issued.  The first call on a device looks
+ * up the array's address with that device current; make it before any stream
+ * capture.  It allocates nothing: no cudaMalloc, cudaFree or heap use. */
+#define JOKER_NOALLOC_MAX_SEGS 1024
+#define JOKER_NOALLOC_MAX_BLOCKS 2048
+int joker_accept_noalloc(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
+                         const uint64_t *d_max_key, int u_source, const double *d_u,
+                         int64_t *d_out_idx, double *d_out_lnl, int64_t *d_count,
+                         void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,7 +23,7 @@ EXPORTED = (
     "joker_abi_version", "joker_last_error", "joker_stars_create", "joker_stars_destroy",
     "joker_stars_info", "joker_cache_create", "joker_cache_destroy", "joker_cache_load",
     "joker_cache_capacity", "joker_batch_marginal_ln_likelihood", "joker_lnl",
-    "joker_key_to_double", "joker_accept_workspace", "joker_accept",
+    "joker_key_to_double", "joker_accept_workspace", "joker_accept", "joker_accept_noalloc",
 )
 
 
@@ -67,6 +67,8 @@ _SIGS = {
     "joker_accept_workspace": (_i64, [ctypes.POINTER(AcceptSeg), ctypes.c_int]),
     "joker_accept": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                     ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
+    "joker_accept_noalloc": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
+                                            ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _LIB = None

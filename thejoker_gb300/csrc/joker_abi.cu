@@ -59,6 +59,11 @@ struct joker_cache {
     float *mx_s2 = nullptr;
 };
 
+namespace joker {
+// lets the other translation units report through joker_last_error()
+void set_last_error(const char *msg) { g_err = msg; }
+}  // namespace joker
+
 extern "C" int joker_abi_version(void) { return JOKER_ABI_VERSION; }
 extern "C" const char *joker_last_error(void) { return g_err.c_str(); }
 
