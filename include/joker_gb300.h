@@ -52,6 +52,8 @@ extern "C" {
                                FP32 epoch sums, FP64 small solve; sin/cos of
                                the Kepler starter on the special-function unit */
 #define JOKER_MIXED_ACCURATE 2  /* as JOKER_MIXED with correctly rounded sincosf */
+#define JOKER_MIXED_FP64_TAIL 3 /* as JOKER_MIXED with the per-sample solve in FP64
+                                   instead of float-float (no error bound) */
 
 /* jitter handling (the reference Cython computes the jittered inverse variance
    but never reads it, fast_likelihood.pyx:458; its NumPy test oracle applies
@@ -81,8 +83,8 @@ typedef struct {
     uint64_t pcg_inc_hi;
     uint64_t pcg_inc_lo;
     int32_t max_slot;      /* which running maximum (d_max_key) the segment uses */
-    int32_t reserved;
-    int64_t reserved2;
+    int32_t star;          /* joker_accept_refined: the segment's star */
+    int64_t row0;          /* joker_accept_refined: cache row of the segment's sample 0 */
 } joker_accept_seg;
 
 int joker_abi_version(void);
@@ -141,14 +143,18 @@ int joker_batch_marginal_ln_likelihood(const joker_stars *stars, int star,
  * d_lnl is n_sel x count with row stride ld.  When d_max_key is not NULL,
  * d_max_key[k] holds an order-preserving integer image of the running
  * maximum of star star0+k and is raised atomically (it must be zeroed, or hold
- * a previous maximum, before the call).  precision: JOKER_FP64, JOKER_MIXED or
- * JOKER_MIXED_ACCURATE.  block (threads per CTA, 0 = 128) and chunk (samples
- * per work item, a multiple of block, 0 = 1024) tune the launch.  Calls that
- * share one joker_stars handle must be ordered on one stream. */
+ * a previous maximum, before the call).  precision: JOKER_FP64, JOKER_MIXED,
+ * JOKER_MIXED_ACCURATE or JOKER_MIXED_FP64_TAIL.
+ * Mixed precisions only: d_err (optional, laid out like d_lnl) receives a
+ * bound on |lnL - lnL_FP64| per sample, and d_bound_key (optional, 2 per star)
+ * the running maxima of lnL + err and lnL - err.
+ * block (threads per CTA, 0 = 128) and chunk (samples per work item, a
+ * multiple of block, 0 = 1024) tune the launch.  Calls that share one
+ * joker_stars handle must be ordered on one stream. */
 int joker_lnl(const joker_stars *stars, const joker_cache *cache, int star0,
               int n_sel, int64_t row0, int64_t count, int precision,
-              double *d_lnl, int64_t ld, uint64_t *d_max_key, int block,
-              int64_t chunk, void *stream);
+              double *d_lnl, int64_t ld, uint64_t *d_max_key, float *d_err,
+              uint64_t *d_bound_key, int block, int64_t chunk, void *stream);
 
 /* Decode an order-preserving key back to the double it encodes. */
 double joker_key_to_double(uint64_t key);
@@ -165,6 +171,22 @@ int joker_accept(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
                  const uint64_t *d_max_key, int u_source, const double *d_u,
                  int64_t *d_out_idx, double *d_out_lnl, int64_t *d_count,
                  void *d_work, int64_t work_bytes, void *stream);
+
+/* The acceptance pass over mixed-precision ln L values with their error
+ * bounds (d_err, d_bound_key from joker_lnl), exact with respect to FP64:
+ * the maximum is re-evaluated in FP64 among the samples whose interval can
+ * reach it, and every sample whose decision the interval leaves open is
+ * re-evaluated in FP64 from the cache (seg.star, seg.row0 locate it).  The
+ * kept indices are then those the FP64 path would keep.  d_exact_key (one per
+ * max_slot) receives the FP64 maxima; d_n_refined (optional) counts the
+ * re-evaluated samples.  Same workspace as joker_accept. */
+int joker_accept_refined(const joker_stars *stars, const joker_cache *cache,
+                         const joker_accept_seg *segs, int n_segs, const double *d_lnl,
+                         const float *d_err, const uint64_t *d_bound_key,
+                         uint64_t *d_exact_key, int n_slots, int u_source,
+                         const double *d_u, int64_t *d_out_idx, double *d_out_lnl,
+                         int64_t *d_count, uint64_t *d_n_refined, void *d_work,
+                         int64_t work_bytes, void *stream);
 
 /* ---- acceptance without allocation ---------------------------------------
  * No counterpart in the reference.  joker_accept_noalloc is joker_accept for

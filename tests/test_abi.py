@@ -96,7 +96,8 @@ def test_argument_validation_without_device(native_lib):
     assert st == 1
     # cache with bad capacity; NULL handles
     assert native_lib.joker_cache_create(ctypes.byref(h), 0) == 1
-    assert native_lib.joker_lnl(None, None, 0, 1, 0, 1, 0, None, 1, None, 0, 0, None) == 1
+    assert native_lib.joker_lnl(None, None, 0, 1, 0, 1, 0, None, 1, None, None, None, 0, 0,
+                                None) == 1
     assert native_lib.joker_batch_marginal_ln_likelihood(None, 0, None, 1, None, None) == 1
     assert native_lib.joker_accept(None, 0, None, None, 0, None, None, None, None, None, 0, None) == 0
     assert native_lib.joker_cache_capacity(None) == -1

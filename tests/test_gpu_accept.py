@@ -140,3 +140,39 @@ def test_thejoker_iterative_matches_reference_loop(cuda):
         n_process = int(1 * (8 - len(good)) / len(good) * len(allm))
         n_process = min(n_process, 200000 - start)
     np.testing.assert_array_equal(out["P"], chunk[good[:8], 0])
+
+
+@pytest.mark.parametrize("n_ep,K,jitter", [(3, 1.0, "reference"), (12, 5.0, "reference"),
+                                           (40, 30.0, "applied"), (8, 0.5, "applied")])
+def test_refined_accept_equals_fp64_accept(cuda, n_ep, K, jitter):
+    """Acceptance over mixed ln L with refinement keeps exactly what the FP64
+    path keeps (same uniforms), while re-evaluating few samples in FP64."""
+    from thejoker_gb300 import device as dev
+    rng = np.random.default_rng(300 + n_ep)
+    st = synth_star(rng, n_ep, K=K)
+    S = 1 << 18
+    chunk = synth_chunk(rng, S, jitter=(jitter == "applied"))
+    table = dev.StarTable([st], jitter=jitter)
+    cache = dev.PriorCache.from_samples(chunk)
+    lnl64 = torch.empty((1, S), dtype=torch.float64, device="cuda")
+    k64 = dev.MaxKeys(1)
+    dev.lnl(table, cache, lnl64, precision="fp64", max_keys=k64)
+    lnlm = torch.empty((1, S), dtype=torch.float64, device="cuda")
+    err = torch.empty((1, S), dtype=torch.float32, device="cuda")
+    km, bk = dev.MaxKeys(1), dev.MaxKeys(2)
+    dev.lnl(table, cache, lnlm, precision="mixed", max_keys=km, err=err, bound_keys=bk)
+    gen = np.random.default_rng(5)
+    pcg = dev.pcg64_state(gen)
+    seg = dict(lnl_off=0, n=S, out_off=0, max_out=S, max_slot=0, star=0, row0=0,
+               pcg=(pcg[0], pcg[1], 0))
+    i64, _, c64 = dev.accept(lnl64.view(-1), k64, [seg])
+    im, _, cm, exact, nref = dev.accept_refined(table, cache, lnlm.view(-1), err.view(-1), bk,
+                                                [seg])
+    n64, nm = int(c64[0]), int(cm[0])
+    print(n_ep, K, jitter, "accepted", n64, "refined in FP64", int(nref[0]))
+    assert n64 == nm
+    np.testing.assert_array_equal(i64[:n64].cpu().numpy(), im[:nm].cpu().numpy())
+    # the refinement re-evaluates in FP64 through a separately compiled call
+    # site; its maximum matches the FP64 kernel's to rounding
+    np.testing.assert_allclose(exact.values()[0], k64.values()[0], rtol=1e-13)
+    assert int(nref[0]) < S // 50

@@ -12,6 +12,7 @@ JOKER_OK = 0
 JOKER_FP64 = 0
 JOKER_MIXED = 1
 JOKER_MIXED_ACCURATE = 2
+JOKER_MIXED_FP64_TAIL = 3
 JOKER_JITTER_REFERENCE = 0
 JOKER_JITTER_APPLIED = 1
 JOKER_U_ARRAY = 0
@@ -23,7 +24,8 @@ EXPORTED = (
     "joker_abi_version", "joker_last_error", "joker_stars_create", "joker_stars_destroy",
     "joker_stars_info", "joker_cache_create", "joker_cache_destroy", "joker_cache_load",
     "joker_cache_capacity", "joker_batch_marginal_ln_likelihood", "joker_lnl",
-    "joker_key_to_double", "joker_accept_workspace", "joker_accept", "joker_accept_noalloc",
+    "joker_key_to_double", "joker_accept_workspace", "joker_accept", "joker_accept_refined",
+    "joker_accept_noalloc",
 )
 
 
@@ -38,7 +40,7 @@ class AcceptSeg(ctypes.Structure):
         ("out_off", ctypes.c_int64), ("max_out", ctypes.c_int64), ("u_off", ctypes.c_int64),
         ("pcg_state_hi", ctypes.c_uint64), ("pcg_state_lo", ctypes.c_uint64),
         ("pcg_inc_hi", ctypes.c_uint64), ("pcg_inc_lo", ctypes.c_uint64),
-        ("max_slot", ctypes.c_int32), ("reserved", ctypes.c_int32), ("reserved2", ctypes.c_int64),
+        ("max_slot", ctypes.c_int32), ("star", ctypes.c_int32), ("row0", ctypes.c_int64),
     ]
 
 
@@ -62,11 +64,14 @@ _SIGS = {
     "joker_cache_capacity": (_i64, [_vp]),
     "joker_batch_marginal_ln_likelihood": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64, _vp, _vp]),
     "joker_lnl": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _i64, _i64, ctypes.c_int,
-                                 _vp, _i64, _vp, ctypes.c_int, _i64, _vp]),
+                                 _vp, _i64, _vp, _vp, _vp, ctypes.c_int, _i64, _vp]),
     "joker_key_to_double": (ctypes.c_double, [ctypes.c_uint64]),
     "joker_accept_workspace": (_i64, [ctypes.POINTER(AcceptSeg), ctypes.c_int]),
     "joker_accept": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                     ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
+    "joker_accept_refined": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(AcceptSeg), ctypes.c_int,
+                                            _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp,
+                                            _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
     "joker_accept_noalloc": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                             ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

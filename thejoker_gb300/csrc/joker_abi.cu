@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -128,6 +129,11 @@ extern "C" int joker_stars_create(joker_stars **out, int n_stars, int n_linear,
     if (!epoch_offsets || !t || !rv || !ivar || !t_ref || !mu || !lambda || !k_prior ||
         (n_linear > 1 && !trend_M))
         return fail(JOKER_EINVAL, "joker_stars_create: NULL array argument");
+    if (n_linear > 1)
+        for (int64_t i = 0; i < epoch_offsets[n_stars]; ++i)
+            if (trend_M[i * (n_linear - 1)] != 1.0)
+                return fail(JOKER_EINVAL, "joker_stars_create: column 0 of trend_M must be 1 (the "
+                                          "constant v0 term of the reference's design matrix)");
     if (epoch_offsets[0] != 0) return fail(JOKER_EINVAL, "epoch_offsets[0] must be 0");
     const int L = n_linear, T = n_linear - 1;
     int max_ep = 0;
@@ -197,17 +203,20 @@ extern "C" int joker_stars_create(joker_stars **out, int n_stars, int n_linear,
             float *r32 = &ep32[(size_t)g * REC32];
             split_ff(dt, r32[0], r32[1]);
             if (jitter_mode == JOKER_JITTER_REFERENCE) {
+                // dt, w, w y', w T_j
                 split_ff(ivar[g], r32[2], r32[3]);
                 split_ff((double)(w * yp), r32[4], r32[5]);
                 for (int j = 0; j < T; ++j)
                     split_ff((double)(w * (long double)trend_M[g * T + j]), r32[6 + 2 * j],
                              r32[7 + 2 * j]);
             } else {
+                // dt, ivar, y', y'^2, T_j
                 r32[2] = (float)ivar[g];
                 r32[3] = 0.0f;
                 split_ff((double)yp, r32[4], r32[5]);
+                split_ff((double)(yp * yp), r32[6], r32[7]);
                 for (int j = 0; j < T; ++j)
-                    split_ff(trend_M[g * T + j], r32[6 + 2 * j], r32[7 + 2 * j]);
+                    split_ff(trend_M[g * T + j], r32[8 + 2 * j], r32[9 + 2 * j]);
             }
         }
         for (int j = 0; j < T; ++j) C[j * T + j] += 1.0L / (long double)lamk[j + 1];
@@ -223,6 +232,20 @@ extern "C" int joker_stars_create(joker_stars **out, int n_stars, int n_linear,
             for (int m = 0; m < T; ++m) r.Cinv[(j + 1) * MAXL + (m + 1)] = (double)Cinv[j * T + m];
         }
         r.chi2_0 = (double)(Syy - cCc);
+        split_ff(r.chi2_0, r.chi2_0_hi, r.chi2_0_lo);
+        for (int j = 1; j < L; ++j) {
+            split_ff(r.cC[j], r.cC_hi[j], r.cC_lo[j]);
+            for (int m = 1; m < L; ++m)
+                split_ff(r.Cinv[j * MAXL + m], r.Cinv_hi[j * MAXL + m], r.Cinv_lo[j * MAXL + m]);
+            split_ff((double)(1.0L / (long double)lamk[j]), r.ilam_hi[j], r.ilam_lo[j]);
+        }
+        {
+            long double sw = 0.0L;
+            for (int i = 0; i < n; ++i) sw += ivar[e0 + i];
+            r.sum_ivar = (float)(sw * (1.0L + 1e-6L));   // rounded up: an upper bound
+        }
+        r.mu0_f = (float)muk[0];
+        r.mu0_zero = muk[0] == 0.0;
         r.logdet_const = (double)(n * LOG2PI - slog_ivar + slog_lam + logdetC);
         r.log_norm_rest = (double)(n * LOG2PI + slog_lam);
         r.sum_log_ivar = (double)slog_ivar;
@@ -368,11 +391,24 @@ extern "C" int joker_batch_marginal_ln_likelihood(const joker_stars *s, int star
     return run_lnl(s, JOKER_FP64, a, 128, (cudaStream_t)stream);
 }
 
+static float err_c0() {
+    // column-error constant of the mixed kernel's bound (see joker_lnl.cu);
+    // JOKER_ERR_C0 in the environment overrides it for calibration runs
+    static float c0 = -1.0f;
+    if (c0 < 0.0f) {
+        const char *v = getenv("JOKER_ERR_C0");
+        c0 = v ? (float)atof(v) : 2.0e-6f;
+    }
+    return c0;
+}
+
 extern "C" int joker_lnl(const joker_stars *s, const joker_cache *c, int star0, int n_sel,
                          int64_t row0, int64_t count, int precision, double *d_lnl, int64_t ld,
-                         uint64_t *d_max_key, int block, int64_t chunk, void *stream) {
+                         uint64_t *d_max_key, float *d_err, uint64_t *d_bound_key, int block,
+                         int64_t chunk, void *stream) {
     if (!s || !c) return fail(JOKER_EINVAL, "joker_lnl: NULL handle");
-    if (precision != JOKER_FP64 && precision != JOKER_MIXED && precision != JOKER_MIXED_ACCURATE)
+    if (precision != JOKER_FP64 && precision != JOKER_MIXED && precision != JOKER_MIXED_ACCURATE &&
+        precision != JOKER_MIXED_FP64_TAIL)
         return fail(JOKER_EINVAL, "joker_lnl: unknown precision %d", precision);
     if (star0 < 0 || n_sel < 0 || star0 + n_sel > s->n_stars)
         return fail(JOKER_EINVAL, "joker_lnl: stars [%d, %d) outside [0, %d)", star0,
@@ -398,6 +434,11 @@ extern "C" int joker_lnl(const joker_stars *s, const joker_cache *c, int star0, 
     a.queue = s->d_queue;
     a.lnl = d_lnl;
     a.max_key = (unsigned long long *)d_max_key;
+    if (precision != JOKER_FP64) {
+        a.err = d_err;
+        a.bound_key = (unsigned long long *)d_bound_key;
+        a.err_c0 = err_c0();
+    }
     a.star0 = star0;
     a.n_sel = n_sel;
     a.row0 = row0;
@@ -420,8 +461,9 @@ static int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
 extern "C" int64_t joker_accept_workspace(const joker_accept_seg *segs, int n_segs) {
     if (!segs || n_segs <= 0) return 0;
     const int64_t nb = accept_blocks(segs, n_segs, nullptr);
+    // the second word array holds the undecided samples of joker_accept_refined
     return align256(sizeof(joker_accept_seg) * (int64_t)n_segs) +
-           align256(8 * (int64_t)(n_segs + 1)) + align256(8 * nb) + align256(4 * 256 * nb);
+           align256(8 * (int64_t)(n_segs + 1)) + align256(8 * nb) + 2 * align256(4 * 256 * nb);
 }
 
 extern "C" int joker_accept(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
@@ -456,6 +498,7 @@ extern "C" int joker_accept(const joker_accept_seg *segs, int n_segs, const doub
     CUDA_TRY(cudaMemcpyAsync(d_segs, segs, sizeof(joker_accept_seg) * n_segs, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_base, base.data(), 8 * (n_segs + 1), cudaMemcpyHostToDevice, st));
     AcceptArgs a;
+    memset(&a, 0, sizeof a);      // no refinement: err, exact_key, ... stay NULL
     a.segs = d_segs;
     a.blk_base = d_base;
     a.n_segs = n_segs;
@@ -469,6 +512,79 @@ extern "C" int joker_accept(const joker_accept_seg *segs, int n_segs, const doub
     a.out_lnl = d_out_lnl;
     a.count = d_count;
     // pageable host sources are staged before cudaMemcpyAsync returns
+    CUDA_TRY(launch_accept(a, nb, st));
+    return JOKER_OK;
+}
+
+extern "C" int joker_accept_refined(const joker_stars *s, const joker_cache *c,
+                                    const joker_accept_seg *segs, int n_segs, const double *d_lnl,
+                                    const float *d_err, const uint64_t *d_bound_key,
+                                    uint64_t *d_exact_key, int n_slots, int u_source,
+                                    const double *d_u, int64_t *d_out_idx, double *d_out_lnl,
+                                    int64_t *d_count, uint64_t *d_n_refined, void *d_work,
+                                    int64_t work_bytes, void *stream) {
+    if (n_segs <= 0) return JOKER_OK;
+    if (!s || !c) return fail(JOKER_EINVAL, "joker_accept_refined: NULL handle");
+    if (!segs || !d_lnl || !d_err || !d_bound_key || !d_exact_key || !d_out_idx || !d_count ||
+        !d_work)
+        return fail(JOKER_EINVAL, "joker_accept_refined: NULL argument");
+    if (u_source != JOKER_U_ARRAY && u_source != JOKER_U_PCG64)
+        return fail(JOKER_EINVAL, "joker_accept_refined: unknown u_source %d", u_source);
+    if (u_source == JOKER_U_ARRAY && !d_u)
+        return fail(JOKER_EINVAL, "joker_accept_refined: d_u is NULL");
+    for (int i = 0; i < n_segs; ++i) {
+        const joker_accept_seg &g = segs[i];
+        if (g.n < 0 || g.max_out < 0 || g.lnl_off < 0 || g.max_slot < 0 || g.max_slot >= n_slots)
+            return fail(JOKER_EINVAL, "joker_accept_refined: segment %d has a bad field", i);
+        if (g.star < 0 || g.star >= s->n_stars || g.row0 < 0 || g.row0 + g.n > c->cap)
+            return fail(JOKER_EINVAL, "joker_accept_refined: segment %d outside the stars or cache",
+                        i);
+    }
+    const int64_t need = joker_accept_workspace(segs, n_segs);
+    if (work_bytes < need)
+        return fail(JOKER_EINVAL, "joker_accept_refined: workspace %lld < %lld bytes",
+                    (long long)work_bytes, (long long)need);
+    std::vector<int64_t> base(n_segs + 1);
+    const int64_t nb = accept_blocks(segs, n_segs, base.data());
+    if (nb > 0x7fffffffLL) return fail(JOKER_ERANGE, "joker_accept_refined: too many samples");
+    char *w = (char *)d_work;
+    joker_accept_seg *d_segs = (joker_accept_seg *)w;
+    w += align256(sizeof(joker_accept_seg) * (int64_t)n_segs);
+    int64_t *d_base = (int64_t *)w;
+    w += align256(8 * (int64_t)(n_segs + 1));
+    int64_t *d_blk = (int64_t *)w;
+    w += align256(8 * nb);
+    uint32_t *d_words = (uint32_t *)w;
+    w += align256(4 * 256 * nb);
+    uint32_t *d_amb = (uint32_t *)w;
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemcpyAsync(d_segs, segs, sizeof(joker_accept_seg) * n_segs, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_base, base.data(), 8 * (n_segs + 1), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(d_exact_key, 0, sizeof(uint64_t) * n_slots, st));
+    AcceptArgs a;
+    memset(&a, 0, sizeof a);
+    a.err = d_err;
+    a.bound_key = (const unsigned long long *)d_bound_key;
+    a.exact_key = (unsigned long long *)d_exact_key;
+    a.stars = s->d_stars;
+    a.ep64 = s->d_ep64;
+    a.P = c->P; a.E = c->E; a.OM = c->OM; a.M0 = c->M0; a.S = c->S;
+    a.L = s->L;
+    a.jit = s->jitter == JOKER_JITTER_APPLIED;
+    a.n_refined = (unsigned long long *)d_n_refined;
+    a.amb_words = d_amb;
+    a.segs = d_segs;
+    a.blk_base = d_base;
+    a.n_segs = n_segs;
+    a.lnl = d_lnl;
+    a.max_key = (const unsigned long long *)d_exact_key;
+    a.u_source = u_source;
+    a.u = d_u;
+    a.words = d_words;
+    a.blk_count = d_blk;
+    a.out_idx = d_out_idx;
+    a.out_lnl = d_out_lnl;
+    a.count = d_count;
     CUDA_TRY(launch_accept(a, nb, st));
     return JOKER_OK;
 }

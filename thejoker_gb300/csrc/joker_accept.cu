@@ -4,6 +4,12 @@
 // (thejoker/likelihood_helpers.py:107-109, multiproc_helpers.py:256-258),
 // applied to many independent segments (stars / sample runs) at once.
 //
+// With mixed-precision ln L values and their per-sample error bounds the
+// pass is exact with respect to FP64: a refine kernel first finds the FP64
+// maximum among the samples whose interval [lnL - err, lnL + err] reaches the
+// largest lower bound, and the mark kernel re-evaluates in FP64 every sample
+// whose decision the interval leaves open.  Both touch a handful of samples.
+//
 // Three kernels, all bandwidth-bound scans over the ln L buffer:
 //   mark  -- one warp per 1024 samples, lanes on consecutive samples (coalesced
 //            loads); the test of 32 samples becomes one 32-bit word by ballot;
@@ -15,8 +21,7 @@
 // The uniforms come either from a device array or from numpy's PCG64 stream,
 // regenerated here from the generator state (joker_math.cuh), so the draws are
 // bit-identical to rng.uniform() on the host.
-#include "joker_internal.cuh"
-#include "joker_math.cuh"
+#include "joker_fp64.cuh"
 
 namespace joker {
 
@@ -49,6 +54,46 @@ __device__ __forceinline__ bool accept_test(double d, double u) {
     return exp(d) > u;
 }
 
+// Decision for a sample known only to lie in [lnl - err, lnl + err]:
+// 1 = keep, 0 = reject, -1 = undecided (needs the FP64 value).  The FP32
+// log of u is trusted to 1e-4.
+__device__ __forceinline__ int interval_test(double lnl, float err, double mx, double u) {
+    if (!(err < 1e29f) || !(lnl == lnl)) return -1;
+    const double dlo = lnl - (double)err - mx, dhi = lnl + (double)err - mx;
+    if (u == 0.0) {
+        if (dhi < -746.0) return 0;
+        if (dlo > -744.0) return 1;
+        return -1;
+    }
+    const float lf = __logf((float)u);
+    if (dhi < -40.0 || (float)dhi < lf - 1e-4f) return 0;
+    if ((float)dlo > lf + 1e-4f) return 1;
+    return -1;
+}
+
+// FP64 maximum of each segment: re-evaluate the samples whose upper bound
+// reaches the largest lower bound (the true maximum lies among them).
+__global__ void __launch_bounds__(ACC_THREADS) accept_maxrefine_kernel(AcceptArgs a) {
+    const int64_t gblk = blockIdx.x;
+    const int si = find_seg(a.blk_base, a.n_segs, gblk);
+    const joker_accept_seg sg = a.segs[si];
+    const int64_t blk = gblk - a.blk_base[si];
+    const double lb = key_to_double(a.bound_key[2 * sg.max_slot + 1]);
+    const int64_t first = blk * ACC_BLOCK;
+    for (int k = threadIdx.x; k < ACC_BLOCK; k += ACC_THREADS) {
+        const int64_t i = first + k;
+        if (i >= sg.n) break;
+        const double v = a.lnl[sg.lnl_off + i];
+        const float er = a.err[sg.lnl_off + i];
+        if (!(v + (double)er >= lb) && er < 1e29f && v == v) continue;
+        const int64_t r = sg.row0 + i;
+        const double x = fp64_lnl_sample(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
+                                         a.OM[r], a.M0[r], a.S[r]);
+        atomicMax(a.exact_key + sg.max_slot, double_to_key(x));
+        if (a.n_refined) atomicAdd(a.n_refined, 1ull);
+    }
+}
+
 __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) {
     const int64_t gblk = blockIdx.x;
     const int si = find_seg(a.blk_base, a.n_segs, gblk);
@@ -56,7 +101,9 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
     const int64_t blk = gblk - a.blk_base[si];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t wbase = blk * ACC_BLOCK + (int64_t)warp * 1024;  // first sample of this warp
-    const double mx = key_to_double(a.max_key[sg.max_slot]);
+    const bool refine = a.err != nullptr;
+    const double mx = refine ? key_to_double(a.exact_key[sg.max_slot])
+                             : key_to_double(a.max_key[sg.max_slot]);
     const double *lnl = a.lnl + sg.lnl_off;
 
     u128 st = 0, inc = 0, Am = 1, Cp = 0;
@@ -72,24 +119,35 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
         Am = cm;
         Cp = cp;
     }
-    uint32_t my_word = 0;
+    uint32_t my_word = 0, my_amb = 0;
     int my_count = 0;
     for (int k = 0; k < 32; ++k) {
         const int64_t i = wbase + (int64_t)k * 32 + lane;
-        bool keep = false;
+        bool keep = false, amb = false;
         if (i < sg.n) {
             double u;
             if (a.u_source == JOKER_U_PCG64) u = pcg_uniform(pcg_output(st));
             else u = a.u[sg.u_off + i];
-            keep = accept_test(lnl[i] - mx, u);
+            if (!refine) {
+                keep = accept_test(lnl[i] - mx, u);
+            } else {
+                const int dec = interval_test(lnl[i], a.err[sg.lnl_off + i], mx, u);
+                keep = dec == 1;
+                amb = dec < 0;
+            }
         }
         if (a.u_source == JOKER_U_PCG64) st = Am * st + Cp;
         const uint32_t bal = __ballot_sync(0xffffffffu, keep);
-        if (lane == k) my_word = bal;
+        const uint32_t abal = __ballot_sync(0xffffffffu, amb);
+        if (lane == k) {
+            my_word = bal;
+            my_amb = abal;
+        }
         my_count += __popc(bal);
     }
     // word index within the CTA: warp * 32 + lane
     a.words[gblk * ACC_THREADS + threadIdx.x] = my_word;
+    if (refine) a.amb_words[gblk * ACC_THREADS + threadIdx.x] = my_amb;
     __shared__ int s_cnt[ACC_THREADS / 32];
     if (lane == 0) s_cnt[warp] = my_count;
     __syncthreads();
@@ -97,6 +155,43 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
         int64_t c = 0;
         for (int w = 0; w < ACC_THREADS / 32; ++w) c += s_cnt[w];
         a.blk_count[gblk] = c;
+    }
+}
+
+// Samples the interval test left open: their FP64 value against the FP64
+// maximum and their own uniform.  Runs between mark and scan; one thread per
+// 32-sample word, almost all of which have nothing to do.
+__global__ void __launch_bounds__(ACC_THREADS) accept_decide_kernel(AcceptArgs a) {
+    const int64_t gblk = blockIdx.x;
+    uint32_t amb = a.amb_words[gblk * ACC_THREADS + threadIdx.x];
+    if (amb == 0) return;
+    const int si = find_seg(a.blk_base, a.n_segs, gblk);
+    const joker_accept_seg sg = a.segs[si];
+    const int64_t blk = gblk - a.blk_base[si];
+    const double mx = key_to_double(a.exact_key[sg.max_slot]);
+    const int64_t first = blk * ACC_BLOCK + (int64_t)threadIdx.x * 32;
+    uint32_t add = 0;
+    while (amb) {
+        const int b = __ffs(amb) - 1;
+        amb &= amb - 1;
+        const int64_t i = first + b;
+        double u;
+        if (a.u_source == JOKER_U_PCG64) {
+            const u128 s0 = ((u128)sg.pcg_state_hi << 64) | (u128)sg.pcg_state_lo;
+            const u128 inc = ((u128)sg.pcg_inc_hi << 64) | (u128)sg.pcg_inc_lo;
+            u = pcg_uniform(pcg_output(pcg_advance(s0, inc, (uint64_t)i + 1)));
+        } else {
+            u = a.u[sg.u_off + i];
+        }
+        const int64_t r = sg.row0 + i;
+        const double v = fp64_lnl_sample(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
+                                         a.OM[r], a.M0[r], a.S[r]);
+        if (a.n_refined) atomicAdd(a.n_refined, 1ull);
+        if (accept_test(v - mx, u)) add |= 1u << b;
+    }
+    if (add) {
+        atomicOr(a.words + gblk * ACC_THREADS + threadIdx.x, add);
+        atomicAdd((unsigned long long *)(a.blk_count + gblk), (unsigned long long)__popc(add));
     }
 }
 
@@ -168,10 +263,20 @@ int64_t accept_blocks(const joker_accept_seg *segs, int n_segs, int64_t *blk_bas
 }
 
 cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st) {
+    if (a.err != nullptr && total_blocks > 0) {
+        accept_maxrefine_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     if (total_blocks > 0) {
         accept_mark_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
+        if (a.err != nullptr) {
+            accept_decide_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
     }
     accept_scan_kernel<<<a.n_segs, ACC_THREADS, 0, st>>>(a);
     cudaError_t e = cudaGetLastError();

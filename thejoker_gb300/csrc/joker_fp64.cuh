@@ -1,0 +1,209 @@
+// FP64 per-sample marginal likelihood, shared by the FP64 kernel and the
+// refinement step of the acceptance pass (both must give identical numbers).
+#pragma once
+#include "joker_internal.cuh"
+#include "joker_math.cuh"
+
+namespace joker {
+
+// Natural log of a positive double for the FP64-tail variant of the mixed
+// path: exact binary exponent, FP32 logf of the mantissa in [1, 2).
+__device__ __forceinline__ double log_mixed(double x) {
+    const int hi = __double2hiint(x);
+    const int ex = ((hi >> 20) & 0x7ff) - 1023;
+    const double m = __hiloint2double((hi & 0x800fffff) | 0x3ff00000, __double2loint(x));
+    if (ex == -1023 || ex == 1024) return log(x);   // zero, subnormal, inf, NaN
+    return (double)ex * 0.69314718055994530942 + (double)logf((float)m);
+}
+
+// Per-sample FP64 state: the epoch sums and the sample's constants.
+template <int L, bool JIT>
+struct Acc64 {
+    double e, Ac, Bc, Dc, k2p, M0, s2, mu0;
+    double A00, b0, A0[MAXL];            // no jitter
+    double G[L][L], q[L], rWr, slw;      // jitter: full system, sum log w
+
+    __device__ __forceinline__ void init(const StarRec &st, double P, double e_, double om,
+                                         double M0_, double s_) {
+        e = e_;
+        M0 = M0_;
+        s2 = s_ * s_;
+        mu0 = st.mu0;
+        k2p = TWO_PI_D / P;
+        double sw, cw;
+        sincos(om, &sw, &cw);
+        const double sq1me2 = sqrt((1.0 - e) * (1.0 + e));
+        Ac = cw;
+        Bc = -sw * sq1me2;
+        Dc = e * cw;
+        A00 = 0.0;
+        b0 = 0.0;
+#pragma unroll
+        for (int k = 0; k < MAXL; ++k) A0[k] = 0.0;
+        rWr = 0.0;
+        slw = 0.0;
+        if (JIT) {
+#pragma unroll
+            for (int i = 0; i < L; ++i) {
+                q[i] = 0.0;
+#pragma unroll
+                for (int k = 0; k < L; ++k) G[i][k] = 0.0;
+            }
+        }
+    }
+
+    // one epoch: dt = t - t_ref, y' = y - sum_{j>=1} mu_j T_j, ivar, T_1..T_{L-1}
+    __device__ __forceinline__ void add(double dt, double yp, double iv, const double *T) {
+        double M = fma(dt, k2p, -M0);
+        const double nrev = rint(M * INV_TWO_PI_D);
+        M = fma(-nrev, TWO_PI_HI_D, M);
+        M = fma(-nrev, TWO_PI_LO_D, M);
+        double sE, cE;
+        kepler_sincos_f64(M, e, sE, cE);
+        const double den = 1.0 - e * cE;
+        const double m = fma(Ac, cE, fma(Bc, sE, -Dc)) / den + Dc;
+        if (!JIT) {
+            const double wm = iv * m;
+            A00 = fma(wm, m, A00);
+            b0 = fma(wm, yp, b0);
+#pragma unroll
+            for (int k = 1; k < L; ++k) A0[k] = fma(wm, T[k - 1], A0[k]);
+        } else {
+            const double wj = iv / (1.0 + s2 * iv);
+            slw += log(wj);
+            double x[L];
+            x[0] = m;
+#pragma unroll
+            for (int k = 1; k < L; ++k) x[k] = T[k - 1];
+            const double r = fma(-mu0, m, yp);
+            rWr = fma(wj * r, r, rWr);
+#pragma unroll
+            for (int ii = 0; ii < L; ++ii) {
+                const double wx = wj * x[ii];
+                q[ii] = fma(wx, r, q[ii]);
+#pragma unroll
+                for (int k = 0; k <= ii; ++k) G[ii][k] = fma(wx, x[k], G[ii][k]);
+            }
+        }
+    }
+
+    __device__ __forceinline__ double finish(const StarRec &st, double P) const;
+};
+
+// Schur-complement tail (no jitter), FP64.
+template <int L, bool MIXED_LOG>
+__device__ __forceinline__ double tail_schur_d(const StarRec &st, double A00, const double *A0,
+                                               double b0, double lam0, double log_lam0) {
+    double gv = 0.0, gcC = 0.0;
+#pragma unroll
+    for (int j = 1; j < L; ++j) {
+        double vj = 0.0;
+#pragma unroll
+        for (int k = 1; k < L; ++k) vj = fma(st.Cinv[j * MAXL + k], A0[k], vj);
+        gv = fma(A0[j], vj, gv);
+        gcC = fma(A0[j], st.cC[j], gcC);
+    }
+    const double a_minus = A00 - gv;           // s - 1/Lambda0
+    const double s = a_minus + 1.0 / lam0;
+    const double u = b0 - gcC;
+    const double mu0 = st.mu0;
+    const double t = fma(-mu0, a_minus, u);
+    double chi2 = st.chi2_0;
+    if (mu0 != 0.0) chi2 = fma(mu0 * mu0, a_minus, fma(-2.0 * mu0, u, chi2));
+    chi2 -= t * t / s;
+    const double logdet = st.logdet_const + log_lam0 + (MIXED_LOG ? log_mixed(s) : log(s));
+    return -0.5 * (chi2 + logdet);
+}
+
+// Full tail (jitter applied), FP64: LDL^T of G, quadratic form, log det.
+template <int L, bool MIXED_LOG>
+__device__ __forceinline__ double tail_full_d(const double (&G)[L][L], const double (&q)[L],
+                                              double rWr, double logdet_const) {
+    double D[L], Lw[L][L];
+    double quad = 0.0, detp = 1.0;
+#pragma unroll
+    for (int k = 0; k < L; ++k) {
+        double dk = G[k][k];
+#pragma unroll
+        for (int m = 0; m < k; ++m) dk = fma(-Lw[k][m] * Lw[k][m], D[m], dk);
+        D[k] = dk;
+        const double rdk = 1.0 / dk;
+#pragma unroll
+        for (int i = k + 1; i < L; ++i) {
+            double v = G[i][k];
+#pragma unroll
+            for (int m = 0; m < k; ++m) v = fma(-Lw[i][m] * Lw[k][m], D[m], v);
+            Lw[i][k] = v * rdk;
+        }
+        detp *= dk;
+    }
+    double z[L];
+#pragma unroll
+    for (int k = 0; k < L; ++k) {
+        double v = q[k];
+#pragma unroll
+        for (int m = 0; m < k; ++m) v = fma(-Lw[k][m], z[m], v);
+        z[k] = v;
+        quad = fma(v * v, 1.0 / D[k], quad);
+    }
+    const double logdet = logdet_const + (MIXED_LOG ? log_mixed(detp) : log(detp));
+    return -0.5 * (rWr - quad + logdet);
+}
+
+// K prior variance per sample (fast_likelihood.pyx:461-464)
+__device__ __forceinline__ double k_prior_variance(const StarRec &st, double P, double e) {
+    if (!st.k_scaled) return st.lam0;
+    const double v = st.sigK0sq / (1.0 - e * e) * pow(P / st.P0, -2.0 / 3.0);
+    return fmin(st.maxK2, v);
+}
+
+template <int L, bool JIT>
+__device__ __forceinline__ double Acc64<L, JIT>::finish(const StarRec &st, double P) const {
+    const double lam0 = k_prior_variance(st, P, e);
+    if (!JIT) return tail_schur_d<L, false>(st, A00, A0, b0, lam0, log(lam0));
+    double Gs[L][L];
+#pragma unroll
+    for (int ii = 0; ii < L; ++ii) {
+#pragma unroll
+        for (int k = 0; k <= ii; ++k) { Gs[ii][k] = G[ii][k]; Gs[k][ii] = G[ii][k]; }
+        Gs[ii][ii] += 1.0 / (ii == 0 ? lam0 : st.lam[ii]);
+    }
+    return tail_full_d<L, false>(Gs, q, rWr, st.log_norm_rest + log(lam0) - slw);
+}
+
+// FP64 ln L of one sample with the star's epochs read from global memory.
+template <int L, bool JIT>
+__device__ __noinline__ double fp64_lnl_global(const StarRec &st, const double *ep64, double P,
+                                               double e, double om, double M0, double s) {
+    Acc64<L, JIT> acc;
+    acc.init(st, P, e, om, M0, s);
+    const double *rec = ep64 + (size_t)st.epoch_off * REC64;
+    for (int i = 0; i < st.n_epochs; ++i, rec += REC64) {
+        double T[MAXL];
+#pragma unroll
+        for (int k = 1; k < L; ++k) T[k - 1] = __ldg(rec + 2 + k);
+        acc.add(__ldg(rec), __ldg(rec + 1), __ldg(rec + 2), T);
+    }
+    return acc.finish(st, P);
+}
+
+__device__ __forceinline__ double fp64_lnl_sample(int L, bool jit, const StarRec &st,
+                                                  const double *ep64, double P, double e,
+                                                  double om, double M0, double s) {
+    switch (L) {
+        case 1: return jit ? fp64_lnl_global<1, true>(st, ep64, P, e, om, M0, s)
+                           : fp64_lnl_global<1, false>(st, ep64, P, e, om, M0, s);
+        case 2: return jit ? fp64_lnl_global<2, true>(st, ep64, P, e, om, M0, s)
+                           : fp64_lnl_global<2, false>(st, ep64, P, e, om, M0, s);
+        case 3: return jit ? fp64_lnl_global<3, true>(st, ep64, P, e, om, M0, s)
+                           : fp64_lnl_global<3, false>(st, ep64, P, e, om, M0, s);
+        case 4: return jit ? fp64_lnl_global<4, true>(st, ep64, P, e, om, M0, s)
+                           : fp64_lnl_global<4, false>(st, ep64, P, e, om, M0, s);
+        case 5: return jit ? fp64_lnl_global<5, true>(st, ep64, P, e, om, M0, s)
+                           : fp64_lnl_global<5, false>(st, ep64, P, e, om, M0, s);
+        default: return jit ? fp64_lnl_global<6, true>(st, ep64, P, e, om, M0, s)
+                            : fp64_lnl_global<6, false>(st, ep64, P, e, om, M0, s);
+    }
+}
+
+}  // namespace joker

@@ -9,7 +9,7 @@ namespace joker {
 
 constexpr int MAXL = JOKER_MAX_LINEAR;
 constexpr int TILE = 256;          // epochs staged in shared memory at a time
-constexpr int REC32 = 16;          // floats per epoch record of the mixed kernel
+constexpr int REC32 = 20;          // floats per epoch record of the mixed kernel
 constexpr int REC64 = 8;           // doubles per epoch record of the FP64 kernel
 
 // Per-star constants, built on the host in FP64 (joker_abi.cu).  Index 0 of
@@ -36,6 +36,15 @@ struct alignas(16) StarRec {
     double lam[MAXL];           // prior variances (lam[0] = lam0)
     double log_norm_rest;       // N log 2pi + sum_{j>=1} log lambda_j
     double sum_log_ivar;        // sum log ivar
+    // float-float copies for the mixed kernel's tail
+    float chi2_0_hi, chi2_0_lo;
+    float cC_hi[MAXL], cC_lo[MAXL];
+    float Cinv_hi[MAXL * MAXL], Cinv_lo[MAXL * MAXL];
+    float ilam_hi[MAXL], ilam_lo[MAXL];   // 1 / lambda_j (j >= 1)
+    float sum_ivar;                        // sum ivar, bounds sum w under any jitter
+    float mu0_f;
+    int32_t mu0_zero;                      // mu0 == 0 (the usual K prior mean)
+    int32_t pad2;
 };
 
 // One unit of the persistent likelihood kernels: `count` samples of star
@@ -71,6 +80,11 @@ struct LnlArgs {
     int *queue;              // dynamic work counter, zeroed before launch
     double *lnl;
     unsigned long long *max_key;
+    // mixed kernel only: per-sample error bound and the per-slot keys of
+    // max(lnL + err) and max(lnL - err)
+    float *err;
+    unsigned long long *bound_key;   // [slot][2]
+    float err_c0;                    // column-error constant of the bound
 };
 
 __device__ __forceinline__ WorkItem get_item(const LnlArgs &a, int it) {
@@ -90,6 +104,17 @@ __device__ __forceinline__ WorkItem get_item(const LnlArgs &a, int it) {
 }
 
 struct AcceptArgs {
+    // refinement (mixed-precision ln L with per-sample error bounds); all NULL
+    // for the plain pass
+    const float *err;
+    const unsigned long long *bound_key;   // [slot][2]: max(lnL + err), max(lnL - err)
+    unsigned long long *exact_key;         // [slot]: exact FP64 maximum
+    const StarRec *stars;
+    const double *ep64;
+    const double *P, *E, *OM, *M0, *S;
+    int L, jit;
+    unsigned long long *n_refined;          // samples re-evaluated in FP64 (statistics)
+    uint32_t *amb_words;                    // undecided samples, one bit each (refinement)
     const joker_accept_seg *segs;
     const int64_t *blk_base;     // n_segs + 1 prefix of CTA counts
     int n_segs;

@@ -1,6 +1,6 @@
 // Marginal-likelihood kernels of libjoker_gb300 (sm_103a).
 //
-// Both kernels evaluate, for one star and one prior sample (P, e, omega, M0, s),
+// For one star and one prior sample (P, e, omega, M0, s) the kernels evaluate
 // the ln-likelihood with the linear parameters (K, v0, offsets, trend)
 // integrated out under their Gaussian prior -- the quantity the reference
 // computes in CJokerHelper.likelihood_worker (thejoker/src/fast_likelihood.pyx
@@ -13,116 +13,43 @@
 //   ln L   = -(chi2 + logdet) / 2
 //
 // Row 0 of M is the unit-K Kepler velocity, rows 1.. the trend/offset
-// columns.  Everything that does not depend on the sample (the trend block of
-// G, its inverse, the trend-only chi2) is folded per star on the host, so per
-// sample only the Schur complement s = G00 - g^T C^-1 g and one scalar
-// quadratic remain:  chi2 = chi2_0 - 2 mu0 u + mu0^2 (s - 1/Lambda0) - t^2 / s,
-// u = b0 - g^T C^-1 c,  t = u - mu0 (s - 1/Lambda0).
+// columns (row 1 is the constant v0 term).  Without jitter everything that
+// does not depend on the sample -- the trend block C of G, its inverse, the
+// trend-only chi2_0 -- is folded per star on the host, so per sample only the
+// Schur complement of the K column remains:
+//   s = A00 + 1/Lambda0 - g^T C^-1 g,   u = b0 - g^T C^-1 c,
+//   t = u - mu0 (s - 1/Lambda0),
+//   chi2 = chi2_0 - 2 mu0 u + mu0^2 (s - 1/Lambda0) - t^2 / s,
+//   log det G = log det C + log s.
+// With the jitter applied the weights change per sample and the full L x L
+// system is factorised per sample (LDL^T, K last).
 //
 // One thread owns one sample and walks the star's epochs, which the CTA
 // stages in shared memory; CTAs pull (star, sample-range) work items from a
 // global counter (a persistent launch sized to the SM count).
-#include "joker_internal.cuh"
-#include "joker_math.cuh"
+#include "joker_fp64.cuh"
 
 namespace joker {
 
 // ------------------------------------------------------------------ staging
 template <typename T, int REC>
 __device__ __forceinline__ void stage_epochs(T *sm, const T *src, int n) {
-    // n records of REC elements, copied with 16-byte vectors
     const int nvec = n * REC * (int)sizeof(T) / 16;
     const float4 *s4 = reinterpret_cast<const float4 *>(src);
     float4 *d4 = reinterpret_cast<float4 *>(sm);
     for (int i = threadIdx.x; i < nvec; i += blockDim.x) d4[i] = __ldg(s4 + i);
 }
 
-// Natural log of a positive double for the mixed path: the binary exponent is
-// taken exactly and only the mantissa in [1, 2) goes through FP32 logf, so the
-// absolute error stays near 1e-7 at any magnitude.
-__device__ __forceinline__ double log_mixed(double x) {
-    const int hi = __double2hiint(x);
-    const int ex = ((hi >> 20) & 0x7ff) - 1023;
-    const double m = __hiloint2double((hi & 0x800fffff) | 0x3ff00000, __double2loint(x));
-    if (ex == -1023 || ex == 1024) return log(x);   // zero, subnormal, inf, NaN
-    return (double)ex * 0.69314718055994530942 + (double)logf((float)m);
-}
-
-// Warp-aggregated update of the running maximum of one star.
-__device__ __forceinline__ void update_max(unsigned long long *max_key, double v, bool active) {
-    if (max_key == nullptr) return;
-    unsigned long long k = active ? double_to_key(v) : 0ull;
+// Warp-aggregated raise of a running maximum.
+__device__ __forceinline__ void warp_max_update(unsigned long long *key, unsigned long long k) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long other = __shfl_xor_sync(0xffffffffu, k, o);
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, k, o);
         k = other > k ? other : k;
     }
     if ((threadIdx.x & 31) == 0 && k != 0ull) {
-        if (k > *((volatile unsigned long long *)max_key)) atomicMax(max_key, k);
+        if (k > *((volatile unsigned long long *)key)) atomicMax(key, k);
     }
-}
-
-// Per-sample tail shared by both kernels (FP64): from the epoch sums
-// A00 = sum w m^2, A0j = sum w m T_j, b0 = sum w m y' and the star constants.
-template <int L, bool MIXED_LOG>
-__device__ __forceinline__ double lnl_tail_nojitter(const StarRec &st, double A00,
-                                                    const double *A0, double b0,
-                                                    double lam0, double log_lam0) {
-    // v = C^-1 g over the trend block (rows/cols 1..L-1)
-    double gv = 0.0, gcC = 0.0;
-#pragma unroll
-    for (int j = 1; j < L; ++j) {
-        double vj = 0.0;
-#pragma unroll
-        for (int k = 1; k < L; ++k) vj = fma(st.Cinv[j * MAXL + k], A0[k], vj);
-        gv = fma(A0[j], vj, gv);
-        gcC = fma(A0[j], st.cC[j], gcC);
-    }
-    const double a_minus = A00 - gv;           // s - 1/Lambda0
-    const double s = a_minus + 1.0 / lam0;
-    const double u = b0 - gcC;
-    const double mu0 = st.mu0;
-    const double t = fma(-mu0, a_minus, u);
-    double chi2 = st.chi2_0;
-    if (mu0 != 0.0) chi2 = fma(mu0 * mu0, a_minus, fma(-2.0 * mu0, u, chi2));
-    chi2 -= t * t / s;
-    const double logdet = st.logdet_const + log_lam0 + (MIXED_LOG ? log_mixed(s) : log(s));
-    return -0.5 * (chi2 + logdet);
-}
-
-// General tail (jitter applied): full L x L system, LDL^T factorisation.
-template <int L, bool MIXED_LOG>
-__device__ __forceinline__ double lnl_tail_full(const double (&G)[L][L], const double (&q)[L],
-                                                double rWr, double logdet_const) {
-    double D[L], Lw[L][L];
-    double logdet = logdet_const, quad = 0.0, detp = 1.0;
-#pragma unroll
-    for (int k = 0; k < L; ++k) {
-        double dk = G[k][k];
-#pragma unroll
-        for (int m = 0; m < k; ++m) dk = fma(-Lw[k][m] * Lw[k][m], D[m], dk);
-        D[k] = dk;
-        const double rdk = 1.0 / dk;
-#pragma unroll
-        for (int i = k + 1; i < L; ++i) {
-            double v = G[i][k];
-#pragma unroll
-            for (int m = 0; m < k; ++m) v = fma(-Lw[i][m] * Lw[k][m], D[m], v);
-            Lw[i][k] = v * rdk;
-        }
-        detp *= dk;
-    }
-    double z[L];
-#pragma unroll
-    for (int k = 0; k < L; ++k) {
-        double v = q[k];
-#pragma unroll
-        for (int m = 0; m < k; ++m) v = fma(-Lw[k][m], z[m], v);
-        z[k] = v;
-        quad = fma(v * v, 1.0 / D[k], quad);
-    }
-    logdet += (MIXED_LOG ? log_mixed(detp) : log(detp));
-    return -0.5 * (rWr - quad + logdet);
 }
 
 // ------------------------------------------------------------- K1: FP64 path
@@ -153,35 +80,10 @@ lnl_fp64_kernel(LnlArgs a) {
             const int j = base + threadIdx.x;
             const bool active = j < w.count;
             const int64_t row = w.row0 + (active ? j : 0);
-            const double P = a.P[row * a.stride], e = a.e[row * a.stride];
-            const double om = a.om[row * a.stride], M0 = a.M0[row * a.stride];
-            const double sj = JIT ? a.s[row * a.stride] : 0.0;
-            const double k2p = TWO_PI_D / P;
-            double sw, cw;
-            sincos(om, &sw, &cw);
-            const double sq1me2 = sqrt((1.0 - e) * (1.0 + e));
-            const double Ac = cw, Bc = -sw * sq1me2, Dc = e * cw;
-            // K prior variance (fast_likelihood.pyx:461-464)
-            double lam0;
-            if (st.k_scaled) {
-                const double v = st.sigK0sq / (1.0 - e * e) * pow(P / st.P0, -2.0 / 3.0);
-                lam0 = fmin(st.maxK2, v);
-            } else {
-                lam0 = st.lam0;
-            }
-            double A00 = 0.0, b0 = 0.0, A0[MAXL];
-#pragma unroll
-            for (int k = 0; k < MAXL; ++k) A0[k] = 0.0;
-            // jitter-applied sums (full system)
-            double G[L][L], q[L], rWr = 0.0, slw = 0.0;
-            if (JIT) {
-#pragma unroll
-                for (int i = 0; i < L; ++i) {
-                    q[i] = 0.0;
-#pragma unroll
-                    for (int k = 0; k < L; ++k) G[i][k] = 0.0;
-                }
-            }
+            const double P = a.P[row * a.stride];
+            Acc64<L, JIT> acc;
+            acc.init(st, P, a.e[row * a.stride], a.om[row * a.stride], a.M0[row * a.stride],
+                     JIT ? a.s[row * a.stride] : 0.0);
             for (int t0 = 0; t0 < N; t0 += TILE) {
                 const int nt = min(TILE, N - t0);
                 if (!single) {
@@ -192,72 +94,40 @@ lnl_fp64_kernel(LnlArgs a) {
                 if (active) {
                     for (int i = 0; i < nt; ++i) {
                         const double *rec = sm + i * REC64;
-                        const double dt = rec[0], yp = rec[1], iv = rec[2];
-                        double M = fma(dt, k2p, -M0);
-                        const double nrev = rint(M * INV_TWO_PI_D);
-                        M = fma(-nrev, TWO_PI_HI_D, M);
-                        M = fma(-nrev, TWO_PI_LO_D, M);
-                        double sE, cE;
-                        kepler_sincos_f64(M, e, sE, cE);
-                        const double den = 1.0 - e * cE;
-                        const double m = fma(Ac, cE, fma(Bc, sE, -Dc)) / den + Dc;
-                        if (!JIT) {
-                            const double wm = iv * m;
-                            A00 = fma(wm, m, A00);
-                            b0 = fma(wm, yp, b0);
-#pragma unroll
-                            for (int k = 1; k < L; ++k) A0[k] = fma(wm, rec[2 + k], A0[k]);
-                        } else {
-                            const double wj = iv / (1.0 + sj * sj * iv);
-                            slw += log(wj);
-                            double x[L];
-                            x[0] = m;
-#pragma unroll
-                            for (int k = 1; k < L; ++k) x[k] = rec[2 + k];
-                            // r = y' - mu0 m
-                            const double r = fma(-st.mu0, m, yp);
-                            rWr = fma(wj * r, r, rWr);
-#pragma unroll
-                            for (int ii = 0; ii < L; ++ii) {
-                                const double wx = wj * x[ii];
-                                q[ii] = fma(wx, r, q[ii]);
-#pragma unroll
-                                for (int k = 0; k <= ii; ++k) G[ii][k] = fma(wx, x[k], G[ii][k]);
-                            }
-                        }
+                        acc.add(rec[0], rec[1], rec[2], rec + 3);
                     }
                 }
             }
             double lnl = 0.0;
             if (active) {
-                if (!JIT) {
-                    lnl = lnl_tail_nojitter<L, false>(st, A00, A0, b0, lam0, log(lam0));
-                } else {
-#pragma unroll
-                    for (int ii = 0; ii < L; ++ii) {
-                        G[ii][ii] += 1.0 / (ii == 0 ? lam0 : st.lam[ii]);
-#pragma unroll
-                        for (int k = ii + 1; k < L; ++k) G[ii][k] = G[k][ii];
-                    }
-                    lnl = lnl_tail_full<L, false>(G, q, rWr, st.log_norm_rest + log(lam0) - slw);
-                }
+                lnl = acc.finish(st, P);
                 a.lnl[w.out_off + j] = lnl;
             }
-            update_max(mk, lnl, active);
+            if (mk) warp_max_update(mk, active ? double_to_key(lnl) : 0ull);
         }
     }
 }
 
 // ----------------------------------------------------------- K2: mixed path
 // Epoch record (REC32 floats), no jitter:
-//   dt_hi, dt_lo, w_hi, w_lo, wy_hi, wy_lo, (wT_j hi, lo) for j = 1..L-1
+//   dt_hi, dt_lo, w_hi, w_lo, wy_hi, wy_lo, (wT_j hi, lo) j = 1..L-1
 // with jitter:
-//   dt_hi, dt_lo, ivar, 0, y_hi, y_lo, (T_j hi, lo) for j = 1..L-1
-// Phase: frac(dt / P - M0 / 2 pi) in float-float (exact to ~2^-46 of the
-// cycle count), rounded once to FP32.  Kepler and the velocity column in
-// FP32; every epoch sum in float-float with exact products; the per-sample
-// tail in FP64.
-template <int L, bool JIT, bool ACC_SINCOS>
+//   dt_hi, dt_lo, ivar, 0, y_hi, y_lo, ysq_hi, ysq_lo, (T_j hi, lo) j = 1..L-1
+// VAR: 0 = MUFU sin/cos + float-float tail, 1 = correctly rounded sincosf +
+// float-float tail, 2 = MUFU sin/cos + FP64 tail.
+//
+// Error bound per sample.  The FP32 column m carries an error |dm| <= D with
+// D = c0 (1 + e) / (1 - e)^2 (phase rounding and FP32 Kepler, amplified near
+// pericentre of eccentric orbits); all epoch sums are exact functions of the
+// FP32 column.  To first order chi2 changes by -2 K_hat sum w res dm and
+// s by 2 sum w m_perp dm, so with W = sum ivar
+//   |d chi2| <= 2 |K_hat| D sqrt(W chi2) + K_hat^2 D^2 W
+//   |d s|    <= 2 D sqrt(W (s - 1/Lambda0)) + W D^2
+// and |d lnL| <= (|d chi2| + |d s| / (s - |d s|)) / 2 plus rounding terms.
+// With the jitter applied each weight w = ivar / (1 + s^2 ivar) is an FP32
+// value (relative error ~2^-22); the sums use it consistently, so chi2 moves
+// by sum dw res^2 <= 2e-7 chi2 and sum log w by the FP32 log2 error per epoch.
+template <int L, bool JIT, int VAR>
 __global__ void __launch_bounds__(128)
 lnl_mixed_kernel(LnlArgs a) {
     __shared__ __align__(16) float sm[TILE * REC32];
@@ -279,6 +149,9 @@ lnl_mixed_kernel(LnlArgs a) {
             __syncthreads();
         }
         unsigned long long *mk = a.max_key ? a.max_key + w.max_slot : nullptr;
+        unsigned long long *bk = a.bound_key ? a.bound_key + 2 * w.max_slot : nullptr;
+        const bool mu0z = st.mu0_zero != 0;
+        const float mu0f = st.mu0_f;
         for (int base = 0; base < w.count; base += blockDim.x) {
             const int j = base + threadIdx.x;
             const bool active = j < w.count;
@@ -290,19 +163,21 @@ lnl_mixed_kernel(LnlArgs a) {
             const float a1 = (float)MK_A1_D * fast_rcp(1.0f + e);
             const float sq1me2 = sqrtf(ome * (1.0f + e));
             const float Ac = pb.y, Bc = -pb.z * sq1me2, Dc = e * pb.y;
-            // accumulators (float-float)
+            // no jitter: A00 = sum w m^2, b0 = sum w m y', A0j = sum w m T_j
             float A00h = 0.f, A00l = 0.f, bh = 0.f, bl = 0.f;
             float Ah[MAXL], Al[MAXL];
 #pragma unroll
             for (int k = 0; k < MAXL; ++k) { Ah[k] = 0.f; Al[k] = 0.f; }
-            // jitter: full Gram matrix, q, r^T W r, sum log2(1 + s^2 ivar)
-            float Gh[L][L], Gl[L][L], qh[L], ql[L], rh = 0.f, rl = 0.f, lg2 = 0.f;
+            // jitter: sum w m^2, sum w r m, sum w m T_j, sum w T_j T_k,
+            // sum w r T_j, sum w r^2, sum log2(1 + s^2 ivar)
+            float GKKh = 0.f, GKKl = 0.f, qKh = 0.f, qKl = 0.f, rh = 0.f, rl = 0.f, lg2 = 0.f;
+            float GKh[MAXL], GKl[MAXL], GTh[MAXL][MAXL], GTl[MAXL][MAXL], qTh[MAXL], qTl[MAXL];
             if (JIT) {
 #pragma unroll
-                for (int i = 0; i < L; ++i) {
-                    qh[i] = ql[i] = 0.f;
+                for (int i = 0; i < MAXL; ++i) {
+                    GKh[i] = GKl[i] = qTh[i] = qTl[i] = 0.f;
 #pragma unroll
-                    for (int k = 0; k < L; ++k) Gh[i][k] = Gl[i][k] = 0.f;
+                    for (int k = 0; k < MAXL; ++k) GTh[i][k] = GTl[i][k] = 0.f;
                 }
             }
             for (int t0 = 0; t0 < N; t0 += TILE) {
@@ -331,70 +206,91 @@ lnl_mixed_kernel(LnlArgs a) {
                         const float M = __fmaf_rn(f, TWO_PI_HI_F, f * TWO_PI_LO_F);
                         // ---- Kepler + unit-K velocity
                         float sE, cE;
-                        kepler_sincos_f32<ACC_SINCOS>(M, e, ome, a1, sE, cE);
+                        kepler_sincos_f32<VAR == 1>(M, e, ome, a1, sE, cE);
                         const float den = __fmaf_rn(-e, cE, 1.0f);
                         float rd = fast_rcp(den);
                         rd = rd * __fmaf_rn(-den, rd, 2.0f);
                         const float m = __fmaf_rn(__fmaf_rn(Ac, cE, __fmaf_rn(Bc, sE, -Dc)), rd, Dc);
+                        const float4 r1 = *reinterpret_cast<const float4 *>(rec + 4);
                         if (!JIT) {
-                            const float4 r1 = *reinterpret_cast<const float4 *>(rec + 4);
-                            // t = w m exactly (two terms)
-                            float th, tl;
+                            float th, tl;                                 // w m, exact pair
                             two_prod(r0.z, m, th, tl);
                             tl = __fmaf_rn(r0.w, m, tl);
                             ff_acc(A00h, A00l, th, tl, m);
                             ff_acc(bh, bl, r1.x, r1.y, m);
-                            if (L > 1) ff_acc(Ah[1], Al[1], r1.z, r1.w, m);
+                            if (L > 1) ff_add(Ah[1], Al[1], th, tl);      // T_1 = 1
 #pragma unroll
                             for (int kk = 2; kk < L; ++kk)
                                 ff_acc(Ah[kk], Al[kk], rec[4 + 2 * kk], rec[5 + 2 * kk], m);
                         } else {
                             const float iv = r0.z;
                             const float onep = __fmaf_rn(s2, iv, 1.0f);
-                            const float wj = iv * fast_rcp(onep) ;   // the weight used consistently below
+                            float ro = fast_rcp(onep);
+                            ro = ro * __fmaf_rn(-onep, ro, 2.0f);
+                            const float wj = iv * ro;        // the weight, used consistently
                             lg2 += __log2f(onep);
-                            const float4 r1 = *reinterpret_cast<const float4 *>(rec + 4);
-                            // x = (m, T_1, ...), each as (hi, lo); y' as (hi, lo)
-                            float xh[L], xl[L];
-                            xh[0] = m; xl[0] = 0.f;
-#pragma unroll
-                            for (int kk = 1; kk < L; ++kk) { xh[kk] = rec[4 + 2 * kk]; xl[kk] = rec[5 + 2 * kk]; }
-                            // r = y' - mu0 m  (float-float)
-                            float rrh, rrl;
-                            two_prod(-(float)st.mu0, m, rrh, rrl);
-                            {
+                            // r = y' - mu0 m (float-float)
+                            float rrh = r1.x, rrl = r1.y;
+                            if (!mu0z) {
+                                float ph, pl;
+                                two_prod(-mu0f, m, ph, pl);
                                 float s_, e_;
-                                two_sum(r1.x, rrh, s_, e_);
-                                rrl = __fadd_rn(__fadd_rn(rrl, e_), r1.y);
+                                two_sum(rrh, ph, s_, e_);
+                                rrl = __fadd_rn(__fadd_rn(rrl, e_), pl);
                                 rrh = s_;
                             }
-                            // wr = w * r (float-float)
-                            float wrh, wrl;
+                            float wmh, wml;                                // w m, exact pair
+                            two_prod(wj, m, wmh, wml);
+                            float wrh, wrl;                                // w r
                             two_prod(wj, rrh, wrh, wrl);
                             wrl = __fmaf_rn(wj, rrl, wrl);
-                            // rWr += wr * r ; q_i += wr * x_i
-                            {
+                            ff_acc(GKKh, GKKl, wmh, wml, m);
+                            ff_acc(qKh, qKl, wrh, wrl, m);
+                            if (L > 1) {                                   // T_1 = 1
+                                ff_add(GKh[1], GKl[1], wmh, wml);
+                                float t_, tl_;
+                                two_sum(GTh[1][1], wj, t_, tl_);
+                                GTh[1][1] = t_;
+                                GTl[1][1] = __fadd_rn(GTl[1][1], tl_);
+                                ff_add(qTh[1], qTl[1], wrh, wrl);
+                            }
+                            if (mu0z) {                                    // r^2 = y'^2, stored
+                                const float p1 = __fmul_rn(wj, r1.z);
+                                float pe1 = __fmaf_rn(wj, r1.z, -p1);
+                                pe1 = __fmaf_rn(wj, r1.w, pe1);
+                                ff_add(rh, rl, p1, pe1);
+                            } else {
                                 const float p1 = __fmul_rn(wrh, rrh);
                                 float pe1 = __fmaf_rn(wrh, rrh, -p1);
                                 pe1 = __fmaf_rn(wrh, rrl, __fmaf_rn(wrl, rrh, pe1));
                                 ff_add(rh, rl, p1, pe1);
                             }
 #pragma unroll
-                            for (int ii = 0; ii < L; ++ii) {
-                                const float p1 = __fmul_rn(wrh, xh[ii]);
-                                float pe1 = __fmaf_rn(wrh, xh[ii], -p1);
-                                pe1 = __fmaf_rn(wrh, xl[ii], __fmaf_rn(wrl, xh[ii], pe1));
-                                ff_add(qh[ii], ql[ii], p1, pe1);
-                                // w x_i (float-float)
-                                float wxh, wxl;
-                                two_prod(wj, xh[ii], wxh, wxl);
-                                wxl = __fmaf_rn(wj, xl[ii], wxl);
+                            for (int ii = 2; ii < L; ++ii) {
+                                const float Th = rec[6 + 2 * ii], Tl = rec[7 + 2 * ii];
+                                {
+                                    const float p2 = __fmul_rn(wmh, Th);
+                                    float pe2 = __fmaf_rn(wmh, Th, -p2);
+                                    pe2 = __fmaf_rn(wmh, Tl, __fmaf_rn(wml, Th, pe2));
+                                    ff_add(GKh[ii], GKl[ii], p2, pe2);
+                                }
+                                {
+                                    const float p2 = __fmul_rn(wrh, Th);
+                                    float pe2 = __fmaf_rn(wrh, Th, -p2);
+                                    pe2 = __fmaf_rn(wrh, Tl, __fmaf_rn(wrl, Th, pe2));
+                                    ff_add(qTh[ii], qTl[ii], p2, pe2);
+                                }
+                                float wth, wtl;                            // w T_ii
+                                two_prod(wj, Th, wth, wtl);
+                                wtl = __fmaf_rn(wj, Tl, wtl);
+                                ff_add(GTh[ii][1], GTl[ii][1], wth, wtl);
 #pragma unroll
-                                for (int kk = 0; kk <= ii; ++kk) {
-                                    const float p2 = __fmul_rn(wxh, xh[kk]);
-                                    float pe2 = __fmaf_rn(wxh, xh[kk], -p2);
-                                    pe2 = __fmaf_rn(wxh, xl[kk], __fmaf_rn(wxl, xh[kk], pe2));
-                                    ff_add(Gh[ii][kk], Gl[ii][kk], p2, pe2);
+                                for (int kk = 2; kk <= ii; ++kk) {
+                                    const float Tkh = rec[6 + 2 * kk], Tkl = rec[7 + 2 * kk];
+                                    const float p2 = __fmul_rn(wth, Tkh);
+                                    float pe2 = __fmaf_rn(wth, Tkh, -p2);
+                                    pe2 = __fmaf_rn(wth, Tkl, __fmaf_rn(wtl, Tkh, pe2));
+                                    ff_add(GTh[ii][kk], GTl[ii][kk], p2, pe2);
                                 }
                             }
                         }
@@ -402,42 +298,147 @@ lnl_mixed_kernel(LnlArgs a) {
                 }
             }
             double lnl = 0.0;
+            float err = 0.0f;
             if (active) {
-                // K prior variance in log form: log Lambda0 (FP32 is ample here)
-                double log_lam0, lam0;
-                if (st.k_scaled) {
-                    log_lam0 = fmin(st.log_maxK2, st.log_kscale + (double)pb.w);
-                    lam0 = (double)expf((float)log_lam0);
-                } else {
-                    lam0 = st.lam0;
-                    log_lam0 = log(lam0);
-                }
-                if (!JIT) {
-                    double A0d[MAXL];
+                // K prior variance: log Lambda0 from the per-sample log g
+                float log_lam0f;
+                if (st.k_scaled) log_lam0f = fminf((float)st.log_maxK2, (float)st.log_kscale + pb.w);
+                else log_lam0f = (float)log(st.lam0);
+                const float ilam0 = expf(-log_lam0f);
+                float chi2f = 0.f, s_f = 1.f, amin_f = 0.f, Khat = 0.f, quadf = 0.f;
+                if (VAR == 2) {
+                    // FP64 tail (the literal FP64 form, kept for comparison)
+                    const double lam0 = st.k_scaled ? (double)expf(log_lam0f) : st.lam0;
+                    if (!JIT) {
+                        double A0d[MAXL];
 #pragma unroll
-                    for (int kk = 0; kk < MAXL; ++kk) A0d[kk] = ff_to_double(Ah[kk], Al[kk]);
-                    lnl = lnl_tail_nojitter<L, true>(st, ff_to_double(A00h, A00l), A0d,
-                                               ff_to_double(bh, bl), lam0, log_lam0);
-                } else {
-                    double G[L][L], q[L];
+                        for (int kk = 0; kk < MAXL; ++kk) A0d[kk] = ff_to_double(Ah[kk], Al[kk]);
+                        lnl = tail_schur_d<L, true>(st, ff_to_double(A00h, A00l), A0d,
+                                                    ff_to_double(bh, bl), lam0, (double)log_lam0f);
+                    } else {
+                        double G[L][L], q[L];
+                        G[0][0] = ff_to_double(GKKh, GKKl) + 1.0 / lam0;
+                        q[0] = ff_to_double(qKh, qKl);
 #pragma unroll
-                    for (int ii = 0; ii < L; ++ii) {
-                        q[ii] = ff_to_double(qh[ii], ql[ii]);
+                        for (int ii = 1; ii < L; ++ii) {
+                            G[ii][0] = G[0][ii] = ff_to_double(GKh[ii], GKl[ii]);
+                            q[ii] = ff_to_double(qTh[ii], qTl[ii]);
 #pragma unroll
-                        for (int kk = 0; kk <= ii; ++kk) {
-                            G[ii][kk] = ff_to_double(Gh[ii][kk], Gl[ii][kk]);
-                            G[kk][ii] = G[ii][kk];
+                            for (int kk = 1; kk <= ii; ++kk)
+                                G[ii][kk] = G[kk][ii] = ff_to_double(GTh[ii][kk], GTl[ii][kk]);
+                            G[ii][ii] += 1.0 / st.lam[ii];
                         }
-                        G[ii][ii] += 1.0 / (ii == 0 ? lam0 : st.lam[ii]);
+                        const double slw = st.sum_log_ivar - 0.6931471805599453 * (double)lg2;
+                        lnl = tail_full_d<L, true>(G, q, ff_to_double(rh, rl),
+                                                   st.log_norm_rest + (double)log_lam0f - slw);
                     }
-                    // sum log w = sum log ivar - ln2 * sum log2(1 + s^2 ivar)
+                    err = 1e30f;   // this variant states no per-sample bound
+                } else if (!JIT) {
+                    // float-float Schur-complement tail
+                    const ff A00 = ff_norm(A00h, A00l);
+                    const ff b0 = ff_norm(bh, bl);
+                    ff gv = ff_make(0.f, 0.f), gcC = ff_make(0.f, 0.f);
+#pragma unroll
+                    for (int jj = 1; jj < L; ++jj) {
+                        const ff gj = ff_norm(Ah[jj], Al[jj]);
+                        ff vj = ff_make(0.f, 0.f);
+#pragma unroll
+                        for (int kk = 1; kk < L; ++kk)
+                            vj = ff_addf(vj, ff_mulf(ff_make(st.Cinv_hi[jj * MAXL + kk],
+                                                             st.Cinv_lo[jj * MAXL + kk]),
+                                                     ff_norm(Ah[kk], Al[kk])));
+                        gv = ff_addf(gv, ff_mulf(gj, vj));
+                        gcC = ff_addf(gcC, ff_mulf(gj, ff_make(st.cC_hi[jj], st.cC_lo[jj])));
+                    }
+                    const ff amin = ff_subf(A00, gv);                    // s - 1/Lambda0
+                    const ff s = ff_addf(amin, ff_make(ilam0, 0.f));
+                    const ff u = ff_subf(b0, gcC);
+                    ff t = u;
+                    ff chi2 = ff_make(st.chi2_0_hi, st.chi2_0_lo);
+                    if (!mu0z) {
+                        t = ff_subf(u, ff_mul1(amin, mu0f));
+                        chi2 = ff_addf(chi2, ff_mul1(ff_subf(ff_mul1(amin, mu0f),
+                                                             ff_mul1(u, 2.0f)), mu0f));
+                    }
+                    chi2 = ff_subf(chi2, ff_divf(ff_mulf(t, t), s));
+                    const float logs = ff_log(s);
+                    lnl = -0.5 * (ff_to_d(chi2) + st.logdet_const + (double)log_lam0f + (double)logs);
+                    chi2f = chi2.hi;
+                    s_f = s.hi;
+                    amin_f = amin.hi;
+                    Khat = t.hi / s.hi;
+                    quadf = Khat * Khat * s_f;
+                } else {
+                    // float-float LDL^T, trend block 1..L-1 first, K last
+                    ff Dd[MAXL], Lw[MAXL][MAXL], lK[MAXL], z[MAXL];
+                    float logdet_G = 0.f;
+#pragma unroll
+                    for (int k = 1; k < L; ++k) {
+                        ff dk = ff_addf(ff_norm(GTh[k][k], GTl[k][k]), ff_make(st.ilam_hi[k], st.ilam_lo[k]));
+#pragma unroll
+                        for (int mm = 1; mm < k; ++mm) dk = ff_subf(dk, ff_mulf(ff_mulf(Lw[k][mm], Lw[k][mm]), Dd[mm]));
+                        Dd[k] = dk;
+#pragma unroll
+                        for (int i = k + 1; i < L; ++i) {
+                            ff v = ff_norm(GTh[i][k], GTl[i][k]);
+#pragma unroll
+                            for (int mm = 1; mm < k; ++mm) v = ff_subf(v, ff_mulf(ff_mulf(Lw[i][mm], Lw[k][mm]), Dd[mm]));
+                            Lw[i][k] = ff_divf(v, dk);
+                        }
+                        ff v = ff_norm(GKh[k], GKl[k]);
+#pragma unroll
+                        for (int mm = 1; mm < k; ++mm) v = ff_subf(v, ff_mulf(ff_mulf(lK[mm], Lw[k][mm]), Dd[mm]));
+                        lK[k] = ff_divf(v, dk);
+                        logdet_G += ff_log(dk);
+                    }
+                    ff amin = ff_norm(GKKh, GKKl);
+#pragma unroll
+                    for (int k = 1; k < L; ++k) amin = ff_subf(amin, ff_mulf(ff_mulf(lK[k], lK[k]), Dd[k]));
+                    const ff sK = ff_addf(amin, ff_make(ilam0, 0.f));
+                    ff zK = ff_norm(qKh, qKl);
+                    ff quad = ff_make(0.f, 0.f);
+#pragma unroll
+                    for (int k = 1; k < L; ++k) {
+                        ff v = ff_norm(qTh[k], qTl[k]);
+#pragma unroll
+                        for (int mm = 1; mm < k; ++mm) v = ff_subf(v, ff_mulf(Lw[k][mm], z[mm]));
+                        z[k] = v;
+                        quad = ff_addf(quad, ff_divf(ff_mulf(v, v), Dd[k]));
+                        zK = ff_subf(zK, ff_mulf(lK[k], v));
+                    }
+                    quad = ff_addf(quad, ff_divf(ff_mulf(zK, zK), sK));
+                    logdet_G += ff_log(sK);
+                    const ff chi2 = ff_subf(ff_norm(rh, rl), quad);
                     const double slw = st.sum_log_ivar - 0.6931471805599453 * (double)lg2;
-                    lnl = lnl_tail_full<L, true>(G, q, ff_to_double(rh, rl),
-                                                     st.log_norm_rest + log_lam0 - slw);
+                    lnl = -0.5 * (ff_to_d(chi2) + st.log_norm_rest + (double)log_lam0f +
+                                  (double)logdet_G - slw);
+                    chi2f = chi2.hi;
+                    s_f = sK.hi;
+                    amin_f = amin.hi;
+                    Khat = zK.hi / sK.hi;
+                    quadf = quad.hi;
+                }
+                if (VAR != 2) {
+                    const float D = a.err_c0 * (1.0f + e) / (ome * ome);
+                    const float Wsum = st.sum_ivar;
+                    const float c2 = fmaxf(chi2f, 0.f);
+                    const float dchi = 2.f * fabsf(Khat) * D * sqrtf(Wsum * c2) +
+                                       Khat * Khat * D * D * Wsum;
+                    const float ds = 2.f * D * sqrtf(Wsum * fmaxf(amin_f, 0.f)) + Wsum * D * D;
+                    const float room = s_f - ds;
+                    const float dlogs = (room > 1e-3f * s_f) ? ds / room : 1e30f;
+                    err = 0.5f * (dchi + dlogs) + 2e-6f + 2e-7f * (float)N +
+                          1e-12f * (fabsf(chi2f) + fabsf(quadf)) + (JIT ? 2e-7f * c2 : 0.f);
+                    if (!(err == err)) err = 1e30f;      // NaN inputs: no bound
                 }
                 a.lnl[w.out_off + j] = lnl;
+                if (a.err) a.err[w.out_off + j] = err;
             }
-            update_max(mk, lnl, active);
+            if (mk) warp_max_update(mk, active ? double_to_key(lnl) : 0ull);
+            if (bk) {
+                warp_max_update(bk, active ? double_to_key(lnl + (double)err) : 0ull);
+                warp_max_update(bk + 1, active ? double_to_key(lnl - (double)err) : 0ull);
+            }
         }
     }
 }
@@ -502,15 +503,18 @@ static cudaError_t launch_fp64_L(bool jit, const LnlArgs &a, int block, cudaStre
     return launch_persistent(lnl_fp64_kernel<L, false>, a, block, st);
 }
 
+template <int L, int VAR>
+static cudaError_t launch_mixed_LV(bool jit, const LnlArgs &a, int block, cudaStream_t st) {
+    if (jit) return launch_persistent(lnl_mixed_kernel<L, true, VAR>, a, block, st);
+    return launch_persistent(lnl_mixed_kernel<L, false, VAR>, a, block, st);
+}
+
 template <int L>
-static cudaError_t launch_mixed_L(bool jit, bool acc, const LnlArgs &a, int block,
+static cudaError_t launch_mixed_L(bool jit, int var, const LnlArgs &a, int block,
                                   cudaStream_t st) {
-    if (jit) {
-        if (acc) return launch_persistent(lnl_mixed_kernel<L, true, true>, a, block, st);
-        return launch_persistent(lnl_mixed_kernel<L, true, false>, a, block, st);
-    }
-    if (acc) return launch_persistent(lnl_mixed_kernel<L, false, true>, a, block, st);
-    return launch_persistent(lnl_mixed_kernel<L, false, false>, a, block, st);
+    if (var == 1) return launch_mixed_LV<L, 1>(jit, a, block, st);
+    if (var == 2) return launch_mixed_LV<L, 2>(jit, a, block, st);
+    return launch_mixed_LV<L, 0>(jit, a, block, st);
 }
 
 cudaError_t launch_lnl(int precision, int L, bool jit, const LnlArgs &a, int block,
@@ -525,14 +529,15 @@ cudaError_t launch_lnl(int precision, int L, bool jit, const LnlArgs &a, int blo
             case 6: return launch_fp64_L<6>(jit, a, block, st);
         }
     } else {
-        const bool acc = precision == JOKER_MIXED_ACCURATE;
+        const int var = precision == JOKER_MIXED_ACCURATE ? 1
+                      : precision == JOKER_MIXED_FP64_TAIL ? 2 : 0;
         switch (L) {
-            case 1: return launch_mixed_L<1>(jit, acc, a, block, st);
-            case 2: return launch_mixed_L<2>(jit, acc, a, block, st);
-            case 3: return launch_mixed_L<3>(jit, acc, a, block, st);
-            case 4: return launch_mixed_L<4>(jit, acc, a, block, st);
-            case 5: return launch_mixed_L<5>(jit, acc, a, block, st);
-            case 6: return launch_mixed_L<6>(jit, acc, a, block, st);
+            case 1: return launch_mixed_L<1>(jit, var, a, block, st);
+            case 2: return launch_mixed_L<2>(jit, var, a, block, st);
+            case 3: return launch_mixed_L<3>(jit, var, a, block, st);
+            case 4: return launch_mixed_L<4>(jit, var, a, block, st);
+            case 5: return launch_mixed_L<5>(jit, var, a, block, st);
+            case 6: return launch_mixed_L<6>(jit, var, a, block, st);
         }
     }
     return cudaErrorInvalidValue;

@@ -168,3 +168,75 @@ __device__ __forceinline__ double pcg_uniform(uint64_t x) {
 }
 
 }  // namespace joker
+
+namespace joker {
+
+// ------------------------------------------------------ float-float numbers
+// A value hi + lo with |lo| <= ulp(hi)/2 after normalisation: a 48-bit
+// significand with FP32 exponent range (Dekker 1971; Hida, Li and Bailey,
+// "Library for double-double and quad-double arithmetic", 2001).
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_make(float hi, float lo) { ff r; r.hi = hi; r.lo = lo; return r; }
+
+// requires |a| >= |b| or a == 0
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return ff_make(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+
+__device__ __forceinline__ ff ff_norm(float hi, float lo) {
+    float s, e;
+    two_sum(hi, lo, s, e);
+    return ff_make(s, e);
+}
+
+__device__ __forceinline__ ff ff_addf(ff a, ff b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    return fast_two_sum(s, e);
+}
+
+__device__ __forceinline__ ff ff_neg(ff a) { return ff_make(-a.hi, -a.lo); }
+
+__device__ __forceinline__ ff ff_subf(ff a, ff b) { return ff_addf(a, ff_neg(b)); }
+
+__device__ __forceinline__ ff ff_mulf(ff a, ff b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ ff ff_mul1(ff a, float b) {
+    const float p = __fmul_rn(a.hi, b);
+    float e = __fmaf_rn(a.hi, b, -p);
+    e = __fmaf_rn(a.lo, b, e);
+    return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ ff ff_divf(ff a, ff b) {
+    const float r = __frcp_rn(b.hi);
+    const float q1 = __fmul_rn(a.hi, r);
+    const ff rem = ff_subf(a, ff_mul1(b, q1));
+    const float q2 = __fmul_rn(rem.hi, r);
+    return fast_two_sum(q1, q2);
+}
+
+__device__ __forceinline__ double ff_to_d(ff a) { return (double)a.hi + (double)a.lo; }
+
+// Natural log of a positive float-float number to about 1e-7 absolute: the
+// binary exponent is exact, the mantissa goes through logf, the low word
+// through log(1 + x) ~ x.
+__device__ __forceinline__ float ff_log(ff a) {
+    const int bits = __float_as_int(a.hi);
+    const int ex = ((bits >> 23) & 0xff) - 127;
+    const float m = __int_as_float((bits & 0x807fffff) | 0x3f800000);   // [1, 2)
+    return (float)ex * 0.69314718f + logf(m) + a.lo / a.hi;
+}
+
+}  // namespace joker

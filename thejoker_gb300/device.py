@@ -134,7 +134,8 @@ class PriorCache:
 
 
 PRECISIONS = {"fp64": nat.JOKER_FP64, "mixed": nat.JOKER_MIXED,
-              "mixed_accurate": nat.JOKER_MIXED_ACCURATE}
+              "mixed_accurate": nat.JOKER_MIXED_ACCURATE,
+              "mixed_fp64_tail": nat.JOKER_MIXED_FP64_TAIL}
 
 
 class MaxKeys:
@@ -152,9 +153,12 @@ class MaxKeys:
 
 
 def lnl(stars, cache, out, precision="fp64", star0=0, n_sel=None, row0=0, count=None,
-        max_keys=None, chunk=0, stream=None):
+        max_keys=None, err=None, bound_keys=None, chunk=0, stream=None):
     """ln L of stars [star0, star0 + n_sel) over cache rows [row0, row0 + count)
-    into ``out`` (a float64 CUDA tensor of shape (n_sel, ld))."""
+    into ``out`` (a float64 CUDA tensor of shape (n_sel, ld)).  Mixed
+    precisions can also write a per-sample error bound into ``err`` (float32,
+    same shape) and the per-star maxima of lnL +- err into ``bound_keys``
+    (a MaxKeys of 2 n_sel entries)."""
     n_sel = stars.n_stars - star0 if n_sel is None else n_sel
     count = cache.size - row0 if count is None else count
     if out.dtype != torch.float64 or out.dim() != 2 or out.shape[0] < n_sel or out.shape[1] < count:
@@ -164,7 +168,9 @@ def lnl(stars, cache, out, precision="fp64", star0=0, n_sel=None, row0=0, count=
     nat.check(nat.lib().joker_lnl(
         stars.handle, cache.handle, int(star0), int(n_sel), int(row0), int(count),
         PRECISIONS[precision], ctypes.c_void_p(out.data_ptr()), out.shape[1],
-        max_keys.ptr() if max_keys is not None else None, 0, int(chunk),
+        max_keys.ptr() if max_keys is not None else None,
+        ctypes.c_void_p(err.data_ptr()) if err is not None else None,
+        bound_keys.ptr() if bound_keys is not None else None, 0, int(chunk),
         stream_handle(stream)), "joker_lnl")
     return out
 
@@ -208,14 +214,7 @@ def pcg64_fields(state, inc, offset=0):
 
 
 # ----------------------------------------------------------------- acceptance
-def accept(lnl_buf, max_keys, segments, u_source="pcg64", u=None, out_idx=None, out_lnl=None,
-           counts=None, stream=None):
-    """Run the acceptance pass (joker_accept) over ``segments``.
-
-    Each segment is a dict with lnl_off, n, idx_base, out_off, max_out,
-    max_slot and either u_off (u_source="array") or pcg=(state, inc, offset).
-    Returns (out_idx, out_lnl, counts) CUDA tensors.
-    """
+def _segments(segments, u_source):
     ns = len(segments)
     arr = (nat.AcceptSeg * ns)()
     total_out = 0
@@ -225,10 +224,58 @@ def accept(lnl_buf, max_keys, segments, u_source="pcg64", u=None, out_idx=None, 
         a.out_off, a.max_out = int(sg["out_off"]), int(sg["max_out"])
         a.u_off = int(sg.get("u_off", 0))
         a.max_slot = int(sg.get("max_slot", 0))
+        a.star = int(sg.get("star", 0))
+        a.row0 = int(sg.get("row0", 0))
         if u_source == "pcg64":
             st, inc, off = sg["pcg"]
             a.pcg_state_hi, a.pcg_state_lo, a.pcg_inc_hi, a.pcg_inc_lo = pcg64_fields(st, inc, off)
         total_out = max(total_out, a.out_off + a.max_out)
+    return arr, total_out
+
+
+def accept_refined(stars, cache, lnl_buf, err, bound_keys, segments, u_source="pcg64", u=None,
+                   out_idx=None, out_lnl=None, counts=None, stream=None):
+    """Acceptance over mixed-precision ln L with its error bounds, exact with
+    respect to FP64 (joker_accept_refined).  Each segment also names its
+    ``star`` and the cache ``row0`` of its first sample.  Returns (out_idx,
+    out_lnl, counts, exact_max_keys, n_refined)."""
+    ns = len(segments)
+    arr, total_out = _segments(segments, u_source)
+    n_slots = max(int(sg.get("max_slot", 0)) for sg in segments) + 1
+    dev = lnl_buf.device
+    if out_idx is None:
+        out_idx = torch.empty(max(total_out, 1), dtype=torch.int64, device=dev)
+    if counts is None:
+        counts = torch.empty(ns, dtype=torch.int64, device=dev)
+    exact = MaxKeys(n_slots)
+    n_ref = torch.zeros(1, dtype=torch.int64, device=dev)
+    wbytes = nat.lib().joker_accept_workspace(arr, ns)
+    work = torch.empty(max(int(wbytes), 1), dtype=torch.uint8, device=dev)
+    usrc = nat.JOKER_U_PCG64 if u_source == "pcg64" else nat.JOKER_U_ARRAY
+    nat.check(nat.lib().joker_accept_refined(
+        stars.handle, cache.handle, arr, ns, ctypes.c_void_p(lnl_buf.data_ptr()),
+        ctypes.c_void_p(err.data_ptr()), bound_keys.ptr(), exact.ptr(), n_slots, usrc,
+        ctypes.c_void_p(u.data_ptr()) if u is not None else None,
+        ctypes.c_void_p(out_idx.data_ptr()),
+        ctypes.c_void_p(out_lnl.data_ptr()) if out_lnl is not None else None,
+        ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(n_ref.data_ptr()),
+        ctypes.c_void_p(work.data_ptr()), int(wbytes), stream_handle(stream)),
+        "joker_accept_refined")
+    if stream is not None:
+        work.record_stream(stream)
+    return out_idx, out_lnl, counts, exact, n_ref
+
+
+def accept(lnl_buf, max_keys, segments, u_source="pcg64", u=None, out_idx=None, out_lnl=None,
+           counts=None, stream=None):
+    """Run the acceptance pass (joker_accept) over ``segments``.
+
+    Each segment is a dict with lnl_off, n, idx_base, out_off, max_out,
+    max_slot and either u_off (u_source="array") or pcg=(state, inc, offset).
+    Returns (out_idx, out_lnl, counts) CUDA tensors.
+    """
+    ns = len(segments)
+    arr, total_out = _segments(segments, u_source)
     dev = lnl_buf.device
     if out_idx is None:
         out_idx = torch.empty(max(total_out, 1), dtype=torch.int64, device=dev)

@@ -66,33 +66,34 @@ class TheJoker:
         return helper.batch_marginal_ln_likelihood(self._packed(prior_samples, helper))
 
     # -------------------------------------------------------------- acceptance
-    def _accept_device(self, lnl, n, max_keys, max_out):
+    def _accept_device(self, st, n, max_out):
         """Indices (ascending, at most max_out) with exp(lnl - max) > uu, uu the
-        next n uniforms of self.rng; advances self.rng past them."""
+        next n uniforms of self.rng; advances self.rng past them.  Mixed ln L
+        go through the refined pass, which keeps what the FP64 path keeps."""
         pcg = dev.pcg64_state(self.rng)
-        seg = dict(lnl_off=0, n=n, idx_base=0, out_off=0, max_out=max_out, max_slot=0)
+        seg = dict(lnl_off=0, n=n, idx_base=0, out_off=0, max_out=max_out, max_slot=0, star=0,
+                   row0=0)
+        kw = {}
         if pcg is not None:
             seg["pcg"] = (pcg[0], pcg[1], 0)
-            out_idx, _, counts = dev.accept(lnl, max_keys, [seg], u_source="pcg64")
-            dev.pcg64_advance_generator(self.rng, n)
+            kw["u_source"] = "pcg64"
         else:
-            uu = torch.from_numpy(self.rng.uniform(size=n)).cuda()
             seg["u_off"] = 0
-            out_idx, _, counts = dev.accept(lnl, max_keys, [seg], u_source="array", u=uu)
+            kw["u_source"] = "array"
+            kw["u"] = torch.from_numpy(self.rng.uniform(size=n)).cuda()
+        if st.err is None:
+            out_idx, _, counts = dev.accept(st.lnl, st.max_keys, [seg], **kw)
+        else:
+            out_idx, _, counts, _, _ = dev.accept_refined(st.stars, st.cache, st.lnl, st.err,
+                                                         st.bound_keys, [seg], **kw)
+        if pcg is not None:
+            dev.pcg64_advance_generator(self.rng, n)
         count = int(counts[0].item())
         return out_idx[:min(count, max_out)].cpu().numpy()
 
-    def _lnl_device(self, helper, chunk_dev, out=None, max_keys=None):
-        """ln L on the device; raises the running maximum in ``max_keys``."""
-        S = chunk_dev.shape[0]
-        if out is None:
-            out = torch.empty(S, dtype=torch.float64, device="cuda")
-        if max_keys is None:
-            max_keys = dev.MaxKeys(1)
-        cache = dev.PriorCache.from_samples(chunk_dev)
-        dev.lnl(helper.stars, cache, out.view(1, S), precision=helper.precision,
-                max_keys=max_keys)
-        return out, max_keys
+    def _device_state(self, helper, chunk_dev):
+        """Prior cache, ln L buffer and running maxima for one call."""
+        return _CallState(helper, chunk_dev)
 
     def _full_samples(self, helper, chunk, n_linear_samples):
         raw, _ = helper.batch_get_posterior_samples(chunk, n_linear_samples, self.rng)
@@ -121,8 +122,10 @@ class TheJoker:
         if max_posterior_samples is None:
             max_posterior_samples = S
         d_chunk = torch.from_numpy(chunk).pin_memory().to("cuda", non_blocking=True)
-        lnl, max_keys = self._lnl_device(helper, d_chunk)
-        good = self._accept_device(lnl, S, max_keys, max_posterior_samples)
+        st = self._device_state(helper, d_chunk)
+        st.evaluate(0, S)
+        good = self._accept_device(st, S, max_posterior_samples)
+        lnl = st.lnl
         samples = self._full_samples(helper, chunk[good], n_linear_samples)
         if return_logprobs:
             lls = lnl.cpu().numpy()
@@ -156,18 +159,17 @@ class TheJoker:
                              f"samples cache file. You have, or have limited to, {n_total} "
                              "samples.")
         d_chunk = torch.from_numpy(chunk).pin_memory().to("cuda", non_blocking=True)
-        lnl_all = torch.empty(n_total, dtype=torch.float64, device="cuda")
-        max_keys = dev.MaxKeys(1)
+        st = self._device_state(helper, d_chunk)
+        lnl_all = st.lnl
         start = 0
         good = None
         for i in range(maxiter):
-            self._lnl_device(helper, d_chunk[start:start + n_process],
-                             out=lnl_all[start:start + n_process], max_keys=max_keys)
+            st.evaluate(start, n_process)
             n_evals = start + n_process
             if not torch.isfinite(lnl_all[:n_evals]).all():
                 # the reference returns (does not raise) this error object
                 return RuntimeError(f"There are NaN or Inf likelihood values in iteration step {i}!")
-            good = self._accept_device(lnl_all, n_evals, max_keys, n_evals)
+            good = self._accept_device(st, n_evals, n_evals)
             if len(good) == 0:
                 raise RuntimeError("Failed to find any good samples!")
             n_good = len(good)
@@ -187,3 +189,31 @@ class TheJoker:
         if return_logprobs:
             samples["ln_likelihood"] = np.repeat(lnl_all[good].cpu().numpy(), n_linear_samples)
         return samples
+
+
+
+class _CallState:
+    """Device state of one sampling call: the prior cache (all rows), the ln L
+    buffer, its error bounds (mixed precision) and the running maxima."""
+
+    def __init__(self, helper, chunk_dev):
+        S = chunk_dev.shape[0]
+        self.stars = helper.stars
+        self.precision = helper.precision
+        self.cache = dev.PriorCache.from_samples(chunk_dev)
+        self.lnl = torch.empty(S, dtype=torch.float64, device="cuda")
+        self.max_keys = dev.MaxKeys(1)
+        if self.precision == "fp64" or self.precision == "mixed_fp64_tail":
+            self.err = None
+            self.bound_keys = None
+        else:
+            self.err = torch.empty(S, dtype=torch.float32, device="cuda")
+            self.bound_keys = dev.MaxKeys(2)
+
+    def evaluate(self, row0, count):
+        if count <= 0:
+            return
+        out = self.lnl[row0:row0 + count].view(1, count)
+        err = self.err[row0:row0 + count].view(1, count) if self.err is not None else None
+        dev.lnl(self.stars, self.cache, out, precision=self.precision, row0=row0, count=count,
+                max_keys=self.max_keys, err=err, bound_keys=self.bound_keys)
