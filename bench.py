@@ -195,34 +195,23 @@ def run_ours(args, rank, world, dist):
         stage[: b - a].copy_(host[a:b], non_blocking=True)
         cache.load(stage[: b - a], row0=a)
     torch.cuda.synchronize()
-    lnl = torch.empty((1, S), dtype=torch.float64, device="cuda")
-    keys = dev.MaxKeys(1)
-    gen = np.random.default_rng(1000 + rank)
+    from thejoker_gb300.batch import BatchRejection
+    from thejoker_gb300.parallel import ShardedRejection
+    gen = np.random.default_rng(1000)
     pcg_state, pcg_inc = dev.pcg64_state(gen)
-    seg = dict(lnl_off=0, n=S, idx_base=0, out_off=0, max_out=S, max_slot=0,
-               pcg=(pcg_state, pcg_inc, 0))
-    out_idx = torch.empty(S, dtype=torch.int64, device="cuda")
-    counts = torch.empty(1, dtype=torch.int64, device="cuda")
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    del stage
+    torch.cuda.empty_cache()
+    if world > 1:
+        runner = ShardedRejection(table, cache, row0=rank * S, precision="mixed", max_out=S)
+    else:
+        runner = BatchRejection(table, cache, precision="mixed", max_out=S, seeds=[1000],
+                                timing=True)
     lnl_ms = []
 
-    def step(precision="mixed", count=S, timing=False):
-        keys.t.zero_()
-        if timing:
-            ev[0].record()
-        dev.lnl(table, cache, lnl, precision=precision, count=count, max_keys=keys)
-        if timing:
-            ev[1].record()
-        if dist is not None and world > 1:
-            # keys order as unsigned 64-bit integers; flip the top bit so that
-            # the signed MAX of the all-reduce keeps that order
-            flip = torch.tensor(-(1 << 63), dtype=torch.int64, device="cuda")
-            m = torch.bitwise_xor(keys.t, flip)
-            dist.all_reduce(m, op=dist.ReduceOp.MAX)
-            keys.t.copy_(torch.bitwise_xor(m, flip))
-        sg = dict(seg)
-        sg["n"] = count
-        dev.accept(lnl, keys, [sg], u_source="pcg64", out_idx=out_idx, counts=counts)
+    def step():
+        if world > 1:
+            return runner.run((pcg_state, pcg_inc))
+        runner.run()
 
     def barrier():
         if dist is not None and world > 1:
@@ -239,41 +228,63 @@ def run_ours(args, rank, world, dist):
         barrier()
         t0.record()
         for _ in range(args.steps):
-            step(timing=True)
-            torch.cuda.synchronize()
-            lnl_ms.append(ev[0].elapsed_time(ev[1]))
+            step()
         t1.record()
         barrier()
     ms = t0.elapsed_time(t1) / args.steps
-    n_acc = int(counts.item())
+    if world == 1:
+        lnl_ms.append(runner.lnl_ms())
+        n_acc = int(runner.counts[0].item())
+    else:
+        lnl_ms.append(float("nan"))
+        n_acc = None
 
-    # ---- e2e: pinned host chunk -> device -> prepare -> lnL -> accept -> host indices
-    def e2e_step():
-        for a in range(0, S, args.h2d_chunk):
-            b = min(S, a + args.h2d_chunk)
-            stage[: b - a].copy_(host[a:b], non_blocking=True)
-            cache.load(stage[: b - a], row0=a)
-        step()
-        c = int(counts.item())
-        return out_idx[: min(c, S)].cpu()
+    # ---- e2e: pinned host chunk -> device (sliced, copies overlapped with the
+    # preparation and ln L of the previous slice) -> acceptance -> host indices
+    from thejoker_gb300.pipeline import HostRejection
+    if world == 1:
+        del runner, cache
+        torch.cuda.empty_cache()
+        hr = HostRejection(table, S, precision="mixed", slice_rows=args.h2d_chunk, max_out=S)
 
+        def e2e_step():
+            hr.run(host, [(pcg_state, pcg_inc)])
+            return hr.d2h_bytes
+    else:
+        # each rank streams its shard into its cache, then the sharded pass
+        # exchanges the maximum and accepts
+        stage = torch.empty((args.h2d_chunk, 5), dtype=torch.float64, device="cuda")
+
+        def e2e_step():
+            for a0 in range(0, S, args.h2d_chunk):
+                b0 = min(S, a0 + args.h2d_chunk)
+                stage[: b0 - a0].copy_(host[a0:b0], non_blocking=True)
+                cache.load(stage[: b0 - a0], row0=a0)
+            idx, _ = runner.run((pcg_state, pcg_inc))
+            return len(idx) * 8 + 8
     for _ in range(max(1, args.warmup // 2)):
         e2e_step()
     barrier()
     te0 = time.perf_counter()
     for _ in range(args.steps):
-        res = e2e_step()
+        d2h = e2e_step()
     barrier()
     e2e_ms = (time.perf_counter() - te0) * 1e3 / args.steps
-    d2h = int(res.numel()) * 8 + 8
+    if world == 1:
+        del hr
+    else:
+        del runner, cache, stage
+    torch.cuda.empty_cache()
+    cache = dev.PriorCache(min(S, args.fp64_samples)).load(host[:min(S, args.fp64_samples)].cuda())
 
-    # ---- plain FP64 GPU path on a slice of the same workload
+    # ---- plain FP64 GPU path on a slice of the same workload (ln L + accept)
     S64 = min(S, args.fp64_samples)
-    step("fp64", S64)
+    b64 = BatchRejection(table, cache, precision="fp64", max_out=S64, seeds=[1000])
+    b64.run(count=S64)
     barrier()
     f0 = time.perf_counter()
     for _ in range(2):
-        step("fp64", S64)
+        b64.run(count=S64)
     barrier()
     fp64_ms = (time.perf_counter() - f0) * 1e3 / 2
 
@@ -310,14 +321,15 @@ def run_ours(args, rank, world, dist):
                                f"applied, prior cache 2^{int(math.log2(S))} samples per GPU",
                    "prior_samples_per_gpu": S, "n_epochs": N_EPOCHS, "n_linear": 2,
                    "l2": "inputs larger than L2 (cache 76 B/sample resident, 2^28 samples)",
-                   "precision": "mixed", "u_source": "numpy PCG64 stream regenerated on device"},
+                   "precision": "mixed", "u_source": "numpy PCG64 stream regenerated on device",
+                   "accept": "refined to the FP64 decisions"},
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "samples/s",
                 "h2d_bytes_per_step": S * 40, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms},
         "fp64": {"value": S64 * world / (fp64_ms * 1e-3), "unit": "samples/s",
                  "samples": S64, "ms_per_step": fp64_ms},
         "accepted_per_step": n_acc,
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": 6 * args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": args.traffic,
                      "kernel": "lnl_mixed_kernel<2,true,false>",
@@ -436,7 +448,7 @@ def main():
     p.add_argument("--samples", type=int, default=1 << 28)
     p.add_argument("--fp64-samples", type=int, default=1 << 25)
     p.add_argument("--cpu-samples", type=int, default=1 << 20)
-    p.add_argument("--h2d-chunk", type=int, default=1 << 25)
+    p.add_argument("--h2d-chunk", type=int, default=1 << 24)
     p.add_argument("--fp32-peak", type=float, default=67.6)
     p.add_argument("--traffic", type=float, default=None)
     p.add_argument("--no-cpu", action="store_true")

@@ -178,15 +178,26 @@ int joker_accept(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
  * reach it, and every sample whose decision the interval leaves open is
  * re-evaluated in FP64 from the cache (seg.star, seg.row0 locate it).  The
  * kept indices are then those the FP64 path would keep.  d_exact_key (one per
- * max_slot) receives the FP64 maxima; d_n_refined (optional) counts the
- * re-evaluated samples.  Same workspace as joker_accept. */
+ * max_slot) receives the FP64 maxima -- or, with max_given != 0, already holds
+ * them (from joker_refine_max, e.g. combined over ranks that each own a range
+ * of the same star's samples).  d_n_refined (optional) counts the re-evaluated
+ * samples.  Same workspace as joker_accept. */
 int joker_accept_refined(const joker_stars *stars, const joker_cache *cache,
                          const joker_accept_seg *segs, int n_segs, const double *d_lnl,
                          const float *d_err, const uint64_t *d_bound_key,
-                         uint64_t *d_exact_key, int n_slots, int u_source,
+                         uint64_t *d_exact_key, int n_slots, int max_given, int u_source,
                          const double *d_u, int64_t *d_out_idx, double *d_out_lnl,
                          int64_t *d_count, uint64_t *d_n_refined, void *d_work,
                          int64_t work_bytes, void *stream);
+
+/* The first step of joker_accept_refined alone: raise d_exact_key[slot] to the
+ * FP64 maximum over the samples of the segments whose interval
+ * [lnL - err, lnL + err] reaches the slot's largest lower bound (d_bound_key).
+ * d_exact_key must be zeroed (or hold a smaller maximum) before the call. */
+int joker_refine_max(const joker_stars *stars, const joker_cache *cache,
+                     const joker_accept_seg *segs, int n_segs, const double *d_lnl,
+                     const float *d_err, const uint64_t *d_bound_key, uint64_t *d_exact_key,
+                     uint64_t *d_n_refined, void *d_work, int64_t work_bytes, void *stream);
 
 /* ---- acceptance without allocation ---------------------------------------
  * No counterpart in the reference.  joker_accept_noalloc is joker_accept for

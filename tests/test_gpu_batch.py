@@ -56,3 +56,29 @@ def test_batch_rows_subrange(cuda):
         good = np.where(np.exp(lls - lls.max()) > uu)[0] + 1000
         assert counts[k] == len(good)
         np.testing.assert_array_equal(idx[k], good[:1000])
+
+
+def test_host_pipeline_matches_batch(cuda):
+    """Streaming a host chunk in slices (copies overlapped with ln L) gives the
+    same accepted indices as the resident-cache path."""
+    from thejoker_gb300 import device as dev
+    from thejoker_gb300.batch import BatchRejection
+    from thejoker_gb300.pipeline import HostRejection
+    from thejoker_gb300.synthetic import fill_prior_cache, survey_stars
+    stars = survey_stars(6, seed=12, n_max=40)
+    S = 100_000
+    chunk = fill_prior_cache(np.empty((S, 5)), 6)
+    table = dev.StarTable(stars)
+    seeds = [11, 12, 13, 14, 15, 16]
+    host = torch.from_numpy(chunk).pin_memory()
+    for prec in ("mixed", "fp64"):
+        hr = HostRejection(table, S, precision=prec, slice_rows=30_000, max_out=500)
+        pcg = [dev.pcg64_state(np.random.default_rng(sd)) for sd in seeds]
+        counts, idx = hr.run(host, pcg)
+        cache = dev.PriorCache.from_samples(chunk)
+        b = BatchRejection(table, cache, precision=prec, max_out=500, seeds=seeds)
+        b.run()
+        c2, i2, _ = b.results()
+        np.testing.assert_array_equal(counts, c2)
+        for k in range(6):
+            np.testing.assert_array_equal(idx[k], i2[k])

@@ -25,6 +25,7 @@ EXPORTED = (
     "joker_stars_info", "joker_cache_create", "joker_cache_destroy", "joker_cache_load",
     "joker_cache_capacity", "joker_batch_marginal_ln_likelihood", "joker_lnl",
     "joker_key_to_double", "joker_accept_workspace", "joker_accept", "joker_accept_refined",
+    "joker_refine_max",
     "joker_accept_noalloc",
 )
 
@@ -70,8 +71,11 @@ _SIGS = {
     "joker_accept": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                     ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
     "joker_accept_refined": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(AcceptSeg), ctypes.c_int,
-                                            _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp,
-                                            _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
+                                            _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _i64,
+                                            _vp]),
+    "joker_refine_max": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp,
+                                        _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
     "joker_accept_noalloc": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                             ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

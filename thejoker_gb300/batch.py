@@ -42,7 +42,7 @@ class BatchRejection:
     """
 
     def __init__(self, stars, cache, precision="mixed", jitter="reference", group=None,
-                 max_out=256, seeds=None, chunk=0):
+                 max_out=256, seeds=None, chunk=0, timing=False):
         self.table = stars if isinstance(stars, dev.StarTable) else dev.StarTable(stars,
                                                                                   jitter=jitter)
         self.cache = cache
@@ -73,12 +73,16 @@ class BatchRejection:
                                    device="cuda")
         self.counts = torch.zeros(self.n_stars, dtype=torch.int64, device="cuda")
         self.n_refined = 0
+        # CUDA events around each group's ln L launch (for kernel timing)
+        self.timing = timing
+        self.lnl_events = []
 
     def run(self, row0=0, count=None, stream=None):
         """Evaluate every star over cache rows [row0, row0 + count) and accept.
         Results stay on the device (``out_idx``, ``out_lnl``, ``counts``)."""
         S = self.cache.size - row0 if count is None else int(count)
         refined = torch.zeros(1, dtype=torch.int64, device="cuda")
+        self.lnl_events = []
         for g0 in range(0, self.n_stars, self.group):
             n = min(self.group, self.n_stars - g0)
             self.keys.t.zero_()
@@ -87,10 +91,16 @@ class BatchRejection:
             lnl = self.lnl[:n, :S]
             err = self.err[:n, :S] if self.err is not None else None
             out = self.lnl[:n]
+            if self.timing:
+                ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                ev[0].record(stream)
             dev.lnl(self.table, self.cache, out, precision=self.precision, star0=g0, n_sel=n,
                     row0=row0, count=S, max_keys=self.keys,
                     err=self.err[:n] if err is not None else None, bound_keys=self.bkeys,
                     chunk=self.chunk, stream=stream)
+            if self.timing:
+                ev[1].record(stream)
+                self.lnl_events.append(ev)
             ld = self.lnl.shape[1]
             segs = []
             for k in range(n):
@@ -120,6 +130,10 @@ class BatchRejection:
         k = np.minimum(counts, self.max_out)
         return counts, [idx[i, :k[i]] for i in range(self.n_stars)], \
             [ll[i, :k[i]] for i in range(self.n_stars)]
+
+    def lnl_ms(self):
+        """Device time of the last run's ln L launches (needs timing=True)."""
+        return sum(a.elapsed_time(b) for a, b in self.lnl_events)
 
     @property
     def n_refined_last(self):

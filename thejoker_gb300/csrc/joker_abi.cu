@@ -17,7 +17,9 @@ cudaError_t launch_lnl(int precision, int L, bool jit, const LnlArgs &a, int blo
 cudaError_t launch_prepare(const double *chunk, int64_t n, int64_t row0, double *P, double *E,
                            double *OM, double *M0, double *S, float4 *mx_a, float4 *mx_b,
                            float *mx_s2, cudaStream_t st);
-cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st);
+cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st,
+                          bool max_given = false);
+cudaError_t launch_refine_max(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st);
 int64_t accept_blocks(const joker_accept_seg *segs, int n_segs, int64_t *blk_base_host);
 }  // namespace joker
 
@@ -516,37 +518,30 @@ extern "C" int joker_accept(const joker_accept_seg *segs, int n_segs, const doub
     return JOKER_OK;
 }
 
-extern "C" int joker_accept_refined(const joker_stars *s, const joker_cache *c,
-                                    const joker_accept_seg *segs, int n_segs, const double *d_lnl,
-                                    const float *d_err, const uint64_t *d_bound_key,
-                                    uint64_t *d_exact_key, int n_slots, int u_source,
-                                    const double *d_u, int64_t *d_out_idx, double *d_out_lnl,
-                                    int64_t *d_count, uint64_t *d_n_refined, void *d_work,
-                                    int64_t work_bytes, void *stream) {
-    if (n_segs <= 0) return JOKER_OK;
-    if (!s || !c) return fail(JOKER_EINVAL, "joker_accept_refined: NULL handle");
-    if (!segs || !d_lnl || !d_err || !d_bound_key || !d_exact_key || !d_out_idx || !d_count ||
-        !d_work)
-        return fail(JOKER_EINVAL, "joker_accept_refined: NULL argument");
-    if (u_source != JOKER_U_ARRAY && u_source != JOKER_U_PCG64)
-        return fail(JOKER_EINVAL, "joker_accept_refined: unknown u_source %d", u_source);
-    if (u_source == JOKER_U_ARRAY && !d_u)
-        return fail(JOKER_EINVAL, "joker_accept_refined: d_u is NULL");
+// Shared set-up of the refined acceptance entry points: validation, the
+// segment table copied into the workspace, and the arguments.
+static int refined_setup(const joker_stars *s, const joker_cache *c, const joker_accept_seg *segs,
+                         int n_segs, const double *d_lnl, const float *d_err,
+                         const uint64_t *d_bound_key, uint64_t *d_exact_key, int n_slots,
+                         uint64_t *d_n_refined, void *d_work, int64_t work_bytes,
+                         cudaStream_t st, AcceptArgs &a, int64_t &nb, const char *who) {
+    if (!s || !c) return fail(JOKER_EINVAL, "%s: NULL handle", who);
+    if (!segs || !d_lnl || !d_err || !d_bound_key || !d_exact_key || !d_work)
+        return fail(JOKER_EINVAL, "%s: NULL argument", who);
     for (int i = 0; i < n_segs; ++i) {
         const joker_accept_seg &g = segs[i];
         if (g.n < 0 || g.max_out < 0 || g.lnl_off < 0 || g.max_slot < 0 || g.max_slot >= n_slots)
-            return fail(JOKER_EINVAL, "joker_accept_refined: segment %d has a bad field", i);
+            return fail(JOKER_EINVAL, "%s: segment %d has a bad field", who, i);
         if (g.star < 0 || g.star >= s->n_stars || g.row0 < 0 || g.row0 + g.n > c->cap)
-            return fail(JOKER_EINVAL, "joker_accept_refined: segment %d outside the stars or cache",
-                        i);
+            return fail(JOKER_EINVAL, "%s: segment %d outside the stars or cache", who, i);
     }
     const int64_t need = joker_accept_workspace(segs, n_segs);
     if (work_bytes < need)
-        return fail(JOKER_EINVAL, "joker_accept_refined: workspace %lld < %lld bytes",
-                    (long long)work_bytes, (long long)need);
+        return fail(JOKER_EINVAL, "%s: workspace %lld < %lld bytes", who, (long long)work_bytes,
+                    (long long)need);
     std::vector<int64_t> base(n_segs + 1);
-    const int64_t nb = accept_blocks(segs, n_segs, base.data());
-    if (nb > 0x7fffffffLL) return fail(JOKER_ERANGE, "joker_accept_refined: too many samples");
+    nb = accept_blocks(segs, n_segs, base.data());
+    if (nb > 0x7fffffffLL) return fail(JOKER_ERANGE, "%s: too many samples", who);
     char *w = (char *)d_work;
     joker_accept_seg *d_segs = (joker_accept_seg *)w;
     w += align256(sizeof(joker_accept_seg) * (int64_t)n_segs);
@@ -557,11 +552,8 @@ extern "C" int joker_accept_refined(const joker_stars *s, const joker_cache *c,
     uint32_t *d_words = (uint32_t *)w;
     w += align256(4 * 256 * nb);
     uint32_t *d_amb = (uint32_t *)w;
-    cudaStream_t st = (cudaStream_t)stream;
     CUDA_TRY(cudaMemcpyAsync(d_segs, segs, sizeof(joker_accept_seg) * n_segs, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_base, base.data(), 8 * (n_segs + 1), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemsetAsync(d_exact_key, 0, sizeof(uint64_t) * n_slots, st));
-    AcceptArgs a;
     memset(&a, 0, sizeof a);
     a.err = d_err;
     a.bound_key = (const unsigned long long *)d_bound_key;
@@ -578,13 +570,57 @@ extern "C" int joker_accept_refined(const joker_stars *s, const joker_cache *c,
     a.n_segs = n_segs;
     a.lnl = d_lnl;
     a.max_key = (const unsigned long long *)d_exact_key;
-    a.u_source = u_source;
-    a.u = d_u;
     a.words = d_words;
     a.blk_count = d_blk;
+    return JOKER_OK;
+}
+
+extern "C" int joker_refine_max(const joker_stars *s, const joker_cache *c,
+                                const joker_accept_seg *segs, int n_segs, const double *d_lnl,
+                                const float *d_err, const uint64_t *d_bound_key,
+                                uint64_t *d_exact_key, uint64_t *d_n_refined, void *d_work,
+                                int64_t work_bytes, void *stream) {
+    if (n_segs <= 0) return JOKER_OK;
+    int n_slots = 0;
+    if (segs)
+        for (int i = 0; i < n_segs; ++i) n_slots = std::max(n_slots, segs[i].max_slot + 1);
+    AcceptArgs a;
+    int64_t nb = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int rc = refined_setup(s, c, segs, n_segs, d_lnl, d_err, d_bound_key, d_exact_key,
+                                 n_slots, d_n_refined, d_work, work_bytes, st, a, nb,
+                                 "joker_refine_max");
+    if (rc != JOKER_OK) return rc;
+    CUDA_TRY(launch_refine_max(a, nb, st));
+    return JOKER_OK;
+}
+
+extern "C" int joker_accept_refined(const joker_stars *s, const joker_cache *c,
+                                    const joker_accept_seg *segs, int n_segs, const double *d_lnl,
+                                    const float *d_err, const uint64_t *d_bound_key,
+                                    uint64_t *d_exact_key, int n_slots, int max_given,
+                                    int u_source, const double *d_u, int64_t *d_out_idx,
+                                    double *d_out_lnl, int64_t *d_count, uint64_t *d_n_refined,
+                                    void *d_work, int64_t work_bytes, void *stream) {
+    if (n_segs <= 0) return JOKER_OK;
+    if (!d_out_idx || !d_count) return fail(JOKER_EINVAL, "joker_accept_refined: NULL output");
+    if (u_source != JOKER_U_ARRAY && u_source != JOKER_U_PCG64)
+        return fail(JOKER_EINVAL, "joker_accept_refined: unknown u_source %d", u_source);
+    if (u_source == JOKER_U_ARRAY && !d_u)
+        return fail(JOKER_EINVAL, "joker_accept_refined: d_u is NULL");
+    AcceptArgs a;
+    int64_t nb = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int rc = refined_setup(s, c, segs, n_segs, d_lnl, d_err, d_bound_key, d_exact_key,
+                                 n_slots, d_n_refined, d_work, work_bytes, st, a, nb,
+                                 "joker_accept_refined");
+    if (rc != JOKER_OK) return rc;
+    if (!max_given) CUDA_TRY(cudaMemsetAsync(d_exact_key, 0, sizeof(uint64_t) * n_slots, st));
+    a.u_source = u_source;
+    a.u = d_u;
     a.out_idx = d_out_idx;
     a.out_lnl = d_out_lnl;
     a.count = d_count;
-    CUDA_TRY(launch_accept(a, nb, st));
+    CUDA_TRY(launch_accept(a, nb, st, max_given != 0));
     return JOKER_OK;
 }

@@ -71,26 +71,91 @@ __device__ __forceinline__ int interval_test(double lnl, float err, double mx, d
     return -1;
 }
 
-// FP64 maximum of each segment: re-evaluate the samples whose upper bound
-// reaches the largest lower bound (the true maximum lies among them).
-__global__ void __launch_bounds__(ACC_THREADS) accept_maxrefine_kernel(AcceptArgs a) {
+// Candidates for each segment's FP64 maximum: the samples whose upper bound
+// reaches the largest lower bound (the true maximum lies among them), plus
+// samples without a usable bound.  Lean scan; marks bits in amb_words.
+__global__ void __launch_bounds__(ACC_THREADS) accept_candidates_kernel(AcceptArgs a) {
     const int64_t gblk = blockIdx.x;
     const int si = find_seg(a.blk_base, a.n_segs, gblk);
     const joker_accept_seg sg = a.segs[si];
     const int64_t blk = gblk - a.blk_base[si];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t wbase = blk * ACC_BLOCK + (int64_t)warp * 1024;
     const double lb = key_to_double(a.bound_key[2 * sg.max_slot + 1]);
-    const int64_t first = blk * ACC_BLOCK;
-    for (int k = threadIdx.x; k < ACC_BLOCK; k += ACC_THREADS) {
-        const int64_t i = first + k;
-        if (i >= sg.n) break;
-        const double v = a.lnl[sg.lnl_off + i];
-        const float er = a.err[sg.lnl_off + i];
-        if (!(v + (double)er >= lb) && er < 1e29f && v == v) continue;
-        const int64_t r = sg.row0 + i;
-        const double x = fp64_lnl_sample(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
-                                         a.OM[r], a.M0[r], a.S[r]);
-        atomicMax(a.exact_key + sg.max_slot, double_to_key(x));
-        if (a.n_refined) atomicAdd(a.n_refined, 1ull);
+    uint32_t my_word = 0;
+    for (int k = 0; k < 32; ++k) {
+        const int64_t i = wbase + (int64_t)k * 32 + lane;
+        bool cand = false;
+        if (i < sg.n) {
+            const double v = a.lnl[sg.lnl_off + i];
+            const float er = a.err[sg.lnl_off + i];
+            cand = (v + (double)er >= lb) || !(er < 1e29f) || !(v == v);
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, cand);
+        if (lane == k) my_word = bal;
+    }
+    a.amb_words[gblk * ACC_THREADS + threadIdx.x] = my_word;
+}
+
+// FP64 work on the samples flagged in amb_words.  One thread covers
+// WORDS_PER_THREAD consecutive words (all inside one 256-word CTA block);
+// almost all words are zero.  MODE 0 raises the FP64 maximum; MODE 1 decides
+// the undecided samples against it and their own uniforms.
+constexpr int WORDS_PER_THREAD = 16;
+
+template <int MODE>
+__global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, int64_t n_words) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t w0 = t * WORDS_PER_THREAD;
+    if (w0 >= n_words) return;
+    uint32_t wv[WORDS_PER_THREAD];
+    const uint4 *p = reinterpret_cast<const uint4 *>(a.amb_words + w0);
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < WORDS_PER_THREAD / 4; ++q) {
+        const uint4 v = p[q];
+        wv[4 * q] = v.x; wv[4 * q + 1] = v.y; wv[4 * q + 2] = v.z; wv[4 * q + 3] = v.w;
+        any |= (v.x | v.y | v.z | v.w) != 0u;
+    }
+    if (!any) return;
+    const int64_t gblk = w0 / ACC_THREADS;
+    const int si = find_seg(a.blk_base, a.n_segs, gblk);
+    const joker_accept_seg sg = a.segs[si];
+    const int64_t blk = gblk - a.blk_base[si];
+    const double mx = MODE == 1 ? key_to_double(a.exact_key[sg.max_slot]) : 0.0;
+    for (int q = 0; q < WORDS_PER_THREAD; ++q) {
+        uint32_t bits = wv[q];
+        if (!bits) continue;
+        const int64_t wi = w0 + q;                                 // global word
+        const int64_t first = blk * ACC_BLOCK + (wi - gblk * ACC_THREADS) * 32;
+        uint32_t add = 0;
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            const int64_t i = first + b;
+            if (i >= sg.n) continue;
+            const int64_t r = sg.row0 + i;
+            const double v = fp64_lnl_sample(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
+                                             a.OM[r], a.M0[r], a.S[r]);
+            if (a.n_refined) atomicAdd(a.n_refined, 1ull);
+            if (MODE == 0) {
+                atomicMax(a.exact_key + sg.max_slot, double_to_key(v));
+            } else {
+                double u;
+                if (a.u_source == JOKER_U_PCG64) {
+                    const u128 s0 = ((u128)sg.pcg_state_hi << 64) | (u128)sg.pcg_state_lo;
+                    const u128 inc = ((u128)sg.pcg_inc_hi << 64) | (u128)sg.pcg_inc_lo;
+                    u = pcg_uniform(pcg_output(pcg_advance(s0, inc, (uint64_t)i + 1)));
+                } else {
+                    u = a.u[sg.u_off + i];
+                }
+                if (accept_test(v - mx, u)) add |= 1u << b;
+            }
+        }
+        if (MODE == 1 && add) {
+            atomicOr(a.words + wi, add);
+            atomicAdd((unsigned long long *)(a.blk_count + gblk), (unsigned long long)__popc(add));
+        }
     }
 }
 
@@ -155,43 +220,6 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
         int64_t c = 0;
         for (int w = 0; w < ACC_THREADS / 32; ++w) c += s_cnt[w];
         a.blk_count[gblk] = c;
-    }
-}
-
-// Samples the interval test left open: their FP64 value against the FP64
-// maximum and their own uniform.  Runs between mark and scan; one thread per
-// 32-sample word, almost all of which have nothing to do.
-__global__ void __launch_bounds__(ACC_THREADS) accept_decide_kernel(AcceptArgs a) {
-    const int64_t gblk = blockIdx.x;
-    uint32_t amb = a.amb_words[gblk * ACC_THREADS + threadIdx.x];
-    if (amb == 0) return;
-    const int si = find_seg(a.blk_base, a.n_segs, gblk);
-    const joker_accept_seg sg = a.segs[si];
-    const int64_t blk = gblk - a.blk_base[si];
-    const double mx = key_to_double(a.exact_key[sg.max_slot]);
-    const int64_t first = blk * ACC_BLOCK + (int64_t)threadIdx.x * 32;
-    uint32_t add = 0;
-    while (amb) {
-        const int b = __ffs(amb) - 1;
-        amb &= amb - 1;
-        const int64_t i = first + b;
-        double u;
-        if (a.u_source == JOKER_U_PCG64) {
-            const u128 s0 = ((u128)sg.pcg_state_hi << 64) | (u128)sg.pcg_state_lo;
-            const u128 inc = ((u128)sg.pcg_inc_hi << 64) | (u128)sg.pcg_inc_lo;
-            u = pcg_uniform(pcg_output(pcg_advance(s0, inc, (uint64_t)i + 1)));
-        } else {
-            u = a.u[sg.u_off + i];
-        }
-        const int64_t r = sg.row0 + i;
-        const double v = fp64_lnl_sample(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
-                                         a.OM[r], a.M0[r], a.S[r]);
-        if (a.n_refined) atomicAdd(a.n_refined, 1ull);
-        if (accept_test(v - mx, u)) add |= 1u << b;
-    }
-    if (add) {
-        atomicOr(a.words + gblk * ACC_THREADS + threadIdx.x, add);
-        atomicAdd((unsigned long long *)(a.blk_count + gblk), (unsigned long long)__popc(add));
     }
 }
 
@@ -262,10 +290,28 @@ int64_t accept_blocks(const joker_accept_seg *segs, int n_segs, int64_t *blk_bas
     return tot;
 }
 
-cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st) {
-    if (a.err != nullptr && total_blocks > 0) {
-        accept_maxrefine_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
-        cudaError_t e = cudaGetLastError();
+static cudaError_t launch_fp64_words(int mode, const AcceptArgs &a, int64_t total_blocks,
+                                     cudaStream_t st) {
+    const int64_t n_words = total_blocks * ACC_THREADS;
+    const int64_t threads = (n_words + WORDS_PER_THREAD - 1) / WORDS_PER_THREAD;
+    const unsigned grid = (unsigned)((threads + 127) / 128);
+    if (mode == 0) accept_fp64_words_kernel<0><<<grid, 128, 0, st>>>(a, n_words);
+    else accept_fp64_words_kernel<1><<<grid, 128, 0, st>>>(a, n_words);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine_max(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st) {
+    if (total_blocks <= 0) return cudaSuccess;
+    accept_candidates_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_fp64_words(0, a, total_blocks, st);
+}
+
+cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st,
+                          bool max_given) {
+    if (a.err != nullptr && !max_given && total_blocks > 0) {
+        cudaError_t e = launch_refine_max(a, total_blocks, st);
         if (e != cudaSuccess) return e;
     }
     if (total_blocks > 0) {
@@ -273,8 +319,7 @@ cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         if (a.err != nullptr) {
-            accept_decide_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
-            e = cudaGetLastError();
+            e = launch_fp64_words(1, a, total_blocks, st);
             if (e != cudaSuccess) return e;
         }
     }

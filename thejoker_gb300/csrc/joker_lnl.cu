@@ -455,6 +455,7 @@ __global__ void prepare_cache_kernel(const double *__restrict__ chunk, int64_t n
         const double m0 = chunk[i * 5 + 3], s = chunk[i * 5 + 4];
         const int64_t r = row0 + i;
         P[r] = p; E[r] = e; OM[r] = om; M0[r] = m0; S[r] = s;
+        // 1/P and M0/(2 pi) need their low words: FP64 (one division)
         const double ip = 1.0 / p;
         const float ip_hi = (float)ip;
         const float ip_lo = (float)(ip - (double)ip_hi);
@@ -462,13 +463,18 @@ __global__ void prepare_cache_kernel(const double *__restrict__ chunk, int64_t n
         mc -= floor(mc);                       // [0, 1)
         const float mc_hi = (float)mc;
         const float mc_lo = (float)(mc - (double)mc_hi);
-        double sw, cw;
-        sincos(om, &sw, &cw);
+        // cos w, sin w and log g are stored as floats: FP32 is enough, with
+        // the angle reduced to half-turns in FP64 first (sincospif is exact
+        // in its argument reduction)
+        double wc = om * 0.31830988618379067154;    // omega / pi
+        wc -= 2.0 * floor(0.5 * wc);                // [0, 2)
+        float sw, cw;
+        sincospif((float)wc, &sw, &cw);
         // log g, g = P^(-2/3) / (1 - e^2): the per-sample factor of the
         // FixedCompanionMass variance sigma_K0^2 P0^(2/3) g
-        const double lg = -2.0 / 3.0 * log(p) - log((1.0 - e) * (1.0 + e));
+        const float lg = -0.6666667f * logf((float)p) - log1pf(-(float)(e * e));
         mx_a[r] = make_float4(ip_hi, ip_lo, mc_hi, mc_lo);
-        mx_b[r] = make_float4((float)e, (float)cw, (float)sw, (float)lg);
+        mx_b[r] = make_float4((float)e, cw, sw, lg);
         mx_s2[r] = (float)(s * s);
     }
 }

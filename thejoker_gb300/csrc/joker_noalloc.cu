@@ -36,7 +36,8 @@
 #include "joker_internal.cuh"
 
 namespace joker {
-cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st);
+cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st,
+                          bool max_given = false);
 int64_t accept_blocks(const joker_accept_seg *segs, int n_segs, int64_t *blk_base_host);
 void set_last_error(const char *msg);
 }  // namespace joker

@@ -153,23 +153,26 @@ class MaxKeys:
 
 
 def lnl(stars, cache, out, precision="fp64", star0=0, n_sel=None, row0=0, count=None,
-        max_keys=None, err=None, bound_keys=None, chunk=0, stream=None):
+        max_keys=None, err=None, bound_keys=None, chunk=0, out_offset=0, stream=None):
     """ln L of stars [star0, star0 + n_sel) over cache rows [row0, row0 + count)
     into ``out`` (a float64 CUDA tensor of shape (n_sel, ld)).  Mixed
     precisions can also write a per-sample error bound into ``err`` (float32,
     same shape) and the per-star maxima of lnL +- err into ``bound_keys``
-    (a MaxKeys of 2 n_sel entries)."""
+    (a MaxKeys of 2 n_sel entries).  Star k's value for row row0 + j goes to
+    out[k, out_offset + j]."""
     n_sel = stars.n_stars - star0 if n_sel is None else n_sel
     count = cache.size - row0 if count is None else count
-    if out.dtype != torch.float64 or out.dim() != 2 or out.shape[0] < n_sel or out.shape[1] < count:
-        raise ValueError("out must be float64 with shape (n_sel, >= count)")
-    if not out.is_contiguous():
-        raise ValueError("out must be contiguous")
+    if out.dtype != torch.float64 or out.dim() != 2 or out.shape[0] < n_sel or \
+            out.shape[1] < out_offset + count:
+        raise ValueError("out must be float64 with shape (n_sel, >= out_offset + count)")
+    if not out.is_contiguous() or (err is not None and (not err.is_contiguous() or
+                                                         err.shape != out.shape)):
+        raise ValueError("out (and err) must be contiguous, err shaped like out")
     nat.check(nat.lib().joker_lnl(
         stars.handle, cache.handle, int(star0), int(n_sel), int(row0), int(count),
-        PRECISIONS[precision], ctypes.c_void_p(out.data_ptr()), out.shape[1],
+        PRECISIONS[precision], ctypes.c_void_p(out.data_ptr() + 8 * int(out_offset)), out.shape[1],
         max_keys.ptr() if max_keys is not None else None,
-        ctypes.c_void_p(err.data_ptr()) if err is not None else None,
+        ctypes.c_void_p(err.data_ptr() + 4 * int(out_offset)) if err is not None else None,
         bound_keys.ptr() if bound_keys is not None else None, 0, int(chunk),
         stream_handle(stream)), "joker_lnl")
     return out
@@ -233,12 +236,35 @@ def _segments(segments, u_source):
     return arr, total_out
 
 
+def refine_max(stars, cache, lnl_buf, err, bound_keys, segments, exact=None, stream=None):
+    """FP64 maxima of the segments (joker_refine_max) into ``exact`` (a
+    MaxKeys with one slot per max_slot, zeroed here when not given)."""
+    ns = len(segments)
+    arr, _ = _segments(segments, "array")
+    n_slots = max(int(sg.get("max_slot", 0)) for sg in segments) + 1
+    if exact is None:
+        exact = MaxKeys(n_slots)
+    n_ref = torch.zeros(1, dtype=torch.int64, device=lnl_buf.device)
+    wbytes = nat.lib().joker_accept_workspace(arr, ns)
+    work = torch.empty(max(int(wbytes), 1), dtype=torch.uint8, device=lnl_buf.device)
+    nat.check(nat.lib().joker_refine_max(
+        stars.handle, cache.handle, arr, ns, ctypes.c_void_p(lnl_buf.data_ptr()),
+        ctypes.c_void_p(err.data_ptr()), bound_keys.ptr(), exact.ptr(),
+        ctypes.c_void_p(n_ref.data_ptr()), ctypes.c_void_p(work.data_ptr()), int(wbytes),
+        stream_handle(stream)), "joker_refine_max")
+    if stream is not None:
+        work.record_stream(stream)
+    return exact, n_ref
+
+
 def accept_refined(stars, cache, lnl_buf, err, bound_keys, segments, u_source="pcg64", u=None,
-                   out_idx=None, out_lnl=None, counts=None, stream=None):
+                   out_idx=None, out_lnl=None, counts=None, exact=None, stream=None):
     """Acceptance over mixed-precision ln L with its error bounds, exact with
     respect to FP64 (joker_accept_refined).  Each segment also names its
     ``star`` and the cache ``row0`` of its first sample.  Returns (out_idx,
-    out_lnl, counts, exact_max_keys, n_refined)."""
+    out_lnl, counts, exact_max_keys, n_refined).  ``exact``: FP64 maxima already
+    found (joker_refine_max, possibly combined over ranks); computed here when
+    None."""
     ns = len(segments)
     arr, total_out = _segments(segments, u_source)
     n_slots = max(int(sg.get("max_slot", 0)) for sg in segments) + 1
@@ -247,14 +273,17 @@ def accept_refined(stars, cache, lnl_buf, err, bound_keys, segments, u_source="p
         out_idx = torch.empty(max(total_out, 1), dtype=torch.int64, device=dev)
     if counts is None:
         counts = torch.empty(ns, dtype=torch.int64, device=dev)
-    exact = MaxKeys(n_slots)
+    max_given = exact is not None
+    if exact is None:
+        exact = MaxKeys(n_slots)
     n_ref = torch.zeros(1, dtype=torch.int64, device=dev)
     wbytes = nat.lib().joker_accept_workspace(arr, ns)
     work = torch.empty(max(int(wbytes), 1), dtype=torch.uint8, device=dev)
     usrc = nat.JOKER_U_PCG64 if u_source == "pcg64" else nat.JOKER_U_ARRAY
     nat.check(nat.lib().joker_accept_refined(
         stars.handle, cache.handle, arr, ns, ctypes.c_void_p(lnl_buf.data_ptr()),
-        ctypes.c_void_p(err.data_ptr()), bound_keys.ptr(), exact.ptr(), n_slots, usrc,
+        ctypes.c_void_p(err.data_ptr()), bound_keys.ptr(), exact.ptr(), n_slots,
+        int(max_given), usrc,
         ctypes.c_void_p(u.data_ptr()) if u is not None else None,
         ctypes.c_void_p(out_idx.data_ptr()),
         ctypes.c_void_p(out_lnl.data_ptr()) if out_lnl is not None else None,
