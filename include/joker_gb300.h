@@ -199,6 +199,35 @@ int joker_refine_max(const joker_stars *stars, const joker_cache *cache,
                      const float *d_err, const uint64_t *d_bound_key, uint64_t *d_exact_key,
                      uint64_t *d_n_refined, void *d_work, int64_t work_bytes, void *stream);
 
+/* ---- iterative rejection, one device-resident round at a time --------------
+ * Replaces the loop of iterative_rejection_inmem
+ * (thejoker/likelihood_helpers.py:130-229) for every star of a joker_stars
+ * table at once, over library rows [lib_row0, lib_row0 + lib_size) of the
+ * cache.  Per star: init_batch samples first (growth_factor * n_requested in
+ * the reference), then n_process = int(safety_factor * n_need / n_good *
+ * n_evals) clamped to the library; every round draws fresh uniforms for the
+ * whole prefix from the star's numpy PCG64 stream (pcg_states: n_stars x 4
+ * uint64 -- state hi, lo, increment hi, lo -- positioned at its next draw);
+ * a star stops when n_good >= n_requested, when the library is exhausted, on
+ * zero accepted samples, or after maxiter rounds.  precision: JOKER_FP64, or
+ * JOKER_MIXED / JOKER_MIXED_ACCURATE with the acceptance refined to the FP64
+ * decisions.  joker_iter_round launches one round without host copies,
+ * allocation or synchronisation, so a round can be captured in a CUDA graph
+ * and replayed until the finished-star count (joker_iter_outputs) reaches
+ * n_stars.  A handle allocates its buffers once, at creation. */
+typedef struct joker_iter joker_iter;
+int joker_iter_create(joker_iter **out, const joker_stars *stars, const joker_cache *cache,
+                      int precision, int64_t lib_row0, int64_t lib_size, int n_requested,
+                      int64_t init_batch, double safety_factor, int maxiter,
+                      const uint64_t *pcg_states, int chunk);
+int joker_iter_destroy(joker_iter *it);
+int joker_iter_round(joker_iter *it, void *stream);
+int joker_iter_outputs(const joker_iter *it, int64_t **d_state, int64_t **d_idx,
+                       double **d_lnl, int **d_done, uint64_t **d_n_refined);
+/* Synchronous copy of the same outputs to host arrays (any may be NULL). */
+int joker_iter_read(const joker_iter *it, int64_t *h_state, int64_t *h_idx, double *h_lnl,
+                    int *h_done, uint64_t *h_n_refined);
+
 /* ---- acceptance without allocation ---------------------------------------
  * No counterpart in the reference.  joker_accept_noalloc is joker_accept for
  * callers that must not allocate device memory: a serving loop with

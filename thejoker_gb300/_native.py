@@ -25,7 +25,8 @@ EXPORTED = (
     "joker_stars_info", "joker_cache_create", "joker_cache_destroy", "joker_cache_load",
     "joker_cache_capacity", "joker_batch_marginal_ln_likelihood", "joker_lnl",
     "joker_key_to_double", "joker_accept_workspace", "joker_accept", "joker_accept_refined",
-    "joker_refine_max",
+    "joker_refine_max", "joker_iter_create", "joker_iter_destroy", "joker_iter_round",
+    "joker_iter_outputs", "joker_iter_read",
     "joker_accept_noalloc",
 )
 
@@ -76,6 +77,15 @@ _SIGS = {
                                             _vp]),
     "joker_refine_max": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp,
                                         _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
+    "joker_iter_create": (ctypes.c_int, [ctypes.POINTER(_vp), _vp, _vp, ctypes.c_int, _i64, _i64,
+                                         ctypes.c_int, _i64, ctypes.c_double, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]),
+    "joker_iter_destroy": (ctypes.c_int, [_vp]),
+    "joker_iter_round": (ctypes.c_int, [_vp, _vp]),
+    "joker_iter_outputs": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                                          ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                                          ctypes.POINTER(_vp)]),
+    "joker_iter_read": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "joker_accept_noalloc": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                             ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

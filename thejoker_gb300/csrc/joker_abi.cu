@@ -393,6 +393,31 @@ extern "C" int joker_batch_marginal_ln_likelihood(const joker_stars *s, int star
     return run_lnl(s, JOKER_FP64, a, 128, (cudaStream_t)stream);
 }
 
+static float err_c0();
+
+namespace joker {
+float mixed_err_c0() { return err_c0(); }
+
+void stars_internals(const joker_stars *s, const StarRec **recs, const double **ep64,
+                     const float **ep32, int *n_stars, int *L, int *jit, int **queue) {
+    *recs = s->d_stars;
+    *ep64 = s->d_ep64;
+    *ep32 = s->d_ep32;
+    *n_stars = s->n_stars;
+    *L = s->L;
+    *jit = s->jitter == JOKER_JITTER_APPLIED;
+    *queue = s->d_queue;
+}
+
+void cache_internals(const joker_cache *c, int64_t *cap, const double **P, const double **E,
+                     const double **OM, const double **M0, const double **S,
+                     const float4 **mx_a, const float4 **mx_b, const float **mx_s2) {
+    *cap = c->cap;
+    *P = c->P; *E = c->E; *OM = c->OM; *M0 = c->M0; *S = c->S;
+    *mx_a = c->mx_a; *mx_b = c->mx_b; *mx_s2 = c->mx_s2;
+}
+}  // namespace joker
+
 static float err_c0() {
     // column-error constant of the mixed kernel's bound (see joker_lnl.cu);
     // JOKER_ERR_C0 in the environment overrides it for calibration runs

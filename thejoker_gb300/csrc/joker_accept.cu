@@ -29,13 +29,25 @@ constexpr int ACC_THREADS = 256;                       // 8 warps
 constexpr int64_t ACC_BLOCK = ACC_THREADS * 32;        // samples per CTA
 
 
-__device__ __forceinline__ int find_seg(const int64_t *blk_base, int n_segs, int64_t b) {
-    int lo = 0, hi = n_segs - 1;
+__device__ __forceinline__ int find_seg(const AcceptArgs &a, int64_t b) {
+    if (a.fixed_blocks > 0) return (int)(b / a.fixed_blocks);
+    const int64_t *blk_base = a.blk_base;
+    int lo = 0, hi = a.n_segs - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (blk_base[mid] <= b) lo = mid; else hi = mid - 1;
     }
     return lo;
+}
+
+// Number of 8192-sample blocks of this pass: the grid, or a device-side count
+// when the pass runs inside a captured graph with a fixed grid.
+__device__ __forceinline__ int64_t n_blocks(const AcceptArgs &a) {
+    return a.total_blocks_dev ? *((volatile const int64_t *)a.total_blocks_dev) : (int64_t)gridDim.x;
+}
+
+__device__ __forceinline__ int64_t seg_base(const AcceptArgs &a, int si) {
+    return a.fixed_blocks > 0 ? (int64_t)si * a.fixed_blocks : a.blk_base[si];
 }
 
 // exp(d) > u, evaluated as numpy does in FP64 but with an FP32 pre-test that
@@ -75,10 +87,11 @@ __device__ __forceinline__ int interval_test(double lnl, float err, double mx, d
 // reaches the largest lower bound (the true maximum lies among them), plus
 // samples without a usable bound.  Lean scan; marks bits in amb_words.
 __global__ void __launch_bounds__(ACC_THREADS) accept_candidates_kernel(AcceptArgs a) {
-    const int64_t gblk = blockIdx.x;
-    const int si = find_seg(a.blk_base, a.n_segs, gblk);
+    const int64_t nbk = n_blocks(a);
+    for (int64_t gblk = blockIdx.x; gblk < nbk; gblk += gridDim.x) {
+    const int si = find_seg(a, gblk);
     const joker_accept_seg sg = a.segs[si];
-    const int64_t blk = gblk - a.blk_base[si];
+    const int64_t blk = gblk - seg_base(a, si);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t wbase = blk * ACC_BLOCK + (int64_t)warp * 1024;
     const double lb = key_to_double(a.bound_key[2 * sg.max_slot + 1]);
@@ -95,6 +108,7 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_candidates_kernel(AcceptAr
         if (lane == k) my_word = bal;
     }
     a.amb_words[gblk * ACC_THREADS + threadIdx.x] = my_word;
+    }
 }
 
 // FP64 work on the samples flagged in amb_words.  One thread covers
@@ -105,9 +119,10 @@ constexpr int WORDS_PER_THREAD = 16;
 
 template <int MODE>
 __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, int64_t n_words) {
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a.total_blocks_dev) n_words = n_blocks(a) * ACC_THREADS;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+         t * WORDS_PER_THREAD < n_words; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t w0 = t * WORDS_PER_THREAD;
-    if (w0 >= n_words) return;
     uint32_t wv[WORDS_PER_THREAD];
     const uint4 *p = reinterpret_cast<const uint4 *>(a.amb_words + w0);
     bool any = false;
@@ -117,11 +132,11 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
         wv[4 * q] = v.x; wv[4 * q + 1] = v.y; wv[4 * q + 2] = v.z; wv[4 * q + 3] = v.w;
         any |= (v.x | v.y | v.z | v.w) != 0u;
     }
-    if (!any) return;
+    if (!any) continue;
     const int64_t gblk = w0 / ACC_THREADS;
-    const int si = find_seg(a.blk_base, a.n_segs, gblk);
+    const int si = find_seg(a, gblk);
     const joker_accept_seg sg = a.segs[si];
-    const int64_t blk = gblk - a.blk_base[si];
+    const int64_t blk = gblk - seg_base(a, si);
     const double mx = MODE == 1 ? key_to_double(a.exact_key[sg.max_slot]) : 0.0;
     for (int q = 0; q < WORDS_PER_THREAD; ++q) {
         uint32_t bits = wv[q];
@@ -157,13 +172,16 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
             atomicAdd((unsigned long long *)(a.blk_count + gblk), (unsigned long long)__popc(add));
         }
     }
+    }
 }
 
 __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) {
-    const int64_t gblk = blockIdx.x;
-    const int si = find_seg(a.blk_base, a.n_segs, gblk);
+    __shared__ int s_cnt[ACC_THREADS / 32];
+    const int64_t nbk = n_blocks(a);
+    for (int64_t gblk = blockIdx.x; gblk < nbk; gblk += gridDim.x) {
+    const int si = find_seg(a, gblk);
     const joker_accept_seg sg = a.segs[si];
-    const int64_t blk = gblk - a.blk_base[si];
+    const int64_t blk = gblk - seg_base(a, si);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t wbase = blk * ACC_BLOCK + (int64_t)warp * 1024;  // first sample of this warp
     const bool refine = a.err != nullptr;
@@ -213,7 +231,6 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
     // word index within the CTA: warp * 32 + lane
     a.words[gblk * ACC_THREADS + threadIdx.x] = my_word;
     if (refine) a.amb_words[gblk * ACC_THREADS + threadIdx.x] = my_amb;
-    __shared__ int s_cnt[ACC_THREADS / 32];
     if (lane == 0) s_cnt[warp] = my_count;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -221,12 +238,14 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
         for (int w = 0; w < ACC_THREADS / 32; ++w) c += s_cnt[w];
         a.blk_count[gblk] = c;
     }
+    __syncthreads();
+    }
 }
 
 // One CTA per segment: exclusive scan of that segment's per-CTA counts.
 __global__ void __launch_bounds__(ACC_THREADS) accept_scan_kernel(AcceptArgs a) {
     const int si = blockIdx.x;
-    const int64_t b0 = a.blk_base[si], nb = a.blk_base[si + 1] - b0;
+    const int64_t b0 = seg_base(a, si), nb = seg_base(a, si + 1) - b0;
     __shared__ int64_t s_part[ACC_THREADS];
     int64_t carry = 0;
     for (int64_t base = 0; base < nb; base += ACC_THREADS) {
@@ -250,15 +269,16 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_scan_kernel(AcceptArgs a) 
 }
 
 __global__ void __launch_bounds__(ACC_THREADS) accept_emit_kernel(AcceptArgs a) {
-    const int64_t gblk = blockIdx.x;
-    const int si = find_seg(a.blk_base, a.n_segs, gblk);
+    __shared__ int s_scan[ACC_THREADS];
+    const int64_t nbk = n_blocks(a);
+    for (int64_t gblk = blockIdx.x; gblk < nbk; gblk += gridDim.x) {
+    const int si = find_seg(a, gblk);
     const joker_accept_seg sg = a.segs[si];
-    const int64_t blk = gblk - a.blk_base[si];
+    const int64_t blk = gblk - seg_base(a, si);
     const int64_t boff = a.blk_count[gblk];
-    if (boff >= sg.max_out) return;
+    if (boff >= sg.max_out) continue;
     const uint32_t word = a.words[gblk * ACC_THREADS + threadIdx.x];
     const int c = __popc(word);
-    __shared__ int s_scan[ACC_THREADS];
     s_scan[threadIdx.x] = c;
     __syncthreads();
     for (int off = 1; off < ACC_THREADS; off <<= 1) {
@@ -277,6 +297,8 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_emit_kernel(AcceptArgs a) 
         a.out_idx[sg.out_off + pos] = sg.idx_base + i;
         if (a.out_lnl) a.out_lnl[sg.out_off + pos] = a.lnl[sg.lnl_off + i];
         ++pos;
+    }
+    __syncthreads();
     }
 }
 

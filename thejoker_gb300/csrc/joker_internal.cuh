@@ -74,6 +74,7 @@ struct LnlArgs {
     // star-major, stars visited in `order` (relative indices) when given.
     const WorkItem *items;
     int n_items;
+    const int *n_items_dev;  // when set, the item count is read from device memory
     int star0, n_sel, chunk;
     int64_t row0, count, ld, ips;
     const int *order;
@@ -86,6 +87,10 @@ struct LnlArgs {
     unsigned long long *bound_key;   // [slot][2]
     float err_c0;                    // column-error constant of the bound
 };
+
+__device__ __forceinline__ int item_count(const LnlArgs &a) {
+    return a.n_items_dev ? *((volatile const int *)a.n_items_dev) : a.n_items;
+}
 
 __device__ __forceinline__ WorkItem get_item(const LnlArgs &a, int it) {
     if (a.items) return a.items[it];
@@ -117,6 +122,9 @@ struct AcceptArgs {
     uint32_t *amb_words;                    // undecided samples, one bit each (refinement)
     const joker_accept_seg *segs;
     const int64_t *blk_base;     // n_segs + 1 prefix of CTA counts
+    int64_t fixed_blocks;        // > 0: segment s owns CTA blocks [s * fixed, (s+1) * fixed)
+    const int64_t *total_blocks_dev;  // when set: block count in device memory, kernels
+                                      // loop over blocks (grid-stride), blk_base on device
     int n_segs;
     const double *lnl;
     const unsigned long long *max_key;

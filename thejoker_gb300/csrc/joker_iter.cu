@@ -1,0 +1,418 @@
+// Iterative rejection sampling for many stars, one device-resident round at a
+// time (the rounds can be captured in a CUDA graph and replayed).
+//
+// Per star this follows iterative_rejection_inmem
+// (thejoker/likelihood_helpers.py:130-229):
+//   n_process = growth_factor * n_requested (or init_batch_size)
+//   loop (at most maxiter rounds):
+//     ln L of the next n_process library samples, appended to the star's
+//     prefix; uu = rng.uniform(size=len(prefix)) -- fresh draws for the whole
+//     prefix every round; keep exp(lnL - max) > uu;
+//     stop when n_good >= n_requested; otherwise
+//     n_process = int(safety_factor * n_need / n_good * n_evals), clamped to
+//     the library, stop when it is <= 0.
+// A round is: plan (work items and acceptance segments from the per-star
+// state, the star's uniform stream advanced past the draws of earlier
+// rounds), the persistent ln L launch over the items, the acceptance pass
+// over every active star's prefix, and the update of the state.  Nothing in a
+// round allocates, copies from the host or synchronises.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include "joker_internal.cuh"
+#include "joker_math.cuh"
+
+namespace joker {
+cudaError_t launch_lnl(int precision, int L, bool jit, const LnlArgs &a, int block,
+                       cudaStream_t st);
+cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st,
+                          bool max_given);
+void set_last_error(const char *msg);
+float mixed_err_c0();
+}  // namespace joker
+
+using namespace joker;
+
+namespace {
+
+constexpr int ST_START = 0, ST_NPROC = 1, ST_NEVALS = 2, ST_NGOOD = 3, ST_DONE = 4,
+              ST_ROUNDS = 5, ST_UCONS = 6, ST_FIELDS = 8;
+constexpr int64_t BLOCK_SAMPLES = 8192;   // samples per acceptance CTA block
+
+struct IterParams {
+    int n_stars;
+    int64_t cap;            // library size (samples per star prefix at most)
+    int64_t lib_row0;       // cache row of library sample 0
+    int chunk;              // samples per ln L work item
+    int n_req;
+    double safety;
+    int maxiter;
+    int64_t *state;
+    const uint64_t *pcg0;   // per star: state_hi, state_lo, inc_hi, inc_lo
+    joker_accept_seg *segs;
+    int64_t *blk_base;      // n_stars + 1
+    int64_t *total_blocks;
+    WorkItem *items;
+    int *n_items;
+    unsigned long long *exact_key;
+    const int64_t *counts;
+    int *done_count;
+};
+
+// One CTA: work items and segments of the active stars, then the block prefix.
+__global__ void __launch_bounds__(1024) iter_plan_kernel(IterParams p, int zero_exact) {
+    __shared__ int64_t s_part[1024];
+    if (threadIdx.x == 0) *p.n_items = 0;
+    __syncthreads();
+    int64_t carry = 0;
+    for (int base = 0; base < p.n_stars; base += blockDim.x) {
+        const int s = base + threadIdx.x;
+        int64_t nblk = 0;
+        if (s < p.n_stars) {
+            int64_t *st = p.state + (int64_t)s * ST_FIELDS;
+            joker_accept_seg &g = p.segs[s];
+            if (zero_exact) p.exact_key[s] = 0ull;
+            if (st[ST_DONE] == 0) {
+                const int64_t start = st[ST_START], np = st[ST_NPROC];
+                const int64_t nch = (np + p.chunk - 1) / p.chunk;
+                const int pos = atomicAdd(p.n_items, (int)nch);
+                for (int64_t c = 0; c < nch; ++c) {
+                    WorkItem w;
+                    w.star = s;
+                    w.row0 = p.lib_row0 + start + c * p.chunk;
+                    const int64_t rem = np - c * p.chunk;
+                    w.count = (int)(rem < p.chunk ? rem : p.chunk);
+                    w.out_off = (int64_t)s * p.cap + start + c * p.chunk;
+                    w.max_slot = s;
+                    w.pad = 0;
+                    p.items[pos + c] = w;
+                }
+                const int64_t n_evals = start + np;
+                st[ST_NEVALS] = n_evals;
+                g.n = n_evals;
+                // the star's uniforms for this round follow those of the
+                // earlier rounds in its generator's stream
+                const u128 s0 = ((u128)p.pcg0[4 * s] << 64) | (u128)p.pcg0[4 * s + 1];
+                const u128 inc = ((u128)p.pcg0[4 * s + 2] << 64) | (u128)p.pcg0[4 * s + 3];
+                const u128 sr = pcg_advance(s0, inc, (uint64_t)st[ST_UCONS]);
+                g.pcg_state_hi = (uint64_t)(sr >> 64);
+                g.pcg_state_lo = (uint64_t)sr;
+                g.pcg_inc_hi = p.pcg0[4 * s + 2];
+                g.pcg_inc_lo = p.pcg0[4 * s + 3];
+                nblk = (n_evals + BLOCK_SAMPLES - 1) / BLOCK_SAMPLES;
+            } else {
+                g.n = 0;
+            }
+        }
+        s_part[threadIdx.x] = nblk;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int m = min((int)blockDim.x, p.n_stars - base);
+            for (int k = 0; k < m; ++k) {
+                p.blk_base[base + k] = carry;
+                carry += s_part[k];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        p.blk_base[p.n_stars] = carry;
+        *p.total_blocks = carry;
+    }
+}
+
+// One thread per star: the growth rule of likelihood_helpers.py:187-211.
+__global__ void iter_update_kernel(IterParams p) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= p.n_stars) return;
+    int64_t *st = p.state + (int64_t)s * ST_FIELDS;
+    if (st[ST_DONE] != 0) return;
+    const int64_t n_good = p.counts[s];
+    const int64_t n_evals = st[ST_NEVALS];
+    st[ST_NGOOD] = n_good;
+    st[ST_UCONS] += n_evals;                 // this round drew len(prefix) uniforms
+    st[ST_ROUNDS] += 1;
+    int64_t done = 0;
+    if (n_good == 0) {
+        done = 2;                            // "Failed to find any good samples!"
+    } else if (n_good >= p.n_req) {
+        done = 1;
+    } else {
+        const int64_t start = st[ST_START] + st[ST_NPROC];
+        const int64_t n_need = p.n_req - n_good;
+        double v = p.safety * (double)n_need / (double)n_good * (double)n_evals;
+        int64_t np = (int64_t)v;
+        if (start + np > p.cap) np = p.cap - start;
+        st[ST_START] = start;
+        st[ST_NPROC] = np;
+        if (np <= 0) done = 1;               // the library is exhausted: keep what passed
+        else if (st[ST_ROUNDS] >= p.maxiter) done = 3;
+    }
+    if (done) {
+        st[ST_DONE] = done;
+        atomicAdd(p.done_count, 1);
+    }
+}
+
+}  // namespace
+
+struct joker_iter {
+    const joker_stars *stars = nullptr;
+    const joker_cache *cache = nullptr;
+    int precision = 0;
+    int L = 0, jit = 0;
+    IterParams p{};
+    int64_t max_blocks = 0, items_cap = 0;
+    void *base = nullptr;                    // one allocation holds every buffer
+    double *lnl = nullptr;
+    float *err = nullptr;
+    unsigned long long *max_key = nullptr, *bound_key = nullptr;
+    uint32_t *words = nullptr, *amb = nullptr;
+    int64_t *blk_count = nullptr, *counts = nullptr, *out_idx = nullptr;
+    double *out_lnl = nullptr;
+    unsigned long long *n_refined = nullptr;
+    int *queue = nullptr;
+};
+
+// stars/cache accessors live in joker_abi.cu
+namespace joker {
+void stars_internals(const joker_stars *s, const StarRec **recs, const double **ep64,
+                     const float **ep32, int *n_stars, int *L, int *jit, int **queue);
+void cache_internals(const joker_cache *c, int64_t *cap, const double **P, const double **E,
+                     const double **OM, const double **M0, const double **S,
+                     const float4 **mx_a, const float4 **mx_b, const float **mx_s2);
+}  // namespace joker
+
+static int iter_fail(int code, const char *msg) {
+    set_last_error(msg);
+    return code;
+}
+
+static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+extern "C" int joker_iter_create(joker_iter **out, const joker_stars *stars,
+                                 const joker_cache *cache, int precision, int64_t lib_row0,
+                                 int64_t lib_size, int n_requested, int64_t init_batch,
+                                 double safety_factor, int maxiter, const uint64_t *pcg_states,
+                                 int chunk) {
+    if (!out || !stars || !cache || !pcg_states)
+        return iter_fail(JOKER_EINVAL, "joker_iter_create: NULL argument");
+    *out = nullptr;
+    const StarRec *recs; const double *ep64; const float *ep32; int n_stars, L, jit; int *queue;
+    stars_internals(stars, &recs, &ep64, &ep32, &n_stars, &L, &jit, &queue);
+    int64_t cap; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
+    cache_internals(cache, &cap, &P, &E, &OM, &M0, &S, &ma, &mb, &ms);
+    if (lib_row0 < 0 || lib_size <= 0 || lib_row0 + lib_size > cap)
+        return iter_fail(JOKER_ERANGE, "joker_iter_create: library rows outside the cache");
+    if (n_requested <= 0 || init_batch <= 0 || maxiter <= 0 || !(safety_factor > 0))
+        return iter_fail(JOKER_EINVAL, "joker_iter_create: bad schedule parameters");
+    if (init_batch > lib_size)
+        return iter_fail(JOKER_EINVAL, "Prior sample library not big enough! For iterative "
+                                       "sampling, you have to have at least growth_factor * "
+                                       "n_requested_samples samples in the library.");
+    if (precision != JOKER_FP64 && precision != JOKER_MIXED && precision != JOKER_MIXED_ACCURATE)
+        return iter_fail(JOKER_EINVAL, "joker_iter_create: precision must be FP64 or a mixed "
+                                       "precision with error bounds");
+    if (chunk <= 0) chunk = 1024;
+    joker_iter *it = new joker_iter();
+    it->stars = stars;
+    it->cache = cache;
+    it->precision = precision;
+    it->L = L;
+    it->jit = jit;
+    const int n = n_stars;
+    const int64_t bps = (lib_size + BLOCK_SAMPLES - 1) / BLOCK_SAMPLES;
+    it->max_blocks = bps * n;
+    it->items_cap = (int64_t)n * ((lib_size + chunk - 1) / chunk);
+    const bool mixed = precision != JOKER_FP64;
+    // layout of the single allocation
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += al(bytes); return o; };
+    const size_t o_state = take(8 * (size_t)n * ST_FIELDS), o_pcg = take(32 * (size_t)n),
+                 o_segs = take(sizeof(joker_accept_seg) * (size_t)n),
+                 o_base = take(8 * ((size_t)n + 1)), o_tot = take(8),
+                 o_items = take(sizeof(WorkItem) * (size_t)it->items_cap), o_nitems = take(4),
+                 o_exact = take(8 * (size_t)n), o_done = take(4), o_lnl = take(8 * (size_t)n * lib_size),
+                 o_err = mixed ? take(4 * (size_t)n * lib_size) : 0, o_mk = take(8 * (size_t)n),
+                 o_bk = take(16 * (size_t)n), o_words = take(4 * 256 * (size_t)it->max_blocks),
+                 o_amb = take(4 * 256 * (size_t)it->max_blocks),
+                 o_bc = take(8 * (size_t)it->max_blocks), o_cnt = take(8 * (size_t)n),
+                 o_oidx = take(8 * (size_t)n * n_requested), o_olnl = take(8 * (size_t)n * n_requested),
+                 o_nref = take(8), o_queue = take(16);
+    cudaError_t e = cudaMalloc(&it->base, off);
+    if (e != cudaSuccess) {
+        delete it;
+        char buf[200];
+        snprintf(buf, sizeof buf, "joker_iter_create: cudaMalloc(%zu): %s", off, cudaGetErrorString(e));
+        return iter_fail(JOKER_ENOMEM, buf);
+    }
+    char *b = (char *)it->base;
+    IterParams &p = it->p;
+    p.n_stars = n;
+    p.cap = lib_size;
+    p.lib_row0 = lib_row0;
+    p.chunk = chunk;
+    p.n_req = n_requested;
+    p.safety = safety_factor;
+    p.maxiter = maxiter;
+    p.state = (int64_t *)(b + o_state);
+    p.pcg0 = (const uint64_t *)(b + o_pcg);
+    p.segs = (joker_accept_seg *)(b + o_segs);
+    p.blk_base = (int64_t *)(b + o_base);
+    p.total_blocks = (int64_t *)(b + o_tot);
+    p.items = (WorkItem *)(b + o_items);
+    p.n_items = (int *)(b + o_nitems);
+    p.exact_key = (unsigned long long *)(b + o_exact);
+    p.done_count = (int *)(b + o_done);
+    it->lnl = (double *)(b + o_lnl);
+    it->err = mixed ? (float *)(b + o_err) : nullptr;
+    it->max_key = (unsigned long long *)(b + o_mk);
+    it->bound_key = (unsigned long long *)(b + o_bk);
+    it->words = (uint32_t *)(b + o_words);
+    it->amb = (uint32_t *)(b + o_amb);
+    it->blk_count = (int64_t *)(b + o_bc);
+    it->counts = (int64_t *)(b + o_cnt);
+    p.counts = it->counts;
+    it->out_idx = (int64_t *)(b + o_oidx);
+    it->out_lnl = (double *)(b + o_olnl);
+    it->n_refined = (unsigned long long *)(b + o_nref);
+    it->queue = (int *)(b + o_queue);
+    // initial state and the constant parts of the segments (host copies, once)
+    std::vector<int64_t> st((size_t)n * ST_FIELDS, 0);
+    for (int s = 0; s < n; ++s) st[(size_t)s * ST_FIELDS + ST_NPROC] = init_batch;
+    std::vector<joker_accept_seg> segs(n);
+    memset(segs.data(), 0, sizeof(joker_accept_seg) * n);
+    for (int s = 0; s < n; ++s) {
+        joker_accept_seg &g = segs[s];
+        g.lnl_off = (int64_t)s * lib_size;
+        g.idx_base = 0;
+        g.out_off = (int64_t)s * n_requested;
+        g.max_out = n_requested;
+        g.max_slot = s;
+        g.star = s;
+        g.row0 = lib_row0;
+    }
+    if ((e = cudaMemset(it->base, 0, off)) != cudaSuccess ||
+        (e = cudaMemcpy(p.state, st.data(), 8 * st.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy((void *)p.pcg0, pcg_states, 32 * (size_t)n, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(p.segs, segs.data(), sizeof(joker_accept_seg) * n, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        cudaFree(it->base);
+        delete it;
+        return iter_fail(JOKER_ECUDA, "joker_iter_create: initialisation copy failed");
+    }
+    *out = it;
+    return JOKER_OK;
+}
+
+extern "C" int joker_iter_destroy(joker_iter *it) {
+    if (!it) return JOKER_OK;
+    cudaFree(it->base);
+    delete it;
+    return JOKER_OK;
+}
+
+// One round.  Launches only (capturable into a CUDA graph).
+extern "C" int joker_iter_round(joker_iter *it, void *stream) {
+    if (!it) return iter_fail(JOKER_EINVAL, "joker_iter_round: NULL handle");
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool mixed = it->precision != JOKER_FP64;
+    iter_plan_kernel<<<1, 1024, 0, st>>>(it->p, mixed ? 1 : 0);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
+    // ln L over the planned items
+    const StarRec *recs; const double *ep64; const float *ep32; int n_stars, L, jit; int *queue;
+    stars_internals(it->stars, &recs, &ep64, &ep32, &n_stars, &L, &jit, &queue);
+    int64_t cap; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
+    cache_internals(it->cache, &cap, &P, &E, &OM, &M0, &S, &ma, &mb, &ms);
+    LnlArgs a;
+    memset(&a, 0, sizeof a);
+    a.stars = recs; a.ep64 = ep64; a.ep32 = ep32;
+    a.P = P; a.e = E; a.om = OM; a.M0 = M0; a.s = S; a.stride = 1;
+    a.mx_a = ma; a.mx_b = mb; a.mx_s2 = ms;
+    a.items = it->p.items;
+    a.n_items = (int)it->items_cap;
+    a.n_items_dev = it->p.n_items;
+    a.queue = it->queue;
+    a.lnl = it->lnl;
+    a.max_key = it->max_key;
+    if (mixed) {
+        a.err = it->err;
+        a.bound_key = it->bound_key;
+        a.err_c0 = mixed_err_c0();
+    }
+    if ((e = cudaMemsetAsync(it->queue, 0, sizeof(int), st)) != cudaSuccess ||
+        (e = launch_lnl(it->precision, L, jit != 0, a, 128, st)) != cudaSuccess)
+        return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
+    // acceptance over every active star's prefix (grid-stride over the
+    // device-counted blocks)
+    AcceptArgs c;
+    memset(&c, 0, sizeof c);
+    if (mixed) {
+        c.err = it->err;
+        c.bound_key = it->bound_key;
+        c.exact_key = it->p.exact_key;
+        c.stars = recs;
+        c.ep64 = ep64;
+        c.P = P; c.E = E; c.OM = OM; c.M0 = M0; c.S = S;
+        c.L = L;
+        c.jit = jit;
+        c.n_refined = it->n_refined;
+        c.amb_words = it->amb;
+        c.max_key = it->p.exact_key;
+    } else {
+        c.max_key = it->max_key;
+    }
+    c.segs = it->p.segs;
+    c.blk_base = it->p.blk_base;
+    c.total_blocks_dev = it->p.total_blocks;
+    c.n_segs = it->p.n_stars;
+    c.lnl = it->lnl;
+    c.u_source = JOKER_U_PCG64;
+    c.words = it->words;
+    c.blk_count = it->blk_count;
+    c.out_idx = it->out_idx;
+    c.out_lnl = it->out_lnl;
+    c.count = it->counts;
+    // fixed grid: enough CTAs to cover the device, blocks looped in-kernel
+    const int64_t grid = std::min<int64_t>(it->max_blocks, 152 * 8);
+    if ((e = launch_accept(c, grid, st, false)) != cudaSuccess)
+        return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
+    iter_update_kernel<<<(n_stars + 255) / 256, 256, 0, st>>>(it->p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
+    return JOKER_OK;
+}
+
+// Device pointers of the results for the caller to copy: per star the state
+// row (8 int64: start, n_process, n_evals, n_good, done, rounds, uniforms
+// drawn, 0), the first n_requested accepted indices and their ln L, and the
+// number of finished stars.
+extern "C" int joker_iter_outputs(const joker_iter *it, int64_t **d_state, int64_t **d_idx,
+                                  double **d_lnl, int **d_done, uint64_t **d_n_refined) {
+    if (!it) return iter_fail(JOKER_EINVAL, "joker_iter_outputs: NULL handle");
+    if (d_state) *d_state = it->p.state;
+    if (d_idx) *d_idx = it->out_idx;
+    if (d_lnl) *d_lnl = it->out_lnl;
+    if (d_done) *d_done = it->p.done_count;
+    if (d_n_refined) *d_n_refined = (uint64_t *)it->n_refined;
+    return JOKER_OK;
+}
+
+// Synchronous copy of the results to host arrays (any may be NULL): the state
+// rows (n_stars x 8), the accepted indices and their ln L (n_stars x
+// n_requested) and the finished-star count.
+extern "C" int joker_iter_read(const joker_iter *it, int64_t *h_state, int64_t *h_idx,
+                               double *h_lnl, int *h_done, uint64_t *h_n_refined) {
+    if (!it) return iter_fail(JOKER_EINVAL, "joker_iter_read: NULL handle");
+    const size_t n = (size_t)it->p.n_stars, r = (size_t)it->p.n_req;
+    cudaError_t e = cudaSuccess;
+    if (h_done && e == cudaSuccess) e = cudaMemcpy(h_done, it->p.done_count, 4, cudaMemcpyDeviceToHost);
+    if (h_state && e == cudaSuccess)
+        e = cudaMemcpy(h_state, it->p.state, 8 * n * ST_FIELDS, cudaMemcpyDeviceToHost);
+    if (h_idx && e == cudaSuccess) e = cudaMemcpy(h_idx, it->out_idx, 8 * n * r, cudaMemcpyDeviceToHost);
+    if (h_lnl && e == cudaSuccess) e = cudaMemcpy(h_lnl, it->out_lnl, 8 * n * r, cudaMemcpyDeviceToHost);
+    if (h_n_refined && e == cudaSuccess)
+        e = cudaMemcpy(h_n_refined, it->n_refined, 8, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
+    return JOKER_OK;
+}

@@ -65,7 +65,7 @@ lnl_fp64_kernel(LnlArgs a) {
         if (threadIdx.x == 0) s_item = atomicAdd(a.queue, 1);
         __syncthreads();
         const int it = s_item;
-        if (it >= a.n_items) break;
+        if (it >= item_count(a)) break;
         const WorkItem w = get_item(a, it);
         const StarRec &st = a.stars[w.star];
         const int N = st.n_epochs;
@@ -138,7 +138,7 @@ lnl_mixed_kernel(LnlArgs a) {
         if (threadIdx.x == 0) s_item = atomicAdd(a.queue, 1);
         __syncthreads();
         const int it = s_item;
-        if (it >= a.n_items) break;
+        if (it >= item_count(a)) break;
         const WorkItem w = get_item(a, it);
         const StarRec &st = a.stars[w.star];
         const int N = st.n_epochs;
@@ -497,7 +497,7 @@ static cudaError_t launch_persistent(K kern, const LnlArgs &a, int block, cudaSt
     if (e != cudaSuccess) return e;
     if (occ < 1) occ = 1;
     int grid = sms * occ;
-    if (grid > a.n_items) grid = a.n_items;
+    if (!a.n_items_dev && grid > a.n_items) grid = a.n_items;
     if (grid < 1) return cudaSuccess;
     kern<<<grid, block, 0, st>>>(a);
     return cudaGetLastError();
