@@ -115,6 +115,17 @@ int joker_stars_create(joker_stars **out, int n_stars, int n_linear,
                        const double *lambda, const double *k_prior,
                        int jitter_mode);
 int joker_stars_destroy(joker_stars *stars);
+
+/* A table of n_slots empty stars with room for max_epochs epochs each, for a
+ * serving loop that takes stars as they arrive.  joker_stars_set fills (or
+ * refills) one slot with the per-star arguments of joker_stars_create; its
+ * copies are ordered on `stream`. */
+int joker_stars_create_slots(joker_stars **out, int n_slots, int max_epochs, int n_linear,
+                             int jitter_mode);
+int joker_stars_set(joker_stars *stars, int slot, int n_epochs, const double *t,
+                    const double *rv, const double *ivar, double t_ref, const double *trend_M,
+                    const double *mu, const double *lambda, const double *k_prior,
+                    void *stream);
 int joker_stars_info(const joker_stars *stars, int *n_stars, int *n_linear,
                      int64_t *total_epochs, int *max_epochs);
 
@@ -224,6 +235,18 @@ int joker_iter_destroy(joker_iter *it);
 int joker_iter_round(joker_iter *it, void *stream);
 int joker_iter_outputs(const joker_iter *it, int64_t **d_state, int64_t **d_idx,
                        double **d_lnl, int **d_done, uint64_t **d_n_refined);
+/* A handle with every slot of a slot table empty, whose per-star ln L
+ * buffers are carved from one pool of pool_samples samples, and the
+ * admission of one request into a slot between rounds: its library budget
+ * (cache rows [lib_row0, lib_row0 + budget)), samples requested (at most
+ * max_requested), first batch, pool offset and PCG64 state.  A slot is free
+ * again once its state row reports done != 0. */
+int joker_iter_create_pool(joker_iter **out, const joker_stars *stars, const joker_cache *cache,
+                           int precision, int64_t lib_row0, int64_t pool_samples,
+                           int max_requested, double safety_factor, int maxiter, int chunk);
+int joker_iter_admit(joker_iter *it, int slot, int64_t budget, int n_requested,
+                     int64_t init_batch, int64_t pool_off, const uint64_t *pcg_state,
+                     void *stream);
 /* Synchronous copy of the same outputs to host arrays (any may be NULL). */
 int joker_iter_read(const joker_iter *it, int64_t *h_state, int64_t *h_idx, double *h_lnl,
                     int *h_done, uint64_t *h_n_refined);

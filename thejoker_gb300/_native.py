@@ -22,11 +22,11 @@ JOKER_MAX_LINEAR = 6
 # every extern "C" symbol of include/joker_gb300.h
 EXPORTED = (
     "joker_abi_version", "joker_last_error", "joker_stars_create", "joker_stars_destroy",
-    "joker_stars_info", "joker_cache_create", "joker_cache_destroy", "joker_cache_load",
+    "joker_stars_info", "joker_stars_create_slots", "joker_stars_set", "joker_cache_create", "joker_cache_destroy", "joker_cache_load",
     "joker_cache_capacity", "joker_batch_marginal_ln_likelihood", "joker_lnl",
     "joker_key_to_double", "joker_accept_workspace", "joker_accept", "joker_accept_refined",
     "joker_refine_max", "joker_iter_create", "joker_iter_destroy", "joker_iter_round",
-    "joker_iter_outputs", "joker_iter_read",
+    "joker_iter_outputs", "joker_iter_read", "joker_iter_create_pool", "joker_iter_admit",
     "joker_accept_noalloc",
 )
 
@@ -60,6 +60,10 @@ _SIGS = {
     "joker_stars_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int),
                                         ctypes.POINTER(ctypes.c_int), _lp,
                                         ctypes.POINTER(ctypes.c_int)]),
+    "joker_stars_create_slots": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_int]),
+    "joker_stars_set": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp,
+                                       ctypes.c_double, _dp, _dp, _dp, _dp, _vp]),
     "joker_cache_create": (ctypes.c_int, [ctypes.POINTER(_vp), _i64]),
     "joker_cache_destroy": (ctypes.c_int, [_vp]),
     "joker_cache_load": (ctypes.c_int, [_vp, _vp, _i64, _i64, _vp]),
@@ -86,6 +90,11 @@ _SIGS = {
                                           ctypes.POINTER(_vp), ctypes.POINTER(_vp),
                                           ctypes.POINTER(_vp)]),
     "joker_iter_read": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "joker_iter_create_pool": (ctypes.c_int, [ctypes.POINTER(_vp), _vp, _vp, ctypes.c_int, _i64,
+                                              _i64, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                              ctypes.c_int]),
+    "joker_iter_admit": (ctypes.c_int, [_vp, ctypes.c_int, _i64, ctypes.c_int, _i64, _i64,
+                                        ctypes.POINTER(ctypes.c_uint64), _vp]),
     "joker_accept_noalloc": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                             ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

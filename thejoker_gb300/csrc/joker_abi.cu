@@ -46,6 +46,7 @@ static int fail(int code, const char *fmt, ...) {
 
 struct joker_stars {
     int n_stars = 0, L = 0, jitter = 0, max_epochs = 0;
+    int slot_epochs = 0;         // > 0 for a slot table (joker_stars_create_slots)
     int64_t total_epochs = 0;
     std::vector<int64_t> off;
     StarRec *d_stars = nullptr;
@@ -114,6 +115,116 @@ static bool spd_inverse(int n, const long double *A, long double *Ainv, long dou
     return true;
 }
 
+// Per-star preparation on the host, in FP64 / long double: the StarRec
+// constants and the epoch records of both kernels.  Epoch records are written
+// at rec64 / rec32 (n epochs each); the record's epoch_off is set by the caller.
+static int prep_star(int k, int L, int jitter_mode, int n, const double *t, const double *rv,
+                     const double *ivar, double t_ref, const double *trend_M, const double *muk,
+                     const double *lamk, const double *kp, StarRec &r, double *rec64,
+                     float *rec32) {
+    const int T = L - 1;
+    const long double LOG2PI = logl(2.0L * 3.141592653589793238462643383279502884L);
+    for (int i = 0; i < n; ++i)
+        if (!(ivar[i] > 0.0) || !std::isfinite(ivar[i]) || !std::isfinite(t[i]) ||
+            !std::isfinite(rv[i]))
+            return fail(JOKER_EINVAL, "star %d epoch %d: ivar must be positive and finite, t and "
+                                      "rv finite", k, i);
+    if (T > 0)
+        for (int i = 0; i < n; ++i)
+            if (trend_M[(size_t)i * T] != 1.0)
+                return fail(JOKER_EINVAL, "star %d: column 0 of trend_M must be 1 (the constant "
+                                          "v0 term of the reference's design matrix)", k);
+    for (int j = 0; j < L; ++j)
+        if (!(lamk[j] > 0.0) && !(j == 0 && kp[0] != 0.0))
+            return fail(JOKER_EINVAL, "star %d: prior variance lambda[%d] must be > 0", k, j);
+    if (kp[0] != 0.0 && !(kp[1] > 0.0 && kp[2] > 0.0 && kp[3] > 0.0))
+        return fail(JOKER_EINVAL, "star %d: scaled K prior needs sigma_K0, P0, max_K > 0", k);
+    const int32_t keep_off = r.epoch_off;
+    memset(&r, 0, sizeof r);
+    r.epoch_off = keep_off;
+    r.n_epochs = n;
+    r.k_scaled = kp[0] != 0.0;
+    r.mu0 = muk[0];
+    r.lam0 = lamk[0];
+    r.sigK0sq = kp[1] * kp[1];
+    r.P0 = kp[2];
+    r.maxK2 = kp[3] * kp[3];
+    r.log_kscale = r.k_scaled ? std::log(r.sigK0sq) + 2.0 / 3.0 * std::log(r.P0) : 0.0;
+    r.log_maxK2 = r.k_scaled ? std::log(r.maxK2) : 0.0;
+    for (int j = 0; j < L; ++j) r.lam[j] = lamk[j];
+    std::vector<long double> C(T * T, 0.0L), c(T, 0.0L), Cinv(T * T, 0.0L);
+    long double Syy = 0.0L, slog_ivar = 0.0L, slog_lam = 0.0L, sw = 0.0L;
+    for (int j = 1; j < L; ++j) slog_lam += logl((long double)lamk[j]);
+    for (int i = 0; i < n; ++i) {
+        const double dt = t[i] - t_ref;
+        long double yp = rv[i];
+        for (int j = 1; j < L; ++j) yp -= (long double)muk[j] * trend_M[(size_t)i * T + (j - 1)];
+        const long double w = ivar[i];
+        sw += w;
+        Syy += w * yp * yp;
+        slog_ivar += logl(w);
+        for (int j = 0; j < T; ++j) {
+            const long double Tj = trend_M[(size_t)i * T + j];
+            c[j] += w * Tj * yp;
+            for (int m = 0; m < T; ++m) C[j * T + m] += w * Tj * trend_M[(size_t)i * T + m];
+        }
+        // FP64 record: dt, y', ivar, T_1..T_{L-1}
+        double *r64 = rec64 + (size_t)i * REC64;
+        for (int q = 0; q < REC64; ++q) r64[q] = 0.0;
+        r64[0] = dt;
+        r64[1] = (double)yp;
+        r64[2] = ivar[i];
+        for (int j = 0; j < T; ++j) r64[3 + j] = trend_M[(size_t)i * T + j];
+        // mixed record
+        float *r32 = rec32 + (size_t)i * REC32;
+        for (int q = 0; q < REC32; ++q) r32[q] = 0.0f;
+        split_ff(dt, r32[0], r32[1]);
+        if (jitter_mode == JOKER_JITTER_REFERENCE) {
+            // dt, w, w y', w T_j
+            split_ff(ivar[i], r32[2], r32[3]);
+            split_ff((double)(w * yp), r32[4], r32[5]);
+            for (int j = 0; j < T; ++j)
+                split_ff((double)(w * (long double)trend_M[(size_t)i * T + j]), r32[6 + 2 * j],
+                         r32[7 + 2 * j]);
+        } else {
+            // dt, ivar, y', y'^2, T_j
+            r32[2] = (float)ivar[i];
+            r32[3] = 0.0f;
+            split_ff((double)yp, r32[4], r32[5]);
+            split_ff((double)(yp * yp), r32[6], r32[7]);
+            for (int j = 0; j < T; ++j)
+                split_ff(trend_M[(size_t)i * T + j], r32[8 + 2 * j], r32[9 + 2 * j]);
+        }
+    }
+    for (int j = 0; j < T; ++j) C[j * T + j] += 1.0L / (long double)lamk[j + 1];
+    long double logdetC = 0.0L;
+    if (T > 0 && !spd_inverse(T, C.data(), Cinv.data(), logdetC))
+        return fail(JOKER_EINVAL, "star %d: trend block of the linear system is not positive definite", k);
+    long double cCc = 0.0L;
+    for (int j = 0; j < T; ++j) {
+        long double v = 0.0L;
+        for (int m = 0; m < T; ++m) v += Cinv[j * T + m] * c[m];
+        r.cC[j + 1] = (double)v;
+        cCc += c[j] * v;
+        for (int m = 0; m < T; ++m) r.Cinv[(j + 1) * MAXL + (m + 1)] = (double)Cinv[j * T + m];
+    }
+    r.chi2_0 = (double)(Syy - cCc);
+    split_ff(r.chi2_0, r.chi2_0_hi, r.chi2_0_lo);
+    for (int j = 1; j < L; ++j) {
+        split_ff(r.cC[j], r.cC_hi[j], r.cC_lo[j]);
+        for (int m = 1; m < L; ++m)
+            split_ff(r.Cinv[j * MAXL + m], r.Cinv_hi[j * MAXL + m], r.Cinv_lo[j * MAXL + m]);
+        split_ff((double)(1.0L / (long double)lamk[j]), r.ilam_hi[j], r.ilam_lo[j]);
+    }
+    r.sum_ivar = (float)(sw * (1.0L + 1e-6L));   // rounded up: an upper bound
+    r.mu0_f = (float)muk[0];
+    r.mu0_zero = muk[0] == 0.0;
+    r.logdet_const = (double)(n * LOG2PI - slog_ivar + slog_lam + logdetC);
+    r.log_norm_rest = (double)(n * LOG2PI + slog_lam);
+    r.sum_log_ivar = (double)slog_ivar;
+    return JOKER_OK;
+}
+
 extern "C" int joker_stars_create(joker_stars **out, int n_stars, int n_linear,
                                   const int64_t *epoch_offsets, const double *t,
                                   const double *rv, const double *ivar, const double *t_ref,
@@ -131,11 +242,6 @@ extern "C" int joker_stars_create(joker_stars **out, int n_stars, int n_linear,
     if (!epoch_offsets || !t || !rv || !ivar || !t_ref || !mu || !lambda || !k_prior ||
         (n_linear > 1 && !trend_M))
         return fail(JOKER_EINVAL, "joker_stars_create: NULL array argument");
-    if (n_linear > 1)
-        for (int64_t i = 0; i < epoch_offsets[n_stars]; ++i)
-            if (trend_M[i * (n_linear - 1)] != 1.0)
-                return fail(JOKER_EINVAL, "joker_stars_create: column 0 of trend_M must be 1 (the "
-                                          "constant v0 term of the reference's design matrix)");
     if (epoch_offsets[0] != 0) return fail(JOKER_EINVAL, "epoch_offsets[0] must be 0");
     const int L = n_linear, T = n_linear - 1;
     int max_ep = 0;
@@ -146,111 +252,18 @@ extern "C" int joker_stars_create(joker_stars **out, int n_stars, int n_linear,
         max_ep = std::max<int>(max_ep, (int)n);
     }
     const int64_t NE = epoch_offsets[n_stars];
-    for (int64_t i = 0; i < NE; ++i)
-        if (!(ivar[i] > 0.0) || !std::isfinite(ivar[i]) || !std::isfinite(t[i]) ||
-            !std::isfinite(rv[i]))
-            return fail(JOKER_EINVAL, "epoch %lld: ivar must be positive and finite, t and rv finite",
-                        (long long)i);
     std::vector<StarRec> recs(n_stars);
     std::vector<double> ep64((size_t)NE * REC64, 0.0);
     std::vector<float> ep32((size_t)NE * REC32, 0.0f);
-    const long double LOG2PI = logl(2.0L * 3.141592653589793238462643383279502884L);
     for (int k = 0; k < n_stars; ++k) {
-        const double *muk = mu + (size_t)k * L, *lamk = lambda + (size_t)k * L;
-        const double *kp = k_prior + (size_t)k * 4;
-        for (int j = 0; j < L; ++j)
-            if (!(lamk[j] > 0.0) && !(j == 0 && kp[0] != 0.0))
-                return fail(JOKER_EINVAL, "star %d: prior variance lambda[%d] must be > 0", k, j);
-        if (kp[0] != 0.0 && !(kp[1] > 0.0 && kp[2] > 0.0 && kp[3] > 0.0))
-            return fail(JOKER_EINVAL, "star %d: scaled K prior needs sigma_K0, P0, max_K > 0", k);
-        StarRec &r = recs[k];
-        memset(&r, 0, sizeof r);
         const int64_t e0 = epoch_offsets[k];
         const int n = (int)(epoch_offsets[k + 1] - e0);
-        r.epoch_off = (int32_t)e0;
-        r.n_epochs = n;
-        r.k_scaled = kp[0] != 0.0;
-        r.mu0 = muk[0];
-        r.lam0 = lamk[0];
-        r.sigK0sq = kp[1] * kp[1];
-        r.P0 = kp[2];
-        r.maxK2 = kp[3] * kp[3];
-        r.log_kscale = r.k_scaled ? std::log(r.sigK0sq) + 2.0 / 3.0 * std::log(r.P0) : 0.0;
-        r.log_maxK2 = r.k_scaled ? std::log(r.maxK2) : 0.0;
-        for (int j = 0; j < L; ++j) r.lam[j] = lamk[j];
-        // sums in long double
-        std::vector<long double> C(T * T, 0.0L), c(T, 0.0L), Cinv(T * T, 0.0L);
-        long double Syy = 0.0L, slog_ivar = 0.0L, slog_lam = 0.0L;
-        for (int j = 1; j < L; ++j) slog_lam += logl((long double)lamk[j]);
-        for (int i = 0; i < n; ++i) {
-            const int64_t g = e0 + i;
-            const double dt = t[g] - t_ref[k];
-            long double yp = rv[g];
-            for (int j = 1; j < L; ++j) yp -= (long double)muk[j] * trend_M[g * T + (j - 1)];
-            const long double w = ivar[g];
-            Syy += w * yp * yp;
-            slog_ivar += logl(w);
-            for (int j = 0; j < T; ++j) {
-                const long double Tj = trend_M[g * T + j];
-                c[j] += w * Tj * yp;
-                for (int m = 0; m < T; ++m) C[j * T + m] += w * Tj * trend_M[g * T + m];
-            }
-            // FP64 record: dt, y', ivar, T_1..T_{L-1}
-            double *r64 = &ep64[(size_t)g * REC64];
-            r64[0] = dt;
-            r64[1] = (double)yp;
-            r64[2] = ivar[g];
-            for (int j = 0; j < T; ++j) r64[3 + j] = trend_M[g * T + j];
-            // mixed record
-            float *r32 = &ep32[(size_t)g * REC32];
-            split_ff(dt, r32[0], r32[1]);
-            if (jitter_mode == JOKER_JITTER_REFERENCE) {
-                // dt, w, w y', w T_j
-                split_ff(ivar[g], r32[2], r32[3]);
-                split_ff((double)(w * yp), r32[4], r32[5]);
-                for (int j = 0; j < T; ++j)
-                    split_ff((double)(w * (long double)trend_M[g * T + j]), r32[6 + 2 * j],
-                             r32[7 + 2 * j]);
-            } else {
-                // dt, ivar, y', y'^2, T_j
-                r32[2] = (float)ivar[g];
-                r32[3] = 0.0f;
-                split_ff((double)yp, r32[4], r32[5]);
-                split_ff((double)(yp * yp), r32[6], r32[7]);
-                for (int j = 0; j < T; ++j)
-                    split_ff(trend_M[g * T + j], r32[8 + 2 * j], r32[9 + 2 * j]);
-            }
-        }
-        for (int j = 0; j < T; ++j) C[j * T + j] += 1.0L / (long double)lamk[j + 1];
-        long double logdetC = 0.0L;
-        if (T > 0 && !spd_inverse(T, C.data(), Cinv.data(), logdetC))
-            return fail(JOKER_EINVAL, "star %d: trend block of the linear system is not positive definite", k);
-        long double cCc = 0.0L;
-        for (int j = 0; j < T; ++j) {
-            long double v = 0.0L;
-            for (int m = 0; m < T; ++m) v += Cinv[j * T + m] * c[m];
-            r.cC[j + 1] = (double)v;
-            cCc += c[j] * v;
-            for (int m = 0; m < T; ++m) r.Cinv[(j + 1) * MAXL + (m + 1)] = (double)Cinv[j * T + m];
-        }
-        r.chi2_0 = (double)(Syy - cCc);
-        split_ff(r.chi2_0, r.chi2_0_hi, r.chi2_0_lo);
-        for (int j = 1; j < L; ++j) {
-            split_ff(r.cC[j], r.cC_hi[j], r.cC_lo[j]);
-            for (int m = 1; m < L; ++m)
-                split_ff(r.Cinv[j * MAXL + m], r.Cinv_hi[j * MAXL + m], r.Cinv_lo[j * MAXL + m]);
-            split_ff((double)(1.0L / (long double)lamk[j]), r.ilam_hi[j], r.ilam_lo[j]);
-        }
-        {
-            long double sw = 0.0L;
-            for (int i = 0; i < n; ++i) sw += ivar[e0 + i];
-            r.sum_ivar = (float)(sw * (1.0L + 1e-6L));   // rounded up: an upper bound
-        }
-        r.mu0_f = (float)muk[0];
-        r.mu0_zero = muk[0] == 0.0;
-        r.logdet_const = (double)(n * LOG2PI - slog_ivar + slog_lam + logdetC);
-        r.log_norm_rest = (double)(n * LOG2PI + slog_lam);
-        r.sum_log_ivar = (double)slog_ivar;
+        recs[k].epoch_off = (int32_t)e0;
+        const int rc = prep_star(k, L, jitter_mode, n, t + e0, rv + e0, ivar + e0, t_ref[k],
+                                 T > 0 ? trend_M + (size_t)e0 * T : nullptr,
+                                 mu + (size_t)k * L, lambda + (size_t)k * L, k_prior + (size_t)k * 4,
+                                 recs[k], &ep64[(size_t)e0 * REC64], &ep32[(size_t)e0 * REC32]);
+        if (rc != JOKER_OK) return rc;
     }
     std::vector<int> order(n_stars);
     for (int k = 0; k < n_stars; ++k) order[k] = k;
@@ -287,6 +300,86 @@ extern "C" int joker_stars_create(joker_stars **out, int n_stars, int n_linear,
         return fail(JOKER_ECUDA, "joker_stars_create: cudaMemcpy: %s", cudaGetErrorString(e));
     }
     *out = s;
+    return JOKER_OK;
+}
+
+// A table of n_slots empty stars with room for max_epochs epochs each; slots
+// are filled (and refilled) by joker_stars_set.
+extern "C" int joker_stars_create_slots(joker_stars **out, int n_slots, int max_epochs,
+                                        int n_linear, int jitter_mode) {
+    if (!out) return fail(JOKER_EINVAL, "joker_stars_create_slots: out is NULL");
+    *out = nullptr;
+    if (n_slots <= 0 || max_epochs <= 0)
+        return fail(JOKER_EINVAL, "joker_stars_create_slots: n_slots and max_epochs must be > 0");
+    if ((int64_t)n_slots * max_epochs > ((int64_t)1 << 31) - 1)
+        return fail(JOKER_ERANGE, "joker_stars_create_slots: n_slots * max_epochs too large");
+    if (n_linear < 1 || n_linear > JOKER_MAX_LINEAR)
+        return fail(JOKER_EINVAL, "joker_stars_create_slots: n_linear=%d outside [1, %d]",
+                    n_linear, JOKER_MAX_LINEAR);
+    if (jitter_mode != JOKER_JITTER_REFERENCE && jitter_mode != JOKER_JITTER_APPLIED)
+        return fail(JOKER_EINVAL, "joker_stars_create_slots: unknown jitter_mode %d", jitter_mode);
+    joker_stars *s = new joker_stars();
+    s->n_stars = n_slots;
+    s->L = n_linear;
+    s->jitter = jitter_mode;
+    s->max_epochs = max_epochs;
+    s->slot_epochs = max_epochs;
+    s->total_epochs = (int64_t)n_slots * max_epochs;
+    s->off.resize(n_slots + 1);
+    for (int k = 0; k <= n_slots; ++k) s->off[k] = (int64_t)k * max_epochs;
+    std::vector<StarRec> recs(n_slots);
+    memset(recs.data(), 0, sizeof(StarRec) * n_slots);
+    for (int k = 0; k < n_slots; ++k) recs[k].epoch_off = (int32_t)(k * max_epochs);
+    std::vector<int> order(n_slots);
+    for (int k = 0; k < n_slots; ++k) order[k] = k;
+    cudaError_t e;
+    if ((e = cudaMalloc(&s->d_stars, sizeof(StarRec) * n_slots)) != cudaSuccess ||
+        (e = cudaMalloc(&s->d_ep64, sizeof(double) * REC64 * s->total_epochs)) != cudaSuccess ||
+        (e = cudaMalloc(&s->d_ep32, sizeof(float) * REC32 * s->total_epochs)) != cudaSuccess ||
+        (e = cudaMalloc(&s->d_queue, sizeof(int) * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&s->d_order, sizeof(int) * n_slots)) != cudaSuccess ||
+        (e = cudaMemcpy(s->d_stars, recs.data(), sizeof(StarRec) * n_slots,
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(s->d_order, order.data(), sizeof(int) * n_slots,
+                        cudaMemcpyHostToDevice)) != cudaSuccess) {
+        joker_stars_destroy(s);
+        return fail(JOKER_ENOMEM, "joker_stars_create_slots: %s", cudaGetErrorString(e));
+    }
+    *out = s;
+    return JOKER_OK;
+}
+
+// Fill slot `slot` of a slot table with one star (the per-star arguments of
+// joker_stars_create).  The copies are ordered on `stream`; the host arrays
+// are read before the call returns.
+extern "C" int joker_stars_set(joker_stars *s, int slot, int n_epochs, const double *t,
+                               const double *rv, const double *ivar, double t_ref,
+                               const double *trend_M, const double *mu, const double *lambda,
+                               const double *k_prior, void *stream) {
+    if (!s) return fail(JOKER_EINVAL, "joker_stars_set: NULL handle");
+    if (s->slot_epochs <= 0) return fail(JOKER_EINVAL, "joker_stars_set: not a slot table");
+    if (slot < 0 || slot >= s->n_stars)
+        return fail(JOKER_EINVAL, "joker_stars_set: slot %d outside [0, %d)", slot, s->n_stars);
+    if (n_epochs <= 0 || n_epochs > s->slot_epochs)
+        return fail(JOKER_ERANGE, "joker_stars_set: %d epochs outside [1, %d]", n_epochs,
+                    s->slot_epochs);
+    if (!t || !rv || !ivar || !mu || !lambda || !k_prior || (s->L > 1 && !trend_M))
+        return fail(JOKER_EINVAL, "joker_stars_set: NULL array argument");
+    StarRec r;
+    memset(&r, 0, sizeof r);
+    r.epoch_off = slot * s->slot_epochs;
+    std::vector<double> r64((size_t)n_epochs * REC64);
+    std::vector<float> r32((size_t)n_epochs * REC32);
+    const int rc = prep_star(slot, s->L, s->jitter, n_epochs, t, rv, ivar, t_ref, trend_M, mu,
+                             lambda, k_prior, r, r64.data(), r32.data());
+    if (rc != JOKER_OK) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemcpyAsync(s->d_ep64 + (size_t)r.epoch_off * REC64, r64.data(),
+                             sizeof(double) * r64.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->d_ep32 + (size_t)r.epoch_off * REC32, r32.data(),
+                             sizeof(float) * r32.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->d_stars + slot, &r, sizeof(StarRec), cudaMemcpyHostToDevice, st));
+    // pageable sources: staged before the calls return
     return JOKER_OK;
 }
 

@@ -38,14 +38,17 @@ namespace {
 
 constexpr int ST_START = 0, ST_NPROC = 1, ST_NEVALS = 2, ST_NGOOD = 3, ST_DONE = 4,
               ST_ROUNDS = 5, ST_UCONS = 6, ST_FIELDS = 8;
+constexpr int64_t DONE_EMPTY = 4;          // a slot without a request
 constexpr int64_t BLOCK_SAMPLES = 8192;   // samples per acceptance CTA block
 
 struct IterParams {
     int n_stars;
-    int64_t cap;            // library size (samples per star prefix at most)
     int64_t lib_row0;       // cache row of library sample 0
     int chunk;              // samples per ln L work item
-    int n_req;
+    int max_req;            // output slots per star
+    int64_t *cap;           // per star: library size (its prefix grows to at most this)
+    int *n_req;             // per star: samples requested
+    int64_t *lnl_off;       // per star: offset of its ln L / error buffer in the pool
     double safety;
     int maxiter;
     int64_t *state;
@@ -83,7 +86,7 @@ __global__ void __launch_bounds__(1024) iter_plan_kernel(IterParams p, int zero_
                     w.row0 = p.lib_row0 + start + c * p.chunk;
                     const int64_t rem = np - c * p.chunk;
                     w.count = (int)(rem < p.chunk ? rem : p.chunk);
-                    w.out_off = (int64_t)s * p.cap + start + c * p.chunk;
+                    w.out_off = p.lnl_off[s] + start + c * p.chunk;
                     w.max_slot = s;
                     w.pad = 0;
                     p.items[pos + c] = w;
@@ -91,6 +94,9 @@ __global__ void __launch_bounds__(1024) iter_plan_kernel(IterParams p, int zero_
                 const int64_t n_evals = start + np;
                 st[ST_NEVALS] = n_evals;
                 g.n = n_evals;
+                g.lnl_off = p.lnl_off[s];
+                g.out_off = (int64_t)s * p.max_req;
+                g.max_out = p.n_req[s];
                 // the star's uniforms for this round follow those of the
                 // earlier rounds in its generator's stream
                 const u128 s0 = ((u128)p.pcg0[4 * s] << 64) | (u128)p.pcg0[4 * s + 1];
@@ -136,14 +142,14 @@ __global__ void iter_update_kernel(IterParams p) {
     int64_t done = 0;
     if (n_good == 0) {
         done = 2;                            // "Failed to find any good samples!"
-    } else if (n_good >= p.n_req) {
+    } else if (n_good >= p.n_req[s]) {
         done = 1;
     } else {
         const int64_t start = st[ST_START] + st[ST_NPROC];
-        const int64_t n_need = p.n_req - n_good;
+        const int64_t n_need = p.n_req[s] - n_good;
         double v = p.safety * (double)n_need / (double)n_good * (double)n_evals;
         int64_t np = (int64_t)v;
-        if (start + np > p.cap) np = p.cap - start;
+        if (start + np > p.cap[s]) np = p.cap[s] - start;
         st[ST_START] = start;
         st[ST_NPROC] = np;
         if (np <= 0) done = 1;               // the library is exhausted: keep what passed
@@ -155,6 +161,25 @@ __global__ void iter_update_kernel(IterParams p) {
     }
 }
 
+// Start a request in slot s (between rounds): its schedule, pool buffer and
+// uniform stream; the slot's running maxima are reset.
+__global__ void iter_admit_kernel(IterParams p, unsigned long long *max_key,
+                                  unsigned long long *bound_key, int s, int64_t budget, int n_req,
+                                  int64_t init, int64_t pool_off, uint64_t s_hi, uint64_t s_lo,
+                                  uint64_t i_hi, uint64_t i_lo) {
+    int64_t *st = p.state + (int64_t)s * ST_FIELDS;
+    for (int f = 0; f < ST_FIELDS; ++f) st[f] = 0;
+    st[ST_NPROC] = init;
+    p.cap[s] = budget;
+    p.n_req[s] = n_req;
+    p.lnl_off[s] = pool_off;
+    uint64_t *pc = const_cast<uint64_t *>(p.pcg0) + 4 * s;
+    pc[0] = s_hi; pc[1] = s_lo; pc[2] = i_hi; pc[3] = i_lo;
+    max_key[s] = 0ull;
+    bound_key[2 * s] = 0ull;
+    bound_key[2 * s + 1] = 0ull;
+}
+
 }  // namespace
 
 struct joker_iter {
@@ -163,7 +188,7 @@ struct joker_iter {
     int precision = 0;
     int L = 0, jit = 0;
     IterParams p{};
-    int64_t max_blocks = 0, items_cap = 0;
+    int64_t max_blocks = 0, items_cap = 0, pool = 0;
     void *base = nullptr;                    // one allocation holds every buffer
     double *lnl = nullptr;
     float *err = nullptr;
@@ -191,29 +216,31 @@ static int iter_fail(int code, const char *msg) {
 
 static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
-extern "C" int joker_iter_create(joker_iter **out, const joker_stars *stars,
-                                 const joker_cache *cache, int precision, int64_t lib_row0,
-                                 int64_t lib_size, int n_requested, int64_t init_batch,
-                                 double safety_factor, int maxiter, const uint64_t *pcg_states,
-                                 int chunk) {
-    if (!out || !stars || !cache || !pcg_states)
-        return iter_fail(JOKER_EINVAL, "joker_iter_create: NULL argument");
+// Allocate a handle for n_slots stars whose ln L prefixes share a pool of
+// pool_samples samples.  Every slot starts empty.
+static int iter_alloc(joker_iter **out, const joker_stars *stars, const joker_cache *cache,
+                      int precision, int64_t lib_row0, int64_t pool_samples, int max_req,
+                      double safety_factor, int maxiter, int chunk, const char *who) {
+    char buf[256];
+    if (!out || !stars || !cache) {
+        snprintf(buf, sizeof buf, "%s: NULL argument", who);
+        return iter_fail(JOKER_EINVAL, buf);
+    }
     *out = nullptr;
     const StarRec *recs; const double *ep64; const float *ep32; int n_stars, L, jit; int *queue;
     stars_internals(stars, &recs, &ep64, &ep32, &n_stars, &L, &jit, &queue);
     int64_t cap; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
     cache_internals(cache, &cap, &P, &E, &OM, &M0, &S, &ma, &mb, &ms);
-    if (lib_row0 < 0 || lib_size <= 0 || lib_row0 + lib_size > cap)
-        return iter_fail(JOKER_ERANGE, "joker_iter_create: library rows outside the cache");
-    if (n_requested <= 0 || init_batch <= 0 || maxiter <= 0 || !(safety_factor > 0))
-        return iter_fail(JOKER_EINVAL, "joker_iter_create: bad schedule parameters");
-    if (init_batch > lib_size)
-        return iter_fail(JOKER_EINVAL, "Prior sample library not big enough! For iterative "
-                                       "sampling, you have to have at least growth_factor * "
-                                       "n_requested_samples samples in the library.");
-    if (precision != JOKER_FP64 && precision != JOKER_MIXED && precision != JOKER_MIXED_ACCURATE)
-        return iter_fail(JOKER_EINVAL, "joker_iter_create: precision must be FP64 or a mixed "
-                                       "precision with error bounds");
+    if (lib_row0 < 0 || lib_row0 >= cap || pool_samples <= 0 || max_req <= 0 || maxiter <= 0 ||
+        !(safety_factor > 0)) {
+        snprintf(buf, sizeof buf, "%s: bad library, pool or schedule parameters", who);
+        return iter_fail(JOKER_EINVAL, buf);
+    }
+    if (precision != JOKER_FP64 && precision != JOKER_MIXED && precision != JOKER_MIXED_ACCURATE) {
+        snprintf(buf, sizeof buf, "%s: precision must be FP64 or a mixed precision with error "
+                                  "bounds", who);
+        return iter_fail(JOKER_EINVAL, buf);
+    }
     if (chunk <= 0) chunk = 1024;
     joker_iter *it = new joker_iter();
     it->stars = stars;
@@ -222,38 +249,41 @@ extern "C" int joker_iter_create(joker_iter **out, const joker_stars *stars,
     it->L = L;
     it->jit = jit;
     const int n = n_stars;
-    const int64_t bps = (lib_size + BLOCK_SAMPLES - 1) / BLOCK_SAMPLES;
-    it->max_blocks = bps * n;
-    it->items_cap = (int64_t)n * ((lib_size + chunk - 1) / chunk);
+    it->pool = pool_samples;
+    it->max_blocks = pool_samples / BLOCK_SAMPLES + n + 1;
+    it->items_cap = pool_samples / chunk + n + 1;
     const bool mixed = precision != JOKER_FP64;
-    // layout of the single allocation
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += al(bytes); return o; };
     const size_t o_state = take(8 * (size_t)n * ST_FIELDS), o_pcg = take(32 * (size_t)n),
+                 o_cap = take(8 * (size_t)n), o_nreq = take(4 * (size_t)n),
+                 o_loff = take(8 * (size_t)n),
                  o_segs = take(sizeof(joker_accept_seg) * (size_t)n),
                  o_base = take(8 * ((size_t)n + 1)), o_tot = take(8),
                  o_items = take(sizeof(WorkItem) * (size_t)it->items_cap), o_nitems = take(4),
-                 o_exact = take(8 * (size_t)n), o_done = take(4), o_lnl = take(8 * (size_t)n * lib_size),
-                 o_err = mixed ? take(4 * (size_t)n * lib_size) : 0, o_mk = take(8 * (size_t)n),
+                 o_exact = take(8 * (size_t)n), o_done = take(4),
+                 o_lnl = take(8 * (size_t)pool_samples),
+                 o_err = mixed ? take(4 * (size_t)pool_samples) : 0, o_mk = take(8 * (size_t)n),
                  o_bk = take(16 * (size_t)n), o_words = take(4 * 256 * (size_t)it->max_blocks),
                  o_amb = take(4 * 256 * (size_t)it->max_blocks),
                  o_bc = take(8 * (size_t)it->max_blocks), o_cnt = take(8 * (size_t)n),
-                 o_oidx = take(8 * (size_t)n * n_requested), o_olnl = take(8 * (size_t)n * n_requested),
+                 o_oidx = take(8 * (size_t)n * max_req), o_olnl = take(8 * (size_t)n * max_req),
                  o_nref = take(8), o_queue = take(16);
     cudaError_t e = cudaMalloc(&it->base, off);
     if (e != cudaSuccess) {
         delete it;
-        char buf[200];
-        snprintf(buf, sizeof buf, "joker_iter_create: cudaMalloc(%zu): %s", off, cudaGetErrorString(e));
+        snprintf(buf, sizeof buf, "%s: cudaMalloc(%zu): %s", who, off, cudaGetErrorString(e));
         return iter_fail(JOKER_ENOMEM, buf);
     }
     char *b = (char *)it->base;
     IterParams &p = it->p;
     p.n_stars = n;
-    p.cap = lib_size;
     p.lib_row0 = lib_row0;
     p.chunk = chunk;
-    p.n_req = n_requested;
+    p.max_req = max_req;
+    p.cap = (int64_t *)(b + o_cap);
+    p.n_req = (int *)(b + o_nreq);
+    p.lnl_off = (int64_t *)(b + o_loff);
     p.safety = safety_factor;
     p.maxiter = maxiter;
     p.state = (int64_t *)(b + o_state);
@@ -278,28 +308,98 @@ extern "C" int joker_iter_create(joker_iter **out, const joker_stars *stars,
     it->out_lnl = (double *)(b + o_olnl);
     it->n_refined = (unsigned long long *)(b + o_nref);
     it->queue = (int *)(b + o_queue);
-    // initial state and the constant parts of the segments (host copies, once)
+    // every slot empty; the constant parts of the segments
     std::vector<int64_t> st((size_t)n * ST_FIELDS, 0);
-    for (int s = 0; s < n; ++s) st[(size_t)s * ST_FIELDS + ST_NPROC] = init_batch;
+    for (int s = 0; s < n; ++s) st[(size_t)s * ST_FIELDS + ST_DONE] = DONE_EMPTY;
     std::vector<joker_accept_seg> segs(n);
     memset(segs.data(), 0, sizeof(joker_accept_seg) * n);
     for (int s = 0; s < n; ++s) {
-        joker_accept_seg &g = segs[s];
-        g.lnl_off = (int64_t)s * lib_size;
-        g.idx_base = 0;
-        g.out_off = (int64_t)s * n_requested;
-        g.max_out = n_requested;
-        g.max_slot = s;
-        g.star = s;
-        g.row0 = lib_row0;
+        segs[s].max_slot = s;
+        segs[s].star = s;
+        segs[s].row0 = lib_row0;
     }
     if ((e = cudaMemset(it->base, 0, off)) != cudaSuccess ||
         (e = cudaMemcpy(p.state, st.data(), 8 * st.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy((void *)p.pcg0, pcg_states, 32 * (size_t)n, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(p.segs, segs.data(), sizeof(joker_accept_seg) * n, cudaMemcpyHostToDevice)) != cudaSuccess) {
         cudaFree(it->base);
         delete it;
-        return iter_fail(JOKER_ECUDA, "joker_iter_create: initialisation copy failed");
+        snprintf(buf, sizeof buf, "%s: initialisation failed: %s", who, cudaGetErrorString(e));
+        return iter_fail(JOKER_ECUDA, buf);
+    }
+    *out = it;
+    return JOKER_OK;
+}
+
+extern "C" int joker_iter_admit(joker_iter *it, int slot, int64_t budget, int n_requested,
+                                int64_t init_batch, int64_t pool_off, const uint64_t *pcg_state,
+                                void *stream) {
+    if (!it || !pcg_state) return iter_fail(JOKER_EINVAL, "joker_iter_admit: NULL argument");
+    if (slot < 0 || slot >= it->p.n_stars)
+        return iter_fail(JOKER_EINVAL, "joker_iter_admit: slot out of range");
+    int64_t cap; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
+    cache_internals(it->cache, &cap, &P, &E, &OM, &M0, &S, &ma, &mb, &ms);
+    if (budget <= 0 || it->p.lib_row0 + budget > cap)
+        return iter_fail(JOKER_ERANGE, "joker_iter_admit: budget outside the cache");
+    if (n_requested <= 0 || n_requested > it->p.max_req)
+        return iter_fail(JOKER_ERANGE, "joker_iter_admit: n_requested outside [1, max_req]");
+    if (init_batch <= 0 || init_batch > budget)
+        return iter_fail(JOKER_EINVAL, "Prior sample library not big enough! For iterative "
+                                       "sampling, you have to have at least growth_factor * "
+                                       "n_requested_samples samples in the library.");
+    if (pool_off < 0 || pool_off + budget > it->pool)
+        return iter_fail(JOKER_ERANGE, "joker_iter_admit: pool range outside the pool");
+    iter_admit_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(
+        it->p, it->max_key, it->bound_key, slot, budget, n_requested, init_batch, pool_off,
+        pcg_state[0], pcg_state[1], pcg_state[2], pcg_state[3]);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
+    return JOKER_OK;
+}
+
+extern "C" int joker_iter_create_pool(joker_iter **out, const joker_stars *stars,
+                                      const joker_cache *cache, int precision, int64_t lib_row0,
+                                      int64_t pool_samples, int max_requested,
+                                      double safety_factor, int maxiter, int chunk) {
+    return iter_alloc(out, stars, cache, precision, lib_row0, pool_samples, max_requested,
+                      safety_factor, maxiter, chunk, "joker_iter_create_pool");
+}
+
+extern "C" int joker_iter_create(joker_iter **out, const joker_stars *stars,
+                                 const joker_cache *cache, int precision, int64_t lib_row0,
+                                 int64_t lib_size, int n_requested, int64_t init_batch,
+                                 double safety_factor, int maxiter, const uint64_t *pcg_states,
+                                 int chunk) {
+    if (!pcg_states || !stars) return iter_fail(JOKER_EINVAL, "joker_iter_create: NULL argument");
+    int n_stars = 0;
+    {
+        const StarRec *r; const double *a; const float *b; int L, jit; int *q;
+        stars_internals(stars, &r, &a, &b, &n_stars, &L, &jit, &q);
+    }
+    int64_t cap; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
+    cache_internals(cache, &cap, &P, &E, &OM, &M0, &S, &ma, &mb, &ms);
+    if (lib_row0 < 0 || lib_size <= 0 || lib_row0 + lib_size > cap)
+        return iter_fail(JOKER_ERANGE, "joker_iter_create: library rows outside the cache");
+    if (n_requested <= 0 || init_batch <= 0)
+        return iter_fail(JOKER_EINVAL, "joker_iter_create: bad schedule parameters");
+    if (init_batch > lib_size)
+        return iter_fail(JOKER_EINVAL, "Prior sample library not big enough! For iterative "
+                                       "sampling, you have to have at least growth_factor * "
+                                       "n_requested_samples samples in the library.");
+    joker_iter *it = nullptr;
+    int rc = iter_alloc(&it, stars, cache, precision, lib_row0, lib_size * n_stars, n_requested,
+                        safety_factor, maxiter, chunk, "joker_iter_create");
+    if (rc != JOKER_OK) return rc;
+    for (int s = 0; s < n_stars; ++s) {
+        rc = joker_iter_admit(it, s, lib_size, n_requested, init_batch, (int64_t)s * lib_size,
+                              pcg_states + 4 * (size_t)s, nullptr);
+        if (rc != JOKER_OK) {
+            joker_iter_destroy(it);
+            return rc;
+        }
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        joker_iter_destroy(it);
+        return iter_fail(JOKER_ECUDA, "joker_iter_create: admission failed");
     }
     *out = it;
     return JOKER_OK;
@@ -404,7 +504,7 @@ extern "C" int joker_iter_outputs(const joker_iter *it, int64_t **d_state, int64
 extern "C" int joker_iter_read(const joker_iter *it, int64_t *h_state, int64_t *h_idx,
                                double *h_lnl, int *h_done, uint64_t *h_n_refined) {
     if (!it) return iter_fail(JOKER_EINVAL, "joker_iter_read: NULL handle");
-    const size_t n = (size_t)it->p.n_stars, r = (size_t)it->p.n_req;
+    const size_t n = (size_t)it->p.n_stars, r = (size_t)it->p.max_req;
     cudaError_t e = cudaSuccess;
     if (h_done && e == cudaSuccess) e = cudaMemcpy(h_done, it->p.done_count, 4, cudaMemcpyDeviceToHost);
     if (h_state && e == cudaSuccess)

@@ -66,6 +66,37 @@ class StarTable:
         self.epoch_offsets = off
         self.n_epochs = np.diff(off)
 
+    @classmethod
+    def slots(cls, n_slots, max_epochs, n_linear, jitter="reference"):
+        """An empty slot table (joker_stars_create_slots), filled by ``set``."""
+        self = cls.__new__(cls)
+        jm = {"reference": nat.JOKER_JITTER_REFERENCE, "applied": nat.JOKER_JITTER_APPLIED}[jitter]
+        torch.cuda.init()
+        h = ctypes.c_void_p()
+        nat.check(nat.lib().joker_stars_create_slots(ctypes.byref(h), int(n_slots),
+                                                     int(max_epochs), int(n_linear), jm),
+                  "joker_stars_create_slots")
+        self._h = h
+        self.n_stars = int(n_slots)
+        self.n_linear = int(n_linear)
+        self.jitter = jitter
+        self.max_epochs = int(max_epochs)
+        return self
+
+    def set(self, slot, star, stream=None):
+        """Fill slot ``slot`` with one star (a dict as the constructor takes)."""
+        N = len(star["t"])
+        L = self.n_linear
+        trend = _f64(np.asarray(star["trend_M"], dtype=np.float64).reshape(N, L - 1)) if L > 1 \
+            else np.zeros(1)
+        t, rv, ivar = _f64(star["t"]), _f64(star["rv"]), _f64(star["ivar"])
+        mu, lam, kp = _f64(star["mu"]), _f64(star["lam"]), _f64(star["k_prior"])
+        nat.check(nat.lib().joker_stars_set(self.handle, int(slot), N, nat.dptr(t), nat.dptr(rv),
+                                            nat.dptr(ivar), float(star["t_ref"]),
+                                            nat.dptr(trend), nat.dptr(mu), nat.dptr(lam),
+                                            nat.dptr(kp), stream_handle(stream)),
+                  "joker_stars_set")
+
     @property
     def handle(self):
         if self._h is None:
