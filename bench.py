@@ -412,6 +412,229 @@ def run_batched(args, rank, world):
     }
 
 
+def run_iterative(args, rank, world):
+    """Iterative rejection of 1024 stars with a quadratic trend (poly_trend=3:
+    K, v0, v1, v2 with N(0, [100 km/s, 1 km/s/d, 0.01 km/s/d^2]) priors), 8-64
+    epochs each, n_requested = 256, over a 2^22-sample prior library; every
+    round on the device, rounds after the first replayed from a CUDA graph.
+    The plain FP64 path runs the same schedule on a 64-star subset."""
+    import torch
+    from thejoker_gb300 import build as tb
+    from thejoker_gb300 import device as dev
+    from thejoker_gb300.iterative import IterativeBatch
+    from thejoker_gb300.synthetic import fill_prior_cache, survey_stars
+    tb.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    n_stars, S, n_req = args.stars, args.samples, args.n_requested
+    stars = survey_stars(n_stars * world, seed=4, n_min=8, n_max=64,
+                         poly_trend=3)[rank * n_stars:(rank + 1) * n_stars]
+    host = np.empty((S, 5))
+    fill_prior_cache(host, SEED_CACHE + 1)
+    cache = dev.PriorCache.from_samples(host)
+    table = dev.StarTable(stars)
+    seeds = lambda k: np.arange(n_stars) + 7919 * k + rank * n_stars
+    it = IterativeBatch(table, cache, n_req, precision="mixed", seeds=seeds(0))
+    it.run()
+    for w in range(args.warmup):
+        it.reset(seeds(w + 1)).run()
+    torch.cuda.synchronize()
+    evals, rounds = [], []
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            it.reset(seeds(100 + k)).run()
+            st, _, _ = it.results()
+            evals.append(int(st[:, 2].sum()))
+            rounds.append(int(st[:, 5].max()))
+        ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    # eager rounds (no graph) and the FP64 path on a subset, same schedule
+    sub = min(args.subset_stars, n_stars)
+    table_sub = dev.StarTable(stars[:sub])
+    res = {}
+    for prec in ("mixed", "fp64"):
+        b = IterativeBatch(table_sub, cache, n_req, precision=prec, seeds=np.arange(sub))
+        b.run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.reset(np.arange(sub)).run()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        stt, idx, _ = b.results()
+        res[prec] = (dt, stt, idx)
+        b.close()
+    same = bool(np.array_equal(res["mixed"][1], res["fp64"][1]) and
+                all(np.array_equal(a, b) for a, b in zip(res["mixed"][2], res["fp64"][2])))
+    eager = IterativeBatch(table, cache, n_req, precision="mixed", seeds=seeds(100))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eager.run(use_graph=False)
+    eager_ms = (time.perf_counter() - t0) * 1e3
+    eager.close()
+    n_ep = np.array([len(s["t"]) for s in stars])
+    ev = float(np.mean(evals))
+    return {
+        "metric": "prior samples/s (lnL+accept), iterative",
+        "value": ev * world / (ms * 1e-3), "unit": "samples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded survey, numpy prior library)",
+        "config": {"workload": f"{n_stars} stars, poly_trend=3, epochs log-uniform [8,64] "
+                               f"(mean {n_ep.mean():.1f}), n_requested={n_req}, prior library "
+                               f"2^{int(math.log2(S))}, rounds replayed from a CUDA graph",
+                   "stars_per_gpu": n_stars, "library": S, "n_requested": n_req},
+        "stars_per_s": n_stars * world / (ms * 1e-3),
+        "samples_evaluated_per_step": ev, "rounds_per_step": float(np.mean(rounds)),
+        "eager_rounds_ms": eager_ms,
+        "subset": {"stars": sub, "mixed_s": res["mixed"][0], "fp64_s": res["fp64"][0],
+                   "speedup_mixed_vs_fp64": res["fp64"][0] / res["mixed"][0],
+                   "results_identical": same},
+        "clocks": clk.summary(),
+    }
+
+
+def _serving_requests(n, seed, budget_log2=(20, 27), n_req_choices=(1, 128, 512)):
+    from thejoker_gb300.synthetic import survey_stars
+    rng = np.random.default_rng(seed)
+    stars = survey_stars(n, seed=seed + 1, n_min=3, n_max=200, poly_trend=1)
+    budgets = (2.0 ** rng.uniform(*budget_log2, n)).astype(np.int64)
+    n_reqs = rng.choice(np.asarray(n_req_choices), n)
+    return stars, budgets, n_reqs
+
+
+def _serve_stream(eng, reqs, arrivals):
+    """Feed requests at their arrival times (seconds from now) and step the
+    engine until all are done; latency counts from the scheduled arrival."""
+    t_start = time.perf_counter()
+    arr = t_start + np.asarray(arrivals)
+    i, n = 0, len(reqs)
+    n_done0 = len(eng.done)
+    while i < n or eng.active or eng.queue:
+        now = time.perf_counter()
+        while i < n and arr[i] <= now:
+            eng.submit(reqs[i], t=arr[i])
+            i += 1
+        if not eng.active and not eng.queue:
+            if i < n:
+                while time.perf_counter() < arr[i]:
+                    pass
+            continue
+        eng.step()
+    span = time.perf_counter() - t_start
+    done = eng.done[n_done0:]
+    lat = np.array([r.t_done - r.t_arrival for r in done])
+    evals = sum(r.result[2] for r in done)
+    return lat, span, evals
+
+
+def _lindley(arrivals, service):
+    """Latencies of a FIFO single server (one star at a time)."""
+    t_free, out = 0.0, np.empty(len(arrivals))
+    for k, (a, s) in enumerate(zip(arrivals, service)):
+        start = max(a, t_free)
+        t_free = start + s
+        out[k] = t_free - a
+    return out
+
+
+def run_serving(args, rank, world):
+    """Serving: a Poisson stream of star requests (epochs log-uniform [3,200],
+    prior budget log-uniform 2^20-2^27 samples of a device-resident 2^28
+    cache, n_requested in {1, 128, 512}), admitted by free device memory into
+    the continuously batched iterative rounds; p50/p99 latency and throughput
+    per arrival rate, and the plain FP64 per-star path (one star at a time)
+    measured on a prefix of the stream, its latency at each rate from its
+    measured service times (FIFO queue)."""
+    import torch
+    from thejoker_gb300 import build as tb
+    from thejoker_gb300 import device as dev
+    from thejoker_gb300.serve import Request, ServingEngine
+    from thejoker_gb300.synthetic import fill_prior_cache
+    tb.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    S = args.samples
+    host = torch.empty((S, 5), dtype=torch.float64).pin_memory()
+    fill_prior_cache(host.numpy(), SEED_CACHE + 2)
+    cache = dev.PriorCache(S)
+    stage = torch.empty((1 << 24, 5), dtype=torch.float64, device="cuda")
+    for a in range(0, S, 1 << 24):
+        b = min(S, a + (1 << 24))
+        stage[: b - a].copy_(host[a:b], non_blocking=True)
+        cache.load(stage[: b - a], row0=a)
+    torch.cuda.synchronize()
+    del stage, host
+    torch.cuda.empty_cache()
+    n_all = args.requests
+    stars, budgets, n_reqs = _serving_requests(n_all, 11 + rank)
+
+    def make(k):
+        return Request(stars[k], budget=int(budgets[k]), n_requested=int(n_reqs[k]),
+                       seed=100000 + k)
+
+    eng = ServingEngine(cache, n_slots=args.slots, max_epochs=200, n_linear=2,
+                        max_requested=512, precision="mixed", round_budget=args.round_budget,
+                        pool_fraction=0.6)
+    # warm-up: the first rounds load the kernels and capture the round graph
+    for k in range(min(n_all, 64)):
+        eng.submit(make(k))
+    eng.drain()
+    rates = [float(r) for r in args.rates.split(",")]
+    rng = np.random.default_rng(77)
+    sweep = []
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        for rate in rates:
+            n = int(min(n_all, max(200, rate * args.window)))
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+            reqs = [make(k) for k in range(n)]
+            lat, span, evals = _serve_stream(eng, reqs, arrivals)
+            sweep.append({"rate_per_s": rate, "requests": n,
+                          "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                          "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                          "throughput_req_per_s": n / span,
+                          "samples_per_s": evals / span, "span_s": span})
+    rounds = eng.rounds
+    eng.close()
+    # plain FP64 per-star path: one star at a time, same requests
+    n64 = min(args.fp64_requests, n_all)
+    one = ServingEngine(cache, n_slots=1, max_epochs=200, n_linear=2, max_requested=512,
+                        precision="fp64", pool_samples=1 << 27)
+    one.submit(make(0))
+    one.drain()
+    service = []
+    for k in range(n64):
+        r = make(k)
+        t0 = time.perf_counter()
+        one.submit(r, t=t0)
+        one.drain()
+        service.append(time.perf_counter() - t0)
+    one.close()
+    service = np.array(service)
+    fp64 = {"requests_timed": n64, "mean_service_ms": float(service.mean() * 1e3),
+            "capacity_req_per_s": float(1.0 / service.mean()), "per_rate": []}
+    for rate in rates:
+        n = int(min(n_all, max(200, rate * args.window)))
+        arrivals = np.cumsum(np.random.default_rng(5).exponential(1.0 / rate, n))
+        lat = _lindley(arrivals, np.resize(service, n))
+        fp64["per_rate"].append({"rate_per_s": rate, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                                 "p99_ms": float(np.percentile(lat, 99) * 1e3)})
+    top = sweep[-1]
+    return {
+        "metric": "p50/p99 per-star latency and request throughput, serving",
+        "value": top["throughput_req_per_s"], "unit": "requests/s",
+        "n_gpus": world, "steps": len(rates), "warmup": 1,
+        "ms_per_step": top["span_s"] * 1e3 / max(top["requests"], 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded survey stream, numpy prior cache)",
+        "config": {"workload": "Poisson stream of star requests, epochs log-uniform [3,200], "
+                               "budget log-uniform 2^20-2^27 of a resident "
+                               f"2^{int(math.log2(S))} cache, n_requested in {{1,128,512}}",
+                   "slots": args.slots, "round_budget": args.round_budget,
+                   "requests_max": n_all, "window_s": args.window},
+        "sweep": sweep, "rounds": rounds,
+        "fp64_per_star": fp64,
+        "clocks": clk.summary(),
+    }
+
+
 def run_reference(args, rank):
     if rank != 0:
         return None
@@ -445,18 +668,31 @@ def main():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--samples", type=int, default=1 << 28)
+    p.add_argument("--samples", type=int, default=None)
     p.add_argument("--fp64-samples", type=int, default=1 << 25)
     p.add_argument("--cpu-samples", type=int, default=1 << 20)
     p.add_argument("--h2d-chunk", type=int, default=1 << 24)
     p.add_argument("--fp32-peak", type=float, default=67.6)
     p.add_argument("--traffic", type=float, default=None)
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", default="single", choices=["single", "batched"])
-    p.add_argument("--stars", type=int, default=4096)
+    p.add_argument("--config", default="single",
+                   choices=["single", "batched", "iterative", "serving"])
+    p.add_argument("--stars", type=int, default=None)
+    p.add_argument("--n-requested", type=int, default=256)
+    p.add_argument("--requests", type=int, default=20000)
+    p.add_argument("--rates", default="100,500,1000,2000,5000")
+    p.add_argument("--window", type=float, default=4.0)
+    p.add_argument("--slots", type=int, default=1024)
+    p.add_argument("--round-budget", type=int, default=1 << 26)
+    p.add_argument("--fp64-requests", type=int, default=32)
     p.add_argument("--group", type=int, default=None)
     p.add_argument("--subset-stars", type=int, default=64)
     args = p.parse_args()
+    if args.samples is None:
+        args.samples = {"single": 1 << 28, "batched": 1 << 24, "iterative": 1 << 22,
+                        "serving": 1 << 28}[args.config]
+    if args.stars is None:
+        args.stars = {"batched": 4096, "iterative": 1024}.get(args.config, 1)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
@@ -471,6 +707,10 @@ def main():
             dist = tdist
         if args.config == "batched":
             line = run_batched(args, rank, world)
+        elif args.config == "iterative":
+            line = run_iterative(args, rank, world)
+        elif args.config == "serving":
+            line = run_serving(args, rank, world)
         else:
             line = run_ours(args, rank, world, dist)
         if dist is not None:

@@ -240,13 +240,22 @@ int joker_iter_outputs(const joker_iter *it, int64_t **d_state, int64_t **d_idx,
  * admission of one request into a slot between rounds: its library budget
  * (cache rows [lib_row0, lib_row0 + budget)), samples requested (at most
  * max_requested), first batch, pool offset and PCG64 state.  A slot is free
- * again once its state row reports done != 0. */
+ * again once its state row reports done != 0; admitting into it takes it out
+ * of the finished-star count.  joker_iter_admit also restarts a star of a
+ * joker_iter_create handle (same slot, its own pool range). */
 int joker_iter_create_pool(joker_iter **out, const joker_stars *stars, const joker_cache *cache,
                            int precision, int64_t lib_row0, int64_t pool_samples,
                            int max_requested, double safety_factor, int maxiter, int chunk);
 int joker_iter_admit(joker_iter *it, int slot, int64_t budget, int n_requested,
                      int64_t init_batch, int64_t pool_off, const uint64_t *pcg_state,
                      void *stream);
+/* Samples evaluated per round over all stars (0, the default: no limit).  A
+ * star whose batch is larger than its equal share of the budget spreads the
+ * batch over several rounds; its acceptance runs once the batch is complete,
+ * so the results do not depend on the budget, only the time a round takes.
+ * Read at joker_iter_round launch: a captured graph keeps the budget it was
+ * captured with.  No counterpart in the reference. */
+int joker_iter_set_round_budget(joker_iter *it, int64_t samples);
 /* Synchronous copy of the same outputs to host arrays (any may be NULL). */
 int joker_iter_read(const joker_iter *it, int64_t *h_state, int64_t *h_idx, double *h_lnl,
                     int *h_done, uint64_t *h_n_refined);

@@ -31,9 +31,10 @@ def reference_iterative(lls_all, seed, n_req, init, n_total, safety=1.0, maxiter
     return good, len(allm)
 
 
-@pytest.mark.parametrize("precision,use_graph", [("fp64", False), ("fp64", True),
-                                                 ("mixed", True)])
-def test_iterative_matches_reference_loop(cuda, precision, use_graph):
+@pytest.mark.parametrize("precision,use_graph,budget", [("fp64", False, 0), ("fp64", True, 0),
+                                                        ("mixed", True, 0),
+                                                        ("mixed", True, 20000)])
+def test_iterative_matches_reference_loop(cuda, precision, use_graph, budget):
     from thejoker_gb300 import device as dev
     from thejoker_gb300.iterative import IterativeBatch
     from thejoker_gb300.synthetic import fill_prior_cache, survey_stars
@@ -45,7 +46,7 @@ def test_iterative_matches_reference_loop(cuda, precision, use_graph):
     seeds = np.arange(12) + 50
     n_req, init = 16, 2048
     it = IterativeBatch(table, cache, n_req, precision=precision, seeds=seeds,
-                        init_batch_size=init)
+                        init_batch_size=init, round_budget=budget)
     it.run(use_graph=use_graph)
     state, idx, nref = it.results()
     for k in range(12):
@@ -57,3 +58,34 @@ def test_iterative_matches_reference_loop(cuda, precision, use_graph):
             continue
         assert state[k, 3] == len(good), k
         np.testing.assert_array_equal(idx[k], good[:n_req])
+
+
+def test_reset_replays_same_graph(cuda):
+    """reset() re-admits every star; a second run on the captured round graph
+    gives the same results, and new seeds give those seeds' results."""
+    from thejoker_gb300 import device as dev
+    from thejoker_gb300.iterative import IterativeBatch
+    from thejoker_gb300.synthetic import fill_prior_cache, survey_stars
+    stars = survey_stars(6, seed=22, n_min=8, n_max=48, poly_trend=1)
+    chunk = fill_prior_cache(np.empty((1 << 16, 5)), 9)
+    cache = dev.PriorCache.from_samples(chunk)
+    table = dev.StarTable(stars)
+    it = IterativeBatch(table, cache, 8, precision="mixed", seeds=np.arange(6),
+                        init_batch_size=1024)
+    it.run()
+    s1, i1, _ = it.results()
+    g = it.graph
+    it.reset(np.arange(6)).run()
+    s2, i2, _ = it.results()
+    assert it.graph is g
+    np.testing.assert_array_equal(s1, s2)
+    for a, b in zip(i1, i2):
+        np.testing.assert_array_equal(a, b)
+    it.reset(np.arange(6) + 100).run()
+    s3, i3, _ = it.results()
+    fresh = IterativeBatch(table, cache, 8, precision="mixed", seeds=np.arange(6) + 100,
+                           init_batch_size=1024).run()
+    s4, i4, _ = fresh.results()
+    np.testing.assert_array_equal(s3, s4)
+    for a, b in zip(i3, i4):
+        np.testing.assert_array_equal(a, b)

@@ -50,9 +50,10 @@ def test_alone_equals_mix(cuda, served, precision):
         alone.submit(r)
         alone.drain()
     alone.close()
-    # mix: few slots and a small pool, so admission waits for slots and memory
+    # mix: few slots and a small pool, so admission waits for slots and memory;
+    # a small round budget spreads the large batches over several rounds
     mix = ServingEngine(cache, n_slots=6, max_epochs=64, n_linear=L, pool_samples=3 << 16,
-                        max_requested=32, precision=precision)
+                        max_requested=32, precision=precision, round_budget=1 << 14)
     reqs_m = _requests(stars, np.random.default_rng(5))
     for r in reqs_m[:8]:
         mix.submit(r)

@@ -27,7 +27,7 @@ EXPORTED = (
     "joker_key_to_double", "joker_accept_workspace", "joker_accept", "joker_accept_refined",
     "joker_refine_max", "joker_iter_create", "joker_iter_destroy", "joker_iter_round",
     "joker_iter_outputs", "joker_iter_read", "joker_iter_create_pool", "joker_iter_admit",
-    "joker_accept_noalloc",
+    "joker_iter_set_round_budget", "joker_accept_noalloc",
 )
 
 
@@ -95,6 +95,7 @@ _SIGS = {
                                               ctypes.c_int]),
     "joker_iter_admit": (ctypes.c_int, [_vp, ctypes.c_int, _i64, ctypes.c_int, _i64, _i64,
                                         ctypes.POINTER(ctypes.c_uint64), _vp]),
+    "joker_iter_set_round_budget": (ctypes.c_int, [_vp, _i64]),
     "joker_accept_noalloc": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                             ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

@@ -37,7 +37,7 @@ using namespace joker;
 namespace {
 
 constexpr int ST_START = 0, ST_NPROC = 1, ST_NEVALS = 2, ST_NGOOD = 3, ST_DONE = 4,
-              ST_ROUNDS = 5, ST_UCONS = 6, ST_FIELDS = 8;
+              ST_ROUNDS = 5, ST_UCONS = 6, ST_EVAL = 7, ST_FIELDS = 8;
 constexpr int64_t DONE_EMPTY = 4;          // a slot without a request
 constexpr int64_t BLOCK_SAMPLES = 8192;   // samples per acceptance CTA block
 
@@ -46,6 +46,7 @@ struct IterParams {
     int64_t lib_row0;       // cache row of library sample 0
     int chunk;              // samples per ln L work item
     int max_req;            // output slots per star
+    int64_t round_budget;   // samples per round over all stars (0: no limit)
     int64_t *cap;           // per star: library size (its prefix grows to at most this)
     int *n_req;             // per star: samples requested
     int64_t *lnl_off;       // per star: offset of its ln L / error buffer in the pool
@@ -56,6 +57,9 @@ struct IterParams {
     joker_accept_seg *segs;
     int64_t *blk_base;      // n_stars + 1
     int64_t *total_blocks;
+    int64_t *item_base;     // n_stars + 1: first work item of each star this round
+    int64_t *round_row;     // per star: first library row evaluated this round
+    int64_t *round_take;    // per star: samples evaluated this round
     WorkItem *items;
     int *n_items;
     unsigned long long *exact_key;
@@ -63,68 +67,126 @@ struct IterParams {
     int *done_count;
 };
 
-// One CTA: work items and segments of the active stars, then the block prefix.
-__global__ void __launch_bounds__(1024) iter_plan_kernel(IterParams p, int zero_exact) {
-    __shared__ int64_t s_part[1024];
-    if (threadIdx.x == 0) *p.n_items = 0;
+// Exclusive scan of one int64 per thread over a block of 1024 threads; the
+// block total goes to *total.
+__device__ __forceinline__ int64_t block_exclusive_scan(int64_t v, int64_t *s_warp,
+                                                        int64_t *total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
     __syncthreads();
-    int64_t carry = 0;
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        int64_t w = lane < nw ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) s_warp[lane] = w;         // inclusive warp prefix
+    }
+    __syncthreads();
+    const int64_t excl = x - v + (wid > 0 ? s_warp[wid - 1] : 0);
+    *total = s_warp[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return excl;
+}
+
+// One CTA of 1024 threads.  Pass 1: per active star the samples evaluated
+// this round (the rest of its current batch, at most an equal share of the
+// round budget) and, for stars whose batch completes, the acceptance segment;
+// items and acceptance blocks are scanned over the stars.  Pass 2: the work
+// items, all threads over all items.
+__global__ void __launch_bounds__(1024) iter_plan_kernel(IterParams p, int zero_exact) {
+    __shared__ int64_t s_warp[32];
+    __shared__ int s_active;
+    if (threadIdx.x == 0) s_active = 0;
+    __syncthreads();
+    for (int s = threadIdx.x; s < p.n_stars; s += blockDim.x)
+        if (p.state[(int64_t)s * ST_FIELDS + ST_DONE] == 0) atomicAdd(&s_active, 1);
+    __syncthreads();
+    int64_t share = INT64_MAX;
+    if (p.round_budget > 0 && s_active > 0) {
+        share = max((int64_t)p.chunk, p.round_budget / s_active);
+        share = (share + p.chunk - 1) / p.chunk * p.chunk;
+    }
+    int64_t carry_i = 0, carry_b = 0;
     for (int base = 0; base < p.n_stars; base += blockDim.x) {
         const int s = base + threadIdx.x;
-        int64_t nblk = 0;
+        int64_t nitem = 0, nblk = 0;
         if (s < p.n_stars) {
             int64_t *st = p.state + (int64_t)s * ST_FIELDS;
             joker_accept_seg &g = p.segs[s];
             if (zero_exact) p.exact_key[s] = 0ull;
+            g.n = 0;
             if (st[ST_DONE] == 0) {
-                const int64_t start = st[ST_START], np = st[ST_NPROC];
-                const int64_t nch = (np + p.chunk - 1) / p.chunk;
-                const int pos = atomicAdd(p.n_items, (int)nch);
-                for (int64_t c = 0; c < nch; ++c) {
-                    WorkItem w;
-                    w.star = s;
-                    w.row0 = p.lib_row0 + start + c * p.chunk;
-                    const int64_t rem = np - c * p.chunk;
-                    w.count = (int)(rem < p.chunk ? rem : p.chunk);
-                    w.out_off = p.lnl_off[s] + start + c * p.chunk;
-                    w.max_slot = s;
-                    w.pad = 0;
-                    p.items[pos + c] = w;
+                const int64_t start = st[ST_START], np = st[ST_NPROC], ev = st[ST_EVAL];
+                const int64_t take = min(np - ev, share);
+                nitem = (take + p.chunk - 1) / p.chunk;
+                p.round_row[s] = start + ev;
+                p.round_take[s] = take;
+                st[ST_EVAL] = ev + take;
+                st[ST_NEVALS] = start + ev + take;
+                if (ev + take == np) {
+                    // the batch is complete: accept over the whole prefix
+                    const int64_t n_evals = start + np;
+                    g.n = n_evals;
+                    g.lnl_off = p.lnl_off[s];
+                    g.out_off = (int64_t)s * p.max_req;
+                    g.max_out = p.n_req[s];
+                    // the star's uniforms for this acceptance follow those of
+                    // its earlier ones in its generator's stream
+                    const u128 s0 = ((u128)p.pcg0[4 * s] << 64) | (u128)p.pcg0[4 * s + 1];
+                    const u128 inc = ((u128)p.pcg0[4 * s + 2] << 64) | (u128)p.pcg0[4 * s + 3];
+                    const u128 sr = pcg_advance(s0, inc, (uint64_t)st[ST_UCONS]);
+                    g.pcg_state_hi = (uint64_t)(sr >> 64);
+                    g.pcg_state_lo = (uint64_t)sr;
+                    g.pcg_inc_hi = p.pcg0[4 * s + 2];
+                    g.pcg_inc_lo = p.pcg0[4 * s + 3];
+                    nblk = (n_evals + BLOCK_SAMPLES - 1) / BLOCK_SAMPLES;
                 }
-                const int64_t n_evals = start + np;
-                st[ST_NEVALS] = n_evals;
-                g.n = n_evals;
-                g.lnl_off = p.lnl_off[s];
-                g.out_off = (int64_t)s * p.max_req;
-                g.max_out = p.n_req[s];
-                // the star's uniforms for this round follow those of the
-                // earlier rounds in its generator's stream
-                const u128 s0 = ((u128)p.pcg0[4 * s] << 64) | (u128)p.pcg0[4 * s + 1];
-                const u128 inc = ((u128)p.pcg0[4 * s + 2] << 64) | (u128)p.pcg0[4 * s + 3];
-                const u128 sr = pcg_advance(s0, inc, (uint64_t)st[ST_UCONS]);
-                g.pcg_state_hi = (uint64_t)(sr >> 64);
-                g.pcg_state_lo = (uint64_t)sr;
-                g.pcg_inc_hi = p.pcg0[4 * s + 2];
-                g.pcg_inc_lo = p.pcg0[4 * s + 3];
-                nblk = (n_evals + BLOCK_SAMPLES - 1) / BLOCK_SAMPLES;
-            } else {
-                g.n = 0;
             }
         }
-        s_part[threadIdx.x] = nblk;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            const int m = min((int)blockDim.x, p.n_stars - base);
-            for (int k = 0; k < m; ++k) {
-                p.blk_base[base + k] = carry;
-                carry += s_part[k];
-            }
+        int64_t tot_i, tot_b;
+        const int64_t ei = block_exclusive_scan(nitem, s_warp, &tot_i);
+        const int64_t eb = block_exclusive_scan(nblk, s_warp, &tot_b);
+        if (s < p.n_stars) {
+            p.item_base[s] = carry_i + ei;
+            p.blk_base[s] = carry_b + eb;
         }
-        __syncthreads();
+        carry_i += tot_i;
+        carry_b += tot_b;
     }
     if (threadIdx.x == 0) {
-        p.blk_base[p.n_stars] = carry;
-        *p.total_blocks = carry;
+        p.item_base[p.n_stars] = carry_i;
+        p.blk_base[p.n_stars] = carry_b;
+        *p.total_blocks = carry_b;
+        *p.n_items = (int)carry_i;
+    }
+    __syncthreads();
+    // pass 2: item k belongs to the last star whose first item is <= k
+    for (int64_t k = threadIdx.x; k < carry_i; k += blockDim.x) {
+        int lo = 0, hi = p.n_stars;          // item_base[lo] <= k < item_base[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (p.item_base[mid] <= k) lo = mid; else hi = mid;
+        }
+        const int64_t c = k - p.item_base[lo];
+        const int64_t r = p.round_row[lo] + c * p.chunk;
+        const int64_t rem = p.round_take[lo] - c * p.chunk;
+        WorkItem w;
+        w.star = lo;
+        w.row0 = p.lib_row0 + r;
+        w.count = (int)(rem < p.chunk ? rem : p.chunk);
+        w.out_off = p.lnl_off[lo] + r;
+        w.max_slot = lo;
+        w.pad = 0;
+        p.items[k] = w;
     }
 }
 
@@ -134,6 +196,8 @@ __global__ void iter_update_kernel(IterParams p) {
     if (s >= p.n_stars) return;
     int64_t *st = p.state + (int64_t)s * ST_FIELDS;
     if (st[ST_DONE] != 0) return;
+    if (st[ST_EVAL] < st[ST_NPROC]) return;   // the batch continues next round
+    st[ST_EVAL] = 0;
     const int64_t n_good = p.counts[s];
     const int64_t n_evals = st[ST_NEVALS];
     st[ST_NGOOD] = n_good;
@@ -168,6 +232,8 @@ __global__ void iter_admit_kernel(IterParams p, unsigned long long *max_key,
                                   int64_t init, int64_t pool_off, uint64_t s_hi, uint64_t s_lo,
                                   uint64_t i_hi, uint64_t i_lo) {
     int64_t *st = p.state + (int64_t)s * ST_FIELDS;
+    // the finished count covers slots holding a finished request
+    if (st[ST_DONE] >= 1 && st[ST_DONE] <= 3) atomicSub(p.done_count, 1);
     for (int f = 0; f < ST_FIELDS; ++f) st[f] = 0;
     st[ST_NPROC] = init;
     p.cap[s] = budget;
@@ -260,6 +326,8 @@ static int iter_alloc(joker_iter **out, const joker_stars *stars, const joker_ca
                  o_loff = take(8 * (size_t)n),
                  o_segs = take(sizeof(joker_accept_seg) * (size_t)n),
                  o_base = take(8 * ((size_t)n + 1)), o_tot = take(8),
+                 o_ibase = take(8 * ((size_t)n + 1)), o_rrow = take(8 * (size_t)n),
+                 o_rtake = take(8 * (size_t)n),
                  o_items = take(sizeof(WorkItem) * (size_t)it->items_cap), o_nitems = take(4),
                  o_exact = take(8 * (size_t)n), o_done = take(4),
                  o_lnl = take(8 * (size_t)pool_samples),
@@ -291,6 +359,10 @@ static int iter_alloc(joker_iter **out, const joker_stars *stars, const joker_ca
     p.segs = (joker_accept_seg *)(b + o_segs);
     p.blk_base = (int64_t *)(b + o_base);
     p.total_blocks = (int64_t *)(b + o_tot);
+    p.item_base = (int64_t *)(b + o_ibase);
+    p.round_row = (int64_t *)(b + o_rrow);
+    p.round_take = (int64_t *)(b + o_rtake);
+    p.round_budget = 0;
     p.items = (WorkItem *)(b + o_items);
     p.n_items = (int *)(b + o_nitems);
     p.exact_key = (unsigned long long *)(b + o_exact);
@@ -402,6 +474,13 @@ extern "C" int joker_iter_create(joker_iter **out, const joker_stars *stars,
         return iter_fail(JOKER_ECUDA, "joker_iter_create: admission failed");
     }
     *out = it;
+    return JOKER_OK;
+}
+
+extern "C" int joker_iter_set_round_budget(joker_iter *it, int64_t samples) {
+    if (!it) return iter_fail(JOKER_EINVAL, "joker_iter_set_round_budget: NULL handle");
+    if (samples < 0) return iter_fail(JOKER_EINVAL, "joker_iter_set_round_budget: negative budget");
+    it->p.round_budget = samples;
     return JOKER_OK;
 }
 

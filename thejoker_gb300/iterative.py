@@ -32,7 +32,7 @@ class IterativeBatch:
 
     def __init__(self, table, cache, n_requested, precision="mixed", lib_row0=0, lib_size=None,
                  seeds=None, init_batch_size=None, growth_factor=128, safety_factor=1.0,
-                 maxiter=128, chunk=1024):
+                 maxiter=128, chunk=1024, round_budget=0):
         self.table, self.cache = table, cache
         self.n = table.n_stars
         self.n_requested = int(n_requested)
@@ -45,10 +45,8 @@ class IterativeBatch:
                              f"cache file. You have, or have limited to, {lib_size} samples.")
         if seeds is None:
             seeds = np.arange(self.n)
-        pcg = np.zeros((self.n, 4), dtype=np.uint64)
-        for k, sd in enumerate(seeds):
-            st, inc = dev.pcg64_state(np.random.default_rng(int(sd)))
-            pcg[k] = [st >> 64, st & ((1 << 64) - 1), inc >> 64, inc & ((1 << 64) - 1)]
+        pcg = self._pcg(seeds)
+        self.lib_size, self.init = lib_size, init
         h = ctypes.c_void_p()
         nat.check(nat.lib().joker_iter_create(
             ctypes.byref(h), table.handle, cache.handle, dev.PRECISIONS[precision],
@@ -56,8 +54,30 @@ class IterativeBatch:
             pcg.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), int(chunk)),
             "joker_iter_create")
         self._h = h
+        nat.check(nat.lib().joker_iter_set_round_budget(h, int(round_budget)),
+                  "joker_iter_set_round_budget")
         self.graph = None
         self.rounds = 0
+
+    def _pcg(self, seeds):
+        if len(seeds) != self.n:
+            raise ValueError("one seed per star")
+        pcg = np.zeros((self.n, 4), dtype=np.uint64)
+        for k, sd in enumerate(seeds):
+            st, inc = dev.pcg64_state(np.random.default_rng(int(sd)))
+            pcg[k] = [st >> 64, st & ((1 << 64) - 1), inc >> 64, inc & ((1 << 64) - 1)]
+        return pcg
+
+    def reset(self, seeds):
+        """Start every star again with new seeds (joker_iter_admit per star);
+        the buffers and a captured round graph stay valid."""
+        pcg = self._pcg(seeds)
+        st = dev.stream_handle()
+        for k in range(self.n):
+            nat.check(nat.lib().joker_iter_admit(
+                self._h, k, self.lib_size, self.n_requested, self.init, k * self.lib_size,
+                pcg[k].ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), st), "joker_iter_admit")
+        return self
 
     def _round(self):
         nat.check(nat.lib().joker_iter_round(self._h, dev.stream_handle()), "joker_iter_round")
@@ -69,7 +89,7 @@ class IterativeBatch:
                   "joker_iter_read")
         return int(out[0])
 
-    def run(self, use_graph=True, max_rounds=128):
+    def run(self, use_graph=True, max_rounds=1 << 20):
         """Run rounds until every star is finished; returns self.  The first
         round runs eagerly (it also loads the kernels); with use_graph the
         next rounds replay one captured round."""

@@ -83,11 +83,16 @@ class Request:
 
 
 class ServingEngine:
-    """Continuously batched iterative rejection over one prior cache."""
+    """Continuously batched iterative rejection over one prior cache.
+
+    round_budget: samples evaluated per round over all active stars (0: no
+    limit).  Large batches then take several rounds, which bounds the round
+    time, and with it how long a new request waits to start; the results do
+    not change."""
 
     def __init__(self, cache, n_slots=1024, max_epochs=256, n_linear=2, pool_samples=None,
                  max_requested=512, precision="mixed", safety_factor=1.0, maxiter=128,
-                 chunk=1024, use_graph=True, pool_fraction=0.5):
+                 chunk=1024, use_graph=True, pool_fraction=0.5, round_budget=0):
         self.cache = cache
         self.n_slots = int(n_slots)
         self.table = dev.StarTable.slots(n_slots, max_epochs, n_linear)
@@ -103,6 +108,8 @@ class ServingEngine:
             int(pool_samples), self.max_requested, float(safety_factor), int(maxiter),
             int(chunk)), "joker_iter_create_pool")
         self._h = h
+        nat.check(nat.lib().joker_iter_set_round_budget(h, int(round_budget)),
+                  "joker_iter_set_round_budget")
         self.use_graph = use_graph
         self.graph = None
         self.rounds = 0
