@@ -578,12 +578,18 @@ extern "C" int joker_lnl(const joker_stars *s, const joker_cache *c, int star0, 
 
 static int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
 
+// Entries of the refinement's flag list: 64 per 8192-sample block plus 2^16;
+// flagged samples beyond it are still refined, through the slower word scan.
+static int64_t flag_capacity(int64_t n_blocks) { return 65536 + 64 * n_blocks; }
+
 extern "C" int64_t joker_accept_workspace(const joker_accept_seg *segs, int n_segs) {
     if (!segs || n_segs <= 0) return 0;
     const int64_t nb = accept_blocks(segs, n_segs, nullptr);
-    // the second word array holds the undecided samples of joker_accept_refined
+    // the second word array and the flag list (with its two counters) serve
+    // the refinement of joker_accept_refined
     return align256(sizeof(joker_accept_seg) * (int64_t)n_segs) +
-           align256(8 * (int64_t)(n_segs + 1)) + align256(8 * nb) + 2 * align256(4 * 256 * nb);
+           align256(8 * (int64_t)(n_segs + 1)) + align256(8 * nb) + 2 * align256(4 * 256 * nb) +
+           align256(16) + align256(8 * flag_capacity(nb));
 }
 
 extern "C" int joker_accept(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
@@ -670,6 +676,10 @@ static int refined_setup(const joker_stars *s, const joker_cache *c, const joker
     uint32_t *d_words = (uint32_t *)w;
     w += align256(4 * 256 * nb);
     uint32_t *d_amb = (uint32_t *)w;
+    w += align256(4 * 256 * nb);
+    unsigned long long *d_fcount = (unsigned long long *)w;
+    w += align256(16);
+    int64_t *d_flags = (int64_t *)w;
     CUDA_TRY(cudaMemcpyAsync(d_segs, segs, sizeof(joker_accept_seg) * n_segs, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_base, base.data(), 8 * (n_segs + 1), cudaMemcpyHostToDevice, st));
     memset(&a, 0, sizeof a);
@@ -683,6 +693,9 @@ static int refined_setup(const joker_stars *s, const joker_cache *c, const joker
     a.jit = s->jitter == JOKER_JITTER_APPLIED;
     a.n_refined = (unsigned long long *)d_n_refined;
     a.amb_words = d_amb;
+    a.flag_list = d_flags;
+    a.flag_count = d_fcount;
+    a.flag_cap = flag_capacity(nb);
     a.segs = d_segs;
     a.blk_base = d_base;
     a.n_segs = n_segs;

@@ -83,6 +83,63 @@ __device__ __forceinline__ int interval_test(double lnl, float err, double mx, d
     return -1;
 }
 
+// ---- FP32 / integer fast paths -------------------------------------------
+// GB300 runs FP64 (and FP64 conversions) at 1/64 of the FP32 rate, so the
+// per-sample scans decide nearly every sample from float approximations built
+// with integer operations, with margins that cover their error, and fall back
+// to the FP64 tests above only near a decision boundary.
+
+// float of a double by truncating its mantissa (relative error < 2^-23);
+// false when the value is zero, subnormal in float, too large, inf or NaN.
+__device__ __forceinline__ bool dbl_to_float_trunc(double x, float &f) {
+    const long long b = __double_as_longlong(x);
+    const int hi = (int)(b >> 32);
+    const int ex = (hi >> 20) & 0x7ff;              // biased double exponent
+    if (ex < 1023 - 126 || ex > 1023 + 127) return false;
+    const unsigned mant = (unsigned)(b >> 29) & 0x7fffffu;
+    f = __int_as_float((hi & (int)0x80000000) | ((ex - 1023 + 127) << 23) | (int)mant);
+    return true;
+}
+
+// u = m 2^-53 (m the 53-bit integer of numpy's uniform double) as a float
+// truncated to 24 significant bits; m must be nonzero.
+__device__ __forceinline__ float u53_to_float(uint64_t m) {
+    const int lz = __clzll(m);                       // 11..63
+    const uint64_t norm = m << lz;                   // leading one at bit 63
+    const unsigned mant = (unsigned)(norm >> 40) & 0x7fffffu;
+    const int e2 = 63 - lz - 53;                     // u in [2^e2, 2^(e2+1))
+    return __int_as_float(((e2 + 127) << 23) | (int)mant);
+}
+
+// Decision of exp(v + [-er, er] - mx) > u from float approximations:
+// 1 keep, 0 reject, 2 undecided here (use the FP64 test).  uf = float u
+// (> 0, truncated), vf, mxf = float approximations of v, mx.
+__device__ __forceinline__ int fast_decide(float vf, float er, float mxf, float uf) {
+    const float lu = __logf(uf);                     // |error| < 4e-7 + |log(1 + 2^-23)|
+    const float tol = 1e-4f + 5e-7f * (fabsf(vf) + fabsf(mxf) + er);
+    const float d = vf - mxf;
+    if (d + er + tol < lu) return 0;
+    if (d - er - tol > lu) return 1;
+    return 2;
+}
+
+// Append a flagged sample to the compacted list (one atomic per warp);
+// returns false for the samples that did not fit.
+__device__ __forceinline__ bool flag_append(const AcceptArgs &a, int which, bool flag,
+                                            int si, int64_t i) {
+    const unsigned bal = __ballot_sync(0xffffffffu, flag);
+    if (!bal) return true;
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == __ffs(bal) - 1) base = atomicAdd(a.flag_count + which, (unsigned long long)__popc(bal));
+    base = __shfl_sync(0xffffffffu, base, __ffs(bal) - 1);
+    if (!flag) return true;
+    const int64_t pos = (int64_t)base + __popc(bal & ((1u << lane) - 1u));
+    if (pos >= a.flag_cap) return false;
+    a.flag_list[pos] = ((int64_t)si << 40) | i;
+    return true;
+}
+
 // Candidates for each segment's FP64 maximum: the samples whose upper bound
 // reaches the largest lower bound (the true maximum lies among them), plus
 // samples without a usable bound.  Lean scan; marks bits in amb_words.
@@ -95,6 +152,8 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_candidates_kernel(AcceptAr
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t wbase = blk * ACC_BLOCK + (int64_t)warp * 1024;
     const double lb = key_to_double(a.bound_key[2 * sg.max_slot + 1]);
+    float lbf;
+    const bool fast = dbl_to_float_trunc(lb, lbf);
     uint32_t my_word = 0;
     for (int k = 0; k < 32; ++k) {
         const int64_t i = wbase + (int64_t)k * 32 + lane;
@@ -102,12 +161,59 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_candidates_kernel(AcceptAr
         if (i < sg.n) {
             const double v = a.lnl[sg.lnl_off + i];
             const float er = a.err[sg.lnl_off + i];
-            cand = (v + (double)er >= lb) || !(er < 1e29f) || !(v == v);
+            float vf;
+            if (fast && er < 1e29f && dbl_to_float_trunc(v, vf) &&
+                vf + er + (1e-6f + 5e-7f * (fabsf(vf) + fabsf(lbf) + er)) < lbf) {
+                cand = false;                        // certainly below the largest lower bound
+            } else {
+                cand = (v + (double)er >= lb) || !(er < 1e29f) || !(v == v);
+            }
         }
-        const uint32_t bal = __ballot_sync(0xffffffffu, cand);
+        const bool fit = flag_append(a, 0, cand, si, i);
+        const uint32_t bal = __ballot_sync(0xffffffffu, !fit);
         if (lane == k) my_word = bal;
     }
     a.amb_words[gblk * ACC_THREADS + threadIdx.x] = my_word;
+    }
+}
+
+// FP64 re-evaluation of the listed samples, one warp per sample (lanes over
+// epochs).  MODE 0 raises the FP64 maximum; MODE 1 decides the undecided
+// samples against it and their own uniforms.
+template <int MODE>
+__global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int64_t n = min((int64_t)a.flag_count[MODE], a.flag_cap);
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t e = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); e < n;
+         e += nw) {
+        const int64_t ent = a.flag_list[e];
+        const int si = (int)(ent >> 40);
+        const int64_t i = ent & (((int64_t)1 << 40) - 1);
+        const joker_accept_seg sg = a.segs[si];
+        const int64_t r = sg.row0 + i;
+        const double v = fp64_lnl_warp(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
+                                       a.OM[r], a.M0[r], a.S[r]);
+        if (lane != 0) continue;
+        if (a.n_refined) atomicAdd(a.n_refined, 1ull);
+        if (MODE == 0) {
+            atomicMax(a.exact_key + sg.max_slot, double_to_key(v));
+        } else {
+            const double mx = key_to_double(a.exact_key[sg.max_slot]);
+            double u;
+            if (a.u_source == JOKER_U_PCG64) {
+                const u128 s0 = ((u128)sg.pcg_state_hi << 64) | (u128)sg.pcg_state_lo;
+                const u128 inc = ((u128)sg.pcg_inc_hi << 64) | (u128)sg.pcg_inc_lo;
+                u = pcg_uniform(pcg_output(pcg_advance(s0, inc, (uint64_t)i + 1)));
+            } else {
+                u = a.u[sg.u_off + i];
+            }
+            if (accept_test(v - mx, u)) {
+                const int64_t gblk = seg_base(a, si) + i / ACC_BLOCK;
+                atomicOr(a.words + gblk * ACC_THREADS + (i % ACC_BLOCK) / 32, 1u << (i & 31));
+                atomicAdd((unsigned long long *)(a.blk_count + gblk), 1ull);
+            }
+        }
     }
 }
 
@@ -202,26 +308,48 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
         Am = cm;
         Cp = cp;
     }
+    float mxf;
+    const bool fast = dbl_to_float_trunc(mx, mxf);
     uint32_t my_word = 0, my_amb = 0;
     int my_count = 0;
     for (int k = 0; k < 32; ++k) {
         const int64_t i = wbase + (int64_t)k * 32 + lane;
         bool keep = false, amb = false;
         if (i < sg.n) {
-            double u;
-            if (a.u_source == JOKER_U_PCG64) u = pcg_uniform(pcg_output(st));
-            else u = a.u[sg.u_off + i];
-            if (!refine) {
-                keep = accept_test(lnl[i] - mx, u);
+            // the uniform: its 53-bit integer (PCG64) or the array's double
+            uint64_t m = 0;
+            double ua = 0.0;
+            float uf = 0.0f;
+            bool uf_ok;
+            if (a.u_source == JOKER_U_PCG64) {
+                m = pcg_output(st) >> 11;
+                uf_ok = m != 0;
+                if (uf_ok) uf = u53_to_float(m);
             } else {
-                const int dec = interval_test(lnl[i], a.err[sg.lnl_off + i], mx, u);
-                keep = dec == 1;
-                amb = dec < 0;
+                ua = a.u[sg.u_off + i];
+                uf_ok = dbl_to_float_trunc(ua, uf);
             }
+            const double v = lnl[i];
+            const float er = refine ? a.err[sg.lnl_off + i] : 0.0f;
+            float vf;
+            int dec = 2;
+            if (fast && uf_ok && er < 1e29f && dbl_to_float_trunc(v, vf))
+                dec = fast_decide(vf, er, mxf, uf);
+            if (dec == 2) {
+                const double u = a.u_source == JOKER_U_PCG64 ? (double)m * 0x1.0p-53 : ua;
+                if (!refine) {
+                    dec = accept_test(v - mx, u) ? 1 : 0;
+                } else {
+                    dec = interval_test(v, er, mx, u);
+                }
+            }
+            keep = dec == 1;
+            amb = dec < 0;
         }
         if (a.u_source == JOKER_U_PCG64) st = Am * st + Cp;
         const uint32_t bal = __ballot_sync(0xffffffffu, keep);
-        const uint32_t abal = __ballot_sync(0xffffffffu, amb);
+        const bool fit = !refine || flag_append(a, 1, amb, si, i);
+        const uint32_t abal = __ballot_sync(0xffffffffu, !fit);
         if (lane == k) {
             my_word = bal;
             my_amb = abal;
@@ -314,6 +442,13 @@ int64_t accept_blocks(const joker_accept_seg *segs, int n_segs, int64_t *blk_bas
 
 static cudaError_t launch_fp64_words(int mode, const AcceptArgs &a, int64_t total_blocks,
                                      cudaStream_t st) {
+    // the compacted list first (one warp per sample), then the words of the
+    // samples that did not fit in it (almost always none)
+    const unsigned lgrid = 152 * 4;
+    if (mode == 0) accept_fp64_list_kernel<0><<<lgrid, 256, 0, st>>>(a);
+    else accept_fp64_list_kernel<1><<<lgrid, 256, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     const int64_t n_words = total_blocks * ACC_THREADS;
     const int64_t threads = (n_words + WORDS_PER_THREAD - 1) / WORDS_PER_THREAD;
     const unsigned grid = (unsigned)((threads + 127) / 128);
@@ -324,8 +459,10 @@ static cudaError_t launch_fp64_words(int mode, const AcceptArgs &a, int64_t tota
 
 cudaError_t launch_refine_max(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st) {
     if (total_blocks <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(a.flag_count, 0, 2 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
     accept_candidates_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_fp64_words(0, a, total_blocks, st);
 }
@@ -337,8 +474,12 @@ cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_
         if (e != cudaSuccess) return e;
     }
     if (total_blocks > 0) {
+        cudaError_t e;
+        if (a.err != nullptr &&
+            (e = cudaMemsetAsync(a.flag_count + 1, 0, sizeof(unsigned long long), st)) != cudaSuccess)
+            return e;
         accept_mark_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
-        cudaError_t e = cudaGetLastError();
+        e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         if (a.err != nullptr) {
             e = launch_fp64_words(1, a, total_blocks, st);

@@ -87,6 +87,31 @@ struct Acc64 {
         }
     }
 
+    // Sum the epoch sums of the 32 lanes of a warp (every lane gets the total).
+    __device__ __forceinline__ void warp_sum() {
+        if (!JIT) {
+            A00 = wsum(A00);
+            b0 = wsum(b0);
+#pragma unroll
+            for (int k = 1; k < L; ++k) A0[k] = wsum(A0[k]);
+        } else {
+            rWr = wsum(rWr);
+            slw = wsum(slw);
+#pragma unroll
+            for (int ii = 0; ii < L; ++ii) {
+                q[ii] = wsum(q[ii]);
+#pragma unroll
+                for (int k = 0; k <= ii; ++k) G[ii][k] = wsum(G[ii][k]);
+            }
+        }
+    }
+
+    static __device__ __forceinline__ double wsum(double x) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        return x;
+    }
+
     __device__ __forceinline__ double finish(const StarRec &st, double P) const;
 };
 
@@ -185,6 +210,47 @@ __device__ __noinline__ double fp64_lnl_global(const StarRec &st, const double *
         acc.add(__ldg(rec), __ldg(rec + 1), __ldg(rec + 2), T);
     }
     return acc.finish(st, P);
+}
+
+// FP64 ln L of one sample evaluated by a whole warp: lane l takes epochs l,
+// l + 32, ...; the sums are combined across the warp.  All 32 lanes must call
+// it with the same sample; all return the value.  Same arithmetic per epoch
+// as fp64_lnl_global, summed in a different order (agreement to FP64
+// rounding of the sums).
+template <int L, bool JIT>
+__device__ __noinline__ double fp64_lnl_warp_t(const StarRec &st, const double *ep64, double P,
+                                               double e, double om, double M0, double s) {
+    Acc64<L, JIT> acc;
+    acc.init(st, P, e, om, M0, s);
+    const double *rec0 = ep64 + (size_t)st.epoch_off * REC64;
+    for (int i = threadIdx.x & 31; i < st.n_epochs; i += 32) {
+        const double *rec = rec0 + (size_t)i * REC64;
+        double T[MAXL];
+#pragma unroll
+        for (int k = 1; k < L; ++k) T[k - 1] = __ldg(rec + 2 + k);
+        acc.add(__ldg(rec), __ldg(rec + 1), __ldg(rec + 2), T);
+    }
+    acc.warp_sum();
+    return acc.finish(st, P);
+}
+
+__device__ __forceinline__ double fp64_lnl_warp(int L, bool jit, const StarRec &st,
+                                                const double *ep64, double P, double e,
+                                                double om, double M0, double s) {
+    switch (L) {
+        case 1: return jit ? fp64_lnl_warp_t<1, true>(st, ep64, P, e, om, M0, s)
+                           : fp64_lnl_warp_t<1, false>(st, ep64, P, e, om, M0, s);
+        case 2: return jit ? fp64_lnl_warp_t<2, true>(st, ep64, P, e, om, M0, s)
+                           : fp64_lnl_warp_t<2, false>(st, ep64, P, e, om, M0, s);
+        case 3: return jit ? fp64_lnl_warp_t<3, true>(st, ep64, P, e, om, M0, s)
+                           : fp64_lnl_warp_t<3, false>(st, ep64, P, e, om, M0, s);
+        case 4: return jit ? fp64_lnl_warp_t<4, true>(st, ep64, P, e, om, M0, s)
+                           : fp64_lnl_warp_t<4, false>(st, ep64, P, e, om, M0, s);
+        case 5: return jit ? fp64_lnl_warp_t<5, true>(st, ep64, P, e, om, M0, s)
+                           : fp64_lnl_warp_t<5, false>(st, ep64, P, e, om, M0, s);
+        default: return jit ? fp64_lnl_warp_t<6, true>(st, ep64, P, e, om, M0, s)
+                            : fp64_lnl_warp_t<6, false>(st, ep64, P, e, om, M0, s);
+    }
 }
 
 __device__ __forceinline__ double fp64_lnl_sample(int L, bool jit, const StarRec &st,

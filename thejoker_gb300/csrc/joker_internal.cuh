@@ -120,6 +120,12 @@ struct AcceptArgs {
     int L, jit;
     unsigned long long *n_refined;          // samples re-evaluated in FP64 (statistics)
     uint32_t *amb_words;                    // undecided samples, one bit each (refinement)
+    // flagged samples (max candidates, then undecided ones) compacted into a
+    // list, (segment << 40) | index; entries past flag_cap fall back to
+    // amb_words.  flag_count[0]: candidates, flag_count[1]: undecided.
+    int64_t *flag_list;
+    unsigned long long *flag_count;
+    int64_t flag_cap;
     const joker_accept_seg *segs;
     const int64_t *blk_base;     // n_segs + 1 prefix of CTA counts
     int64_t fixed_blocks;        // > 0: segment s owns CTA blocks [s * fixed, (s+1) * fixed)

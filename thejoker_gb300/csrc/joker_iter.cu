@@ -264,6 +264,9 @@ struct joker_iter {
     double *out_lnl = nullptr;
     unsigned long long *n_refined = nullptr;
     int *queue = nullptr;
+    unsigned long long *flag_count = nullptr;
+    int64_t *flag_list = nullptr;
+    int64_t flag_cap = 0;
 };
 
 // stars/cache accessors live in joker_abi.cu
@@ -336,7 +339,8 @@ static int iter_alloc(joker_iter **out, const joker_stars *stars, const joker_ca
                  o_amb = take(4 * 256 * (size_t)it->max_blocks),
                  o_bc = take(8 * (size_t)it->max_blocks), o_cnt = take(8 * (size_t)n),
                  o_oidx = take(8 * (size_t)n * max_req), o_olnl = take(8 * (size_t)n * max_req),
-                 o_nref = take(8), o_queue = take(16);
+                 o_nref = take(8), o_queue = take(16),
+                 o_fcount = take(16), o_flags = take(8 * (size_t)(65536 + 64 * it->max_blocks));
     cudaError_t e = cudaMalloc(&it->base, off);
     if (e != cudaSuccess) {
         delete it;
@@ -380,6 +384,9 @@ static int iter_alloc(joker_iter **out, const joker_stars *stars, const joker_ca
     it->out_lnl = (double *)(b + o_olnl);
     it->n_refined = (unsigned long long *)(b + o_nref);
     it->queue = (int *)(b + o_queue);
+    it->flag_count = (unsigned long long *)(b + o_fcount);
+    it->flag_list = (int64_t *)(b + o_flags);
+    it->flag_cap = 65536 + 64 * it->max_blocks;
     // every slot empty; the constant parts of the segments
     std::vector<int64_t> st((size_t)n * ST_FIELDS, 0);
     for (int s = 0; s < n; ++s) st[(size_t)s * ST_FIELDS + ST_DONE] = DONE_EMPTY;
@@ -538,6 +545,9 @@ extern "C" int joker_iter_round(joker_iter *it, void *stream) {
         c.jit = jit;
         c.n_refined = it->n_refined;
         c.amb_words = it->amb;
+        c.flag_list = it->flag_list;
+        c.flag_count = it->flag_count;
+        c.flag_cap = it->flag_cap;
         c.max_key = it->p.exact_key;
     } else {
         c.max_key = it->max_key;
