@@ -10,9 +10,10 @@ synthetic inputs stand in for survey data.
 
 metric: prior samples/s (lnL + accept).  ``value``: mixed-precision path, inputs
 resident in HBM.  ``e2e``: the same through the host-facing call -- the packed
-(S, 5) float64 chunk copied from pinned host memory, prepared, evaluated and
-accepted, accepted indices copied back -- every step.  The plain FP64 GPU path
-is reported beside it (``fp64``) on a 2^25-sample slice of the same workload.
+(S, 5) float64 chunk in pinned host memory, read by the ln L kernel over the
+host link (40 bytes per sample, no staging copy), evaluated and accepted,
+accepted indices copied back -- every step.  The plain FP64 GPU path is
+reported beside it (``fp64``) on a 2^25-sample slice of the same workload.
 
 Multi-GPU (torchrun): each rank evaluates its own 2^28-sample shard of the
 cache for the same star (weak scaling); the per-star maximum is exchanged with

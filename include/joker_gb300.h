@@ -138,6 +138,15 @@ int joker_stars_info(const joker_stars *stars, int *n_stars, int *n_linear,
  * result for such rows is NaN, as the reference's arithmetic would give). */
 int joker_cache_create(joker_cache **out, int64_t capacity);
 int joker_cache_destroy(joker_cache *cache);
+/* A cache over the caller's packed (n, 5) FP64 chunk without a copy: the
+ * FP64 columns alias the chunk and the mixed kernel prepares each sample in
+ * registers (the values equal those of joker_cache_load).  The chunk may be
+ * device memory or pinned host memory (read through its mapped device
+ * address, 40 bytes per sample per ln L call over the host link); it must
+ * outlive the view.  joker_cache_load on a view returns JOKER_EINVAL.
+ * Replaces the staging of batch_marginal_ln_likelihood's chunk
+ * (fast_likelihood.pyx:428-451) for callers that keep it pinned. */
+int joker_cache_create_view(joker_cache **out, const double *chunk, int64_t n);
 int joker_cache_load(joker_cache *cache, const double *d_chunk, int64_t n,
                      int64_t row0, void *stream);
 int64_t joker_cache_capacity(const joker_cache *cache);

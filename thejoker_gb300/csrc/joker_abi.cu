@@ -59,6 +59,8 @@ struct joker_stars {
 struct joker_cache {
     int64_t cap = 0;
     double *P = nullptr, *E = nullptr, *OM = nullptr, *M0 = nullptr, *S = nullptr;
+    int64_t stride = 1;          // 5 for a view over a packed chunk
+    bool view = false;           // FP64 columns alias the caller's chunk; no prepared form
     float4 *mx_a = nullptr, *mx_b = nullptr;
     float *mx_s2 = nullptr;
 };
@@ -429,7 +431,9 @@ extern "C" int joker_cache_create(joker_cache **out, int64_t capacity) {
 
 extern "C" int joker_cache_destroy(joker_cache *c) {
     if (!c) return JOKER_OK;
-    cudaFree(c->P); cudaFree(c->E); cudaFree(c->OM); cudaFree(c->M0); cudaFree(c->S);
+    if (!c->view) {
+        cudaFree(c->P); cudaFree(c->E); cudaFree(c->OM); cudaFree(c->M0); cudaFree(c->S);
+    }
     cudaFree(c->mx_a); cudaFree(c->mx_b); cudaFree(c->mx_s2);
     delete c;
     return JOKER_OK;
@@ -437,9 +441,49 @@ extern "C" int joker_cache_destroy(joker_cache *c) {
 
 extern "C" int64_t joker_cache_capacity(const joker_cache *c) { return c ? c->cap : -1; }
 
+// A cache over the caller's packed (n, 5) FP64 chunk, without a copy: the
+// FP64 columns alias it (stride 5) and the mixed kernel prepares each sample
+// in registers.  The chunk may be device memory, or pinned host memory that
+// the device reads through its mapped address (every ln L call then streams
+// 40 bytes per sample over the host link).  Pageable host memory is taken
+// only where the device can address it (cudaDevAttrPageableMemoryAccess).
+extern "C" int joker_cache_create_view(joker_cache **out, const double *chunk, int64_t n) {
+    if (!out) return fail(JOKER_EINVAL, "joker_cache_create_view: out is NULL");
+    *out = nullptr;
+    if (!chunk || n <= 0) return fail(JOKER_EINVAL, "joker_cache_create_view: empty chunk");
+    if (((uintptr_t)chunk) % 8) return fail(JOKER_EINVAL, "joker_cache_create_view: chunk not 8-byte aligned");
+    cudaPointerAttributes at;
+    CUDA_TRY(cudaPointerGetAttributes(&at, chunk));
+    const double *dptr = nullptr;
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+        dptr = chunk;
+    } else if (at.type == cudaMemoryTypeHost) {
+        void *d = nullptr;
+        CUDA_TRY(cudaHostGetDevicePointer(&d, const_cast<double *>(chunk), 0));
+        dptr = (const double *)d;
+    } else {
+        int dev = 0, pageable = 0;
+        CUDA_TRY(cudaGetDevice(&dev));
+        CUDA_TRY(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+        if (!pageable)
+            return fail(JOKER_EINVAL, "joker_cache_create_view: host memory must be pinned "
+                                      "(cudaHostAlloc / cudaHostRegister) on this system");
+        dptr = chunk;
+    }
+    joker_cache *c = new joker_cache();
+    c->cap = n;
+    c->view = true;
+    c->stride = 5;
+    c->P = const_cast<double *>(dptr);
+    c->E = c->P + 1; c->OM = c->P + 2; c->M0 = c->P + 3; c->S = c->P + 4;
+    *out = c;
+    return JOKER_OK;
+}
+
 extern "C" int joker_cache_load(joker_cache *c, const double *d_chunk, int64_t n, int64_t row0,
                                 void *stream) {
     if (!c || (!d_chunk && n > 0)) return fail(JOKER_EINVAL, "joker_cache_load: NULL argument");
+    if (c->view) return fail(JOKER_EINVAL, "joker_cache_load: a cache view holds no storage");
     if (n < 0 || row0 < 0 || row0 + n > c->cap)
         return fail(JOKER_ERANGE, "joker_cache_load: rows [%lld, %lld) exceed capacity %lld",
                     (long long)row0, (long long)(row0 + n), (long long)c->cap);
@@ -503,10 +547,11 @@ void stars_internals(const joker_stars *s, const StarRec **recs, const double **
 }
 
 void cache_internals(const joker_cache *c, int64_t *cap, const double **P, const double **E,
-                     const double **OM, const double **M0, const double **S,
+                     const double **OM, const double **M0, const double **S, int64_t *stride,
                      const float4 **mx_a, const float4 **mx_b, const float **mx_s2) {
     *cap = c->cap;
     *P = c->P; *E = c->E; *OM = c->OM; *M0 = c->M0; *S = c->S;
+    *stride = c->stride;
     *mx_a = c->mx_a; *mx_b = c->mx_b; *mx_s2 = c->mx_s2;
 }
 }  // namespace joker
@@ -549,7 +594,7 @@ extern "C" int joker_lnl(const joker_stars *s, const joker_cache *c, int star0, 
     a.ep64 = s->d_ep64;
     a.ep32 = s->d_ep32;
     a.P = c->P; a.e = c->E; a.om = c->OM; a.M0 = c->M0; a.s = c->S;
-    a.stride = 1;
+    a.stride = c->stride;
     a.mx_a = c->mx_a; a.mx_b = c->mx_b; a.mx_s2 = c->mx_s2;
     a.queue = s->d_queue;
     a.lnl = d_lnl;
@@ -689,6 +734,7 @@ static int refined_setup(const joker_stars *s, const joker_cache *c, const joker
     a.stars = s->d_stars;
     a.ep64 = s->d_ep64;
     a.P = c->P; a.E = c->E; a.OM = c->OM; a.M0 = c->M0; a.S = c->S;
+    a.stride = c->stride;
     a.L = s->L;
     a.jit = s->jitter == JOKER_JITTER_APPLIED;
     a.n_refined = (unsigned long long *)d_n_refined;

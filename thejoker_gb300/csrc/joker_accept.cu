@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
         const int si = (int)(ent >> 40);
         const int64_t i = ent & (((int64_t)1 << 40) - 1);
         const joker_accept_seg sg = a.segs[si];
-        const int64_t r = sg.row0 + i;
+        const int64_t r = (sg.row0 + i) * a.stride;
         const double v = fp64_lnl_warp(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
                                        a.OM[r], a.M0[r], a.S[r]);
         if (lane != 0) continue;
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
             bits &= bits - 1;
             const int64_t i = first + b;
             if (i >= sg.n) continue;
-            const int64_t r = sg.row0 + i;
+            const int64_t r = (sg.row0 + i) * a.stride;
             const double v = fp64_lnl_sample(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
                                              a.OM[r], a.M0[r], a.S[r]);
             if (a.n_refined) atomicAdd(a.n_refined, 1ull);

@@ -185,15 +185,18 @@ __device__ __forceinline__ double k_prior_variance(const StarRec &st, double P, 
 template <int L, bool JIT>
 __device__ __forceinline__ double Acc64<L, JIT>::finish(const StarRec &st, double P) const {
     const double lam0 = k_prior_variance(st, P, e);
-    if (!JIT) return tail_schur_d<L, false>(st, A00, A0, b0, lam0, log(lam0));
-    double Gs[L][L];
+    if constexpr (!JIT) {
+        return tail_schur_d<L, false>(st, A00, A0, b0, lam0, log(lam0));
+    } else {
+        double Gs[L][L];
 #pragma unroll
-    for (int ii = 0; ii < L; ++ii) {
+        for (int ii = 0; ii < L; ++ii) {
 #pragma unroll
-        for (int k = 0; k <= ii; ++k) { Gs[ii][k] = G[ii][k]; Gs[k][ii] = G[ii][k]; }
-        Gs[ii][ii] += 1.0 / (ii == 0 ? lam0 : st.lam[ii]);
+            for (int k = 0; k <= ii; ++k) { Gs[ii][k] = G[ii][k]; Gs[k][ii] = G[ii][k]; }
+            Gs[ii][ii] += 1.0 / (ii == 0 ? lam0 : st.lam[ii]);
+        }
+        return tail_full_d<L, false>(Gs, q, rWr, st.log_norm_rest + log(lam0) - slw);
     }
-    return tail_full_d<L, false>(Gs, q, rWr, st.log_norm_rest + log(lam0) - slw);
 }
 
 // FP64 ln L of one sample with the star's epochs read from global memory.

@@ -117,6 +117,7 @@ struct AcceptArgs {
     const StarRec *stars;
     const double *ep64;
     const double *P, *E, *OM, *M0, *S;
+    int64_t stride;                         // doubles between consecutive samples (1 or 5)
     int L, jit;
     unsigned long long *n_refined;          // samples re-evaluated in FP64 (statistics)
     uint32_t *amb_words;                    // undecided samples, one bit each (refinement)

@@ -274,7 +274,7 @@ namespace joker {
 void stars_internals(const joker_stars *s, const StarRec **recs, const double **ep64,
                      const float **ep32, int *n_stars, int *L, int *jit, int **queue);
 void cache_internals(const joker_cache *c, int64_t *cap, const double **P, const double **E,
-                     const double **OM, const double **M0, const double **S,
+                     const double **OM, const double **M0, const double **S, int64_t *stride,
                      const float4 **mx_a, const float4 **mx_b, const float **mx_s2);
 }  // namespace joker
 
@@ -298,8 +298,8 @@ static int iter_alloc(joker_iter **out, const joker_stars *stars, const joker_ca
     *out = nullptr;
     const StarRec *recs; const double *ep64; const float *ep32; int n_stars, L, jit; int *queue;
     stars_internals(stars, &recs, &ep64, &ep32, &n_stars, &L, &jit, &queue);
-    int64_t cap; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
-    cache_internals(cache, &cap, &P, &E, &OM, &M0, &S, &ma, &mb, &ms);
+    int64_t cap, cstride; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
+    cache_internals(cache, &cap, &P, &E, &OM, &M0, &S, &cstride, &ma, &mb, &ms);
     if (lib_row0 < 0 || lib_row0 >= cap || pool_samples <= 0 || max_req <= 0 || maxiter <= 0 ||
         !(safety_factor > 0)) {
         snprintf(buf, sizeof buf, "%s: bad library, pool or schedule parameters", who);
@@ -415,8 +415,8 @@ extern "C" int joker_iter_admit(joker_iter *it, int slot, int64_t budget, int n_
     if (!it || !pcg_state) return iter_fail(JOKER_EINVAL, "joker_iter_admit: NULL argument");
     if (slot < 0 || slot >= it->p.n_stars)
         return iter_fail(JOKER_EINVAL, "joker_iter_admit: slot out of range");
-    int64_t cap; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
-    cache_internals(it->cache, &cap, &P, &E, &OM, &M0, &S, &ma, &mb, &ms);
+    int64_t cap, cstride; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
+    cache_internals(it->cache, &cap, &P, &E, &OM, &M0, &S, &cstride, &ma, &mb, &ms);
     if (budget <= 0 || it->p.lib_row0 + budget > cap)
         return iter_fail(JOKER_ERANGE, "joker_iter_admit: budget outside the cache");
     if (n_requested <= 0 || n_requested > it->p.max_req)
@@ -454,8 +454,8 @@ extern "C" int joker_iter_create(joker_iter **out, const joker_stars *stars,
         const StarRec *r; const double *a; const float *b; int L, jit; int *q;
         stars_internals(stars, &r, &a, &b, &n_stars, &L, &jit, &q);
     }
-    int64_t cap; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
-    cache_internals(cache, &cap, &P, &E, &OM, &M0, &S, &ma, &mb, &ms);
+    int64_t cap, cstride; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
+    cache_internals(cache, &cap, &P, &E, &OM, &M0, &S, &cstride, &ma, &mb, &ms);
     if (lib_row0 < 0 || lib_size <= 0 || lib_row0 + lib_size > cap)
         return iter_fail(JOKER_ERANGE, "joker_iter_create: library rows outside the cache");
     if (n_requested <= 0 || init_batch <= 0)
@@ -509,12 +509,12 @@ extern "C" int joker_iter_round(joker_iter *it, void *stream) {
     // ln L over the planned items
     const StarRec *recs; const double *ep64; const float *ep32; int n_stars, L, jit; int *queue;
     stars_internals(it->stars, &recs, &ep64, &ep32, &n_stars, &L, &jit, &queue);
-    int64_t cap; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
-    cache_internals(it->cache, &cap, &P, &E, &OM, &M0, &S, &ma, &mb, &ms);
+    int64_t cap, cstride; const double *P, *E, *OM, *M0, *S; const float4 *ma, *mb; const float *ms;
+    cache_internals(it->cache, &cap, &P, &E, &OM, &M0, &S, &cstride, &ma, &mb, &ms);
     LnlArgs a;
     memset(&a, 0, sizeof a);
     a.stars = recs; a.ep64 = ep64; a.ep32 = ep32;
-    a.P = P; a.e = E; a.om = OM; a.M0 = M0; a.s = S; a.stride = 1;
+    a.P = P; a.e = E; a.om = OM; a.M0 = M0; a.s = S; a.stride = cstride;
     a.mx_a = ma; a.mx_b = mb; a.mx_s2 = ms;
     a.items = it->p.items;
     a.n_items = (int)it->items_cap;
@@ -541,6 +541,7 @@ extern "C" int joker_iter_round(joker_iter *it, void *stream) {
         c.stars = recs;
         c.ep64 = ep64;
         c.P = P; c.E = E; c.OM = OM; c.M0 = M0; c.S = S;
+        c.stride = cstride;
         c.L = L;
         c.jit = jit;
         c.n_refined = it->n_refined;

@@ -239,4 +239,83 @@ __device__ __forceinline__ float ff_log(ff a) {
     return (float)ex * 0.69314718f + logf(m) + a.lo / a.hi;
 }
 
+// ---- per-sample preparation of the mixed path -----------------------------
+// Split a double into an unevaluated float pair: hi = x with its mantissa
+// truncated to 24 bits, lo = the remaining 29 bits rounded to a float, so
+// |hi + lo - x| <= 2^-48 |x|.  Integer operations only (GB300's FP64 and
+// FP64-conversion rate is 1/64 of FP32).  Zero, values outside the float
+// normal range, inf and NaN go through one FP64 conversion with lo = 0.
+__device__ __forceinline__ void split_d2ff(double x, float &hi, float &lo) {
+    const long long b = __double_as_longlong(x);
+    if ((b & 0x7fffffffffffffffLL) == 0) { hi = 0.0f; lo = 0.0f; return; }
+    const int hw = (int)(b >> 32);
+    const int ex = (hw >> 20) & 0x7ff;
+    if (ex < 897 || ex > 1150) { hi = __double2float_rn(x); lo = 0.0f; return; }
+    const unsigned sign = (unsigned)hw & 0x80000000u;
+    hi = __uint_as_float(sign | ((unsigned)(ex - 896) << 23) | ((unsigned)(b >> 29) & 0x7fffffu));
+    const unsigned rem = (unsigned)b & 0x1fffffffu;           // the 29 bits below hi
+    const float scale = ex >= 949 ? __uint_as_float((unsigned)(ex - 948) << 23) : 0.0f;
+    lo = __uint_as_float(sign | __float_as_uint(__uint2float_rn(rem) * scale));
+}
+
+// 1/(2 pi) and 1/pi as float pairs (hi = the float nearest, lo = the rest).
+constexpr float INV_2PI_HI_F = 0x1.45f306p-3f, INV_2PI_LO_F = 0x1.b93910p-28f;
+constexpr float INV_PI_HI_F = 0x1.45f306p-2f, INV_PI_LO_F = 0x1.b93910p-27f;
+
+// Product of a float pair with a constant float pair, as a float pair.
+__device__ __forceinline__ void mul_ff_const(float xh, float xl, float ch, float cl, float &ph,
+                                             float &pl) {
+    ph = __fmul_rn(xh, ch);
+    float pe = __fmaf_rn(xh, ch, -ph);
+    pe = __fmaf_rn(xh, cl, pe);
+    pl = __fmaf_rn(xl, ch, pe);
+}
+
+// The prepared form of one prior sample (P, e, omega, M0, s) read by the
+// mixed kernel:
+//   a = (1/P hi, 1/P lo, M0/2pi mod 1 hi, lo)    float pairs, ~2^-46 relative
+//   b = (e, cos omega, sin omega, log g),  g = P^(-2/3) / (1 - e^2)
+//   s2 = s^2
+// FP32 and integer arithmetic only.  The cache preparation and the kernel
+// that reads packed FP64 rows directly both use it, so they agree bit for bit.
+__device__ __forceinline__ void prepare_sample(double p, double e, double om, double m0, double s,
+                                               float4 &pa, float4 &pb, float &s2) {
+    float ph, pl;
+    split_d2ff(p, ph, pl);
+    // 1/P: the float reciprocal of hi, corrected once with the exact residual
+    const float r0 = __frcp_rn(ph);
+    float t = __fmaf_rn(-ph, r0, 1.0f);
+    t = __fmaf_rn(-pl, r0, t);
+    const float r1 = __fmul_rn(r0, t);
+    const float ip_hi = __fadd_rn(r0, r1);
+    const float ip_lo = __fadd_rn(__fsub_rn(r0, ip_hi), r1);
+    // M0 / 2 pi, reduced to [0, 1) (c - floor(c) is exact)
+    float mh, ml, c, ce;
+    split_d2ff(m0, mh, ml);
+    mul_ff_const(mh, ml, INV_2PI_HI_F, INV_2PI_LO_F, c, ce);
+    c = __fsub_rn(c, floorf(c));
+    float mc_hi, mc_lo;
+    two_sum(c, ce, mc_hi, mc_lo);
+    // omega / pi, reduced to [0, 2), then sin and cos of pi times it
+    float oh, ol, w, we;
+    split_d2ff(om, oh, ol);
+    mul_ff_const(oh, ol, INV_PI_HI_F, INV_PI_LO_F, w, we);
+    w = __fsub_rn(w, 2.0f * floorf(0.5f * w));
+    float sw, cw;
+    sincospif(__fadd_rn(w, we), &sw, &cw);
+    // e and e^2 (to one rounding), log g
+    float eh, el;
+    split_d2ff(e, eh, el);
+    const float ef = __fadd_rn(eh, el);
+    const float e2h = __fmul_rn(eh, eh);
+    const float e2 = __fadd_rn(e2h, __fmaf_rn(eh, eh, -e2h) + 2.0f * eh * el);
+    const float lg = -0.6666667f * logf(__fadd_rn(ph, pl)) - log1pf(-e2);
+    float sh, sl;
+    split_d2ff(s, sh, sl);
+    const float s2h = __fmul_rn(sh, sh);
+    s2 = __fadd_rn(s2h, __fmaf_rn(sh, sh, -s2h) + 2.0f * sh * sl);
+    pa = make_float4(ip_hi, ip_lo, mc_hi, mc_lo);
+    pb = make_float4(ef, cw, sw, lg);
+}
+
 }  // namespace joker

@@ -152,6 +152,31 @@ class PriorCache:
         c = cls(len(chunk))
         return c.load(chunk, 0, stream)
 
+    @classmethod
+    def view(cls, chunk):
+        """A cache over a packed (n, 5) float64 chunk without a copy
+        (joker_cache_create_view): a CUDA tensor, or a pinned CPU tensor that
+        the device reads through its mapped address.  The view keeps a
+        reference to the chunk; loading into it is an error."""
+        if not isinstance(chunk, torch.Tensor):
+            raise TypeError("a cache view takes a torch tensor (CUDA, or pinned CPU)")
+        if chunk.dtype != torch.float64 or chunk.dim() != 2 or chunk.shape[1] != 5 or \
+                not chunk.is_contiguous():
+            raise ValueError("chunk must be a contiguous float64 tensor of shape (n, 5)")
+        if not chunk.is_cuda and not chunk.is_pinned():
+            raise ValueError("a CPU chunk must be pinned (tensor.pin_memory())")
+        torch.cuda.init()
+        self = cls.__new__(cls)
+        h = ctypes.c_void_p()
+        nat.check(nat.lib().joker_cache_create_view(ctypes.byref(h),
+                                                    ctypes.c_void_p(chunk.data_ptr()),
+                                                    int(chunk.shape[0])),
+                  "joker_cache_create_view")
+        self._h = h
+        self.capacity = self.size = int(chunk.shape[0])
+        self._chunk = chunk
+        return self
+
     def close(self):
         if getattr(self, "_h", None) is not None:
             nat.lib().joker_cache_destroy(self._h)

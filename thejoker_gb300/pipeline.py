@@ -1,16 +1,24 @@
-"""Rejection sampling from a prior chunk in host memory, with the copy
-overlapped on the device work.
+"""Rejection sampling from a prior chunk in host memory.
 
 The reference's entry point takes a packed (S, 5) prior chunk on the host
 (``batch_marginal_ln_likelihood(chunk)``, thejoker/src/fast_likelihood.pyx
-:428-469, then the acceptance of likelihood_helpers.py:107-109).  Here the
-chunk streams to the device in slices of ``slice_rows`` rows, double-buffered
-on two CUDA streams:
-- the copy of slice k+1 runs while slice k is prepared (cache layout) and
-  evaluated (ln L of every star);
-- the acceptance pass runs once, after the last slice, because it needs each
-  star's maximum over all samples.
-Only the accepted indices (and the counts) come back to the host.
+:428-469, then the acceptance of likelihood_helpers.py:107-109).  Two ways to
+bring it to the device:
+
+- ``zero_copy`` (default for a pinned chunk): the ln L kernel reads the packed
+  rows directly through the chunk's mapped device address and prepares each
+  sample in registers (a cache view, ``PriorCache.view``).  The host link
+  streams 40 bytes per sample while the kernel computes; there is no staging
+  copy, no preparation pass and no device copy of the chunk.  The FP64
+  re-evaluations of the acceptance pass read the few rows they need the same
+  way.
+- staged: the chunk is copied in slices of ``slice_rows`` rows on a copy
+  stream, double-buffered, while the previous slice is prepared into a device
+  cache and evaluated on a compute stream.
+
+Either way the acceptance pass runs once, after every sample's ln L, because
+it needs each star's maximum over all samples; only the accepted indices (and
+the counts) come back to the host.
 """
 import numpy as np
 import torch
@@ -24,16 +32,19 @@ class HostRejection:
     """Reusable buffers for rejection sampling of ``table``'s stars against
     host prior chunks of up to ``capacity`` rows."""
 
-    def __init__(self, table, capacity, precision="mixed", slice_rows=1 << 24, max_out=256):
+    def __init__(self, table, capacity, precision="mixed", slice_rows=1 << 24, max_out=256,
+                 zero_copy=True):
         self.table = table
         self.precision = precision
         self.capacity = int(capacity)
         self.slice_rows = int(min(slice_rows, capacity))
         self.max_out = int(max_out)
+        self.zero_copy = bool(zero_copy)
         n = table.n_stars
-        self.cache = dev.PriorCache(self.capacity)
-        self.stage = [torch.empty((self.slice_rows, 5), dtype=torch.float64, device="cuda")
-                      for _ in range(2)]
+        self.cache = None if self.zero_copy else dev.PriorCache(self.capacity)
+        self.stage = [] if self.zero_copy else \
+            [torch.empty((self.slice_rows, 5), dtype=torch.float64, device="cuda")
+             for _ in range(2)]
         self.lnl = torch.empty((n, self.capacity), dtype=torch.float64, device="cuda")
         mixed = precision != "fp64"
         self.err = torch.empty((n, self.capacity), dtype=torch.float32, device="cuda") \
@@ -48,25 +59,10 @@ class HostRejection:
         self.freed = [torch.cuda.Event() for _ in range(2)]
         self.host_idx = torch.empty(n * self.max_out, dtype=torch.int64).pin_memory()
         self.host_counts = torch.empty(n, dtype=torch.int64).pin_memory()
+        self.d2h_bytes = 0
 
-    def run(self, host_chunk, pcg_states):
-        """Accepted indices per star for a pinned (S, 5) float64 host tensor.
-
-        ``pcg_states``: per star (state, inc) of its numpy PCG64 generator; the
-        star's uniforms are that generator's first S draws.  Returns (counts,
-        list of index arrays, the first max_out per star in ascending order).
-        """
-        S = host_chunk.shape[0]
-        if S > self.capacity:
-            raise ValueError("chunk larger than the capacity")
-        if not host_chunk.is_pinned():
-            host_chunk = host_chunk.pin_memory()
-        cs, ks = self.copy_stream, self.compute_stream
-        ks.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(ks):
-            self.keys.t.zero_()
-            if self.bkeys is not None:
-                self.bkeys.t.zero_()
+    def _staged(self, host_chunk, S, ks):
+        cs = self.copy_stream
         n_slices = (S + self.slice_rows - 1) // self.slice_rows
         for k in range(n_slices):
             a = k * self.slice_rows
@@ -84,6 +80,34 @@ class HostRejection:
                 dev.lnl(self.table, self.cache, self.lnl, precision=self.precision, row0=a,
                         count=b - a, max_keys=self.keys, err=self.err, bound_keys=self.bkeys,
                         out_offset=a, stream=ks)
+        return self.cache
+
+    def run(self, host_chunk, pcg_states):
+        """Accepted indices per star for an (S, 5) float64 host tensor (pinned
+        for the zero-copy path; pinned here otherwise).
+
+        ``pcg_states``: per star (state, inc) of its numpy PCG64 generator; the
+        star's uniforms are that generator's first S draws.  Returns (counts,
+        list of index arrays, the first max_out per star in ascending order).
+        """
+        S = host_chunk.shape[0]
+        if S > self.capacity:
+            raise ValueError("chunk larger than the capacity")
+        if not host_chunk.is_pinned():
+            host_chunk = host_chunk.pin_memory()
+        ks = self.compute_stream
+        ks.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(ks):
+            self.keys.t.zero_()
+            if self.bkeys is not None:
+                self.bkeys.t.zero_()
+        if self.zero_copy:
+            cache = dev.PriorCache.view(host_chunk.contiguous())
+            with torch.cuda.stream(ks):
+                dev.lnl(self.table, cache, self.lnl, precision=self.precision, row0=0, count=S,
+                        max_keys=self.keys, err=self.err, bound_keys=self.bkeys, stream=ks)
+        else:
+            cache = self._staged(host_chunk, S, ks)
         n = self.table.n_stars
         segs = []
         for s in range(n):
@@ -96,7 +120,7 @@ class HostRejection:
                 dev.accept(self.lnl.view(-1), self.keys, segs, out_idx=self.out_idx,
                            counts=self.counts, stream=ks)
             else:
-                dev.accept_refined(self.table, self.cache, self.lnl.view(-1), self.err.view(-1),
+                dev.accept_refined(self.table, cache, self.lnl.view(-1), self.err.view(-1),
                                    self.bkeys, segs, out_idx=self.out_idx, counts=self.counts,
                                    stream=ks)
             self.host_counts.copy_(self.counts, non_blocking=True)
