@@ -38,7 +38,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 N_EPOCHS = 40
-BASELINE_D = 3000.0
+SPAN_D = 3000.0
 SEED_STAR = 2
 SEED_CACHE = 0
 
@@ -47,7 +47,7 @@ SEED_CACHE = 0
 def make_star():
     from thejoker_gb300.linear import rv_unit_columns
     rng = np.random.default_rng(SEED_STAR)
-    t = np.sort(2456000.0 + rng.uniform(0, BASELINE_D, N_EPOCHS))
+    t = np.sort(2456000.0 + rng.uniform(0, SPAN_D, N_EPOCHS))
     err = rng.uniform(0.05, 0.5, N_EPOCHS)
     P = np.exp(rng.uniform(np.log(2), np.log(1024)))
     e = rng.beta(0.867, 3.03)
@@ -84,12 +84,27 @@ def fill_cache_host(out, seed, threads=16):
     return out
 
 
-# Algorithmic work per unit, fixed for the roofline (see DESIGN.md):
+# Algorithmic work per unit, fixed for the roofline:
 # FP32 operations of the mixed kernel per (sample, epoch) with the jitter
 # applied at L = 2, counted from its source (FMA = 2 flops, special-function
 # ops = 1), and per sample for the setup and the FP64 tail.
 FLOPS_PER_EPOCH = 196
 FLOPS_PER_SAMPLE = 60
+# Algorithmic HBM bytes per sample of the cache-form mixed kernel (36 B prepared
+# sample read, 8 B ln L + 4 B bound written) and the DRAM bytes ncu measured per
+# sample (read + write of one 2^24-sample launch / 2^24), scaled to a launch.
+BYTES_PER_SAMPLE = 48
+DRAM_BYTES_PER_SAMPLE = 46.79
+
+
+def _hbm_peak():
+    """Measured copy bandwidth of the GB300 (MEASURED_PEAKS.json), else the
+    6800 GB/s fallback."""
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except Exception:
+        return 6800.0
 
 
 # ------------------------------------------------------------------- clocks
@@ -318,7 +333,7 @@ def run_ours(args, rank, world, dist):
         "vs_baseline": None,
         "dtype": "f32+f64 (mixed)",
         "data": "synthetic (seeded; prior cache and star drawn with numpy)",
-        "config": {"workload": f"1 star x {N_EPOCHS} epochs over {BASELINE_D:.0f} d, jitter "
+        "config": {"workload": f"1 star x {N_EPOCHS} epochs over {SPAN_D:.0f} d, jitter "
                                f"applied, prior cache 2^{int(math.log2(S))} samples per GPU",
                    "prior_samples_per_gpu": S, "n_epochs": N_EPOCHS, "n_linear": 2,
                    "l2": "inputs larger than L2 (cache 76 B/sample resident, 2^28 samples)",
@@ -332,10 +347,17 @@ def run_ours(args, rank, world, dist):
         "accepted_per_step": n_acc,
         "gpu_launches": 6 * args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": args.traffic,
+                     "frac": achieved / peak,
+                     "traffic": args.traffic if args.traffic else DRAM_BYTES_PER_SAMPLE * S,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                       "2^24-sample launch, scaled by samples",
+                     "hbm": {"achieved_gbs": BYTES_PER_SAMPLE * S / (kern_ms * 1e-3) / 1e9,
+                             "peak_gbs": _hbm_peak(),
+                             "frac": BYTES_PER_SAMPLE * S / (kern_ms * 1e-3) / 1e9 / _hbm_peak(),
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
                      "kernel": "lnl_mixed_kernel<2,true,false>",
                      "kernel_ms": kern_ms,
-                     "peak_source": "FP32 FMA throughput measured on this pool's GB300 "
+                     "peak_source": "FP32 FMA throughput measured on a GB300 "
                                     "(FMA-chain microkernel, 67.6 TFLOP/s)",
                      "flops_per_launch": flops},
         "clocks": clk.summary(),
@@ -653,7 +675,7 @@ def run_reference(args, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)", "impl": "reference",
-        "config": {"workload": f"1 star x {N_EPOCHS} epochs over {BASELINE_D:.0f} d, jitter in "
+        "config": {"workload": f"1 star x {N_EPOCHS} epochs over {SPAN_D:.0f} d, jitter in "
                                "the samples (ignored by the reference)",
                    "prior_samples_per_step": args.cpu_samples},
         "cpu_baseline": {"value": v, "unit": "samples/s", "cores": cores, "kind": kind,

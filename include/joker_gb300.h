@@ -269,6 +269,33 @@ int joker_iter_set_round_budget(joker_iter *it, int64_t samples);
 int joker_iter_read(const joker_iter *it, int64_t *h_state, int64_t *h_idx, double *h_lnl,
                     int *h_done, uint64_t *h_n_refined);
 
+/* ---- after acceptance ----------------------------------------------------
+ * joker_linear_posterior: for the n cache rows d_rows[i] (device array) of
+ * star `star`, the Gaussian posterior of the linear parameters (K, v0,
+ * offsets, trend terms; the CJokerHelper order) -- mean d_a[i*L + k] and
+ * covariance d_A[i*L*L + k*L + j] = (Ainv^-1)[k][j] -- and ln L of the sample
+ * (d_lnl, may be NULL; +inf where Ainv is not positive definite, with NaN a
+ * and A), in FP64.  These are the a and inv(Ainv) that
+ * CJokerHelper.batch_get_posterior_samples passes to rng.multivariate_normal
+ * (fast_likelihood.pyx:394-423, :519-530).  k_clip = 0 uses the scaled K
+ * prior variance without the max_K clip, as batch_get_posterior_samples does
+ * (:519-521); 1 clips it as batch_marginal_ln_likelihood does.  Jitter per the
+ * star table's jitter_mode.
+ *
+ * joker_unmarginalized_lnl: ln of the unmarginalized likelihood of n full
+ * samples (JokerSamples.ln_unmarginalized_likelihood, samples.py:611-632):
+ * sum over the star's epochs of ln N(y | K m(t) + sum_k v_k (t - t_ref')^k,
+ * sigma^2 + s^2).  d_pars: n x (6 + n_trend) row-major FP64 rows
+ * P, e, omega, M0, s, K, v_0 .. v_{n_trend-1} (internal units);
+ * dt_shift = t_ref' - t_ref of the star's data (days), t_ref' being the
+ * samples' reference time.  Offsets are not part of the model, as in the
+ * reference's JokerSamples.get_orbit. */
+int joker_linear_posterior(const joker_stars *stars, const joker_cache *cache, int star,
+                           const int64_t *d_rows, int64_t n, int k_clip, double *d_a,
+                           double *d_A, double *d_lnl, void *stream);
+int joker_unmarginalized_lnl(const joker_stars *stars, int star, const double *d_pars, int64_t n,
+                             int n_trend, double dt_shift, double *d_out, void *stream);
+
 /* ---- acceptance without allocation ---------------------------------------
  * No counterpart in the reference.  joker_accept_noalloc is joker_accept for
  * callers that must not allocate device memory: a serving loop with

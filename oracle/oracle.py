@@ -9,6 +9,7 @@
 * ``accept_mask``: the acceptance rule of likelihood_helpers.py:107-109 /
   multiproc_helpers.py:256-258, ``exp(lls - lls.max()) > uu``.
 * ``rv_unit``: the unit-K Kepler RV column (kepler.c).
+* ``posterior_linear_samples``: batch_get_posterior_samples restated in NumPy.
 """
 import ctypes
 import os
@@ -128,3 +129,33 @@ def accept_mask(lls, uu):
     """``np.exp(lls - lls.max()) > uu`` exactly as the reference evaluates it."""
     lls = np.asarray(lls, dtype=np.float64)
     return np.exp(lls - lls.max()) > uu
+
+
+def posterior_linear_samples(chunk, n_per, rng, t, rv, ivar, t_ref, trend_M, mu, lam, k_prior):
+    """CJokerHelper.batch_get_posterior_samples (fast_likelihood.pyx:471-545)
+    restated: per sample a = Ainv^-1 (M C^-1 y + Lambda^-1 mu), A = Ainv^-1 with
+    Ainv = Lambda^-1 + M C^-1 M^T, then rng.multivariate_normal(a, A, size=n_per)
+    in the reference's order.  No jitter and no max_K clip, as there (:516,
+    :519-521).  Returns (samples (S*n, 5+L), a, A)."""
+    chunk = np.asarray(chunk, dtype=np.float64)
+    S = chunk.shape[0]
+    L = len(mu)
+    cols = rv_unit(t, t_ref, chunk)
+    out = np.zeros((S, n_per, 5 + L))
+    a_all = np.zeros((S, L))
+    A_all = np.zeros((S, L, L))
+    lam = np.array(lam, dtype=np.float64)
+    for n in range(S):
+        P, e = chunk[n, 0], chunk[n, 1]
+        if k_prior[0]:
+            lam[0] = k_prior[1] ** 2 / (1 - e ** 2) * (P / k_prior[2]) ** (-2 / 3)
+        M = np.vstack([cols[n][None, :], np.asarray(trend_M).T]) if L > 1 else cols[n][None, :]
+        Ainv = np.diag(1.0 / lam) + (M * ivar) @ M.T
+        rhs = (M * ivar) @ rv + mu / lam
+        a = np.linalg.solve(Ainv, rhs)
+        A = np.linalg.inv(Ainv)
+        draws = rng.multivariate_normal(a, A, size=n_per)
+        out[n, :, :5] = chunk[n]
+        out[n, :, 5:] = draws
+        a_all[n], A_all[n] = a, A
+    return out.reshape(S * n_per, 5 + L), a_all, A_all

@@ -84,7 +84,7 @@ def test_accept_extremes(cuda):
 
 def _reference_rejection(star, chunk, rng, max_post, n_lin, prior):
     """likelihood_helpers.rejection_sample_inmem restated with the oracle."""
-    from thejoker_gb300.linear import posterior_linear_samples
+    from oracle.oracle import posterior_linear_samples
     lls = oracle_lnl(star, chunk)
     uu = rng.uniform(size=len(lls))
     good = np.where(np.exp(lls - lls.max()) > uu)[0][:max_post]

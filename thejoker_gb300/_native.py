@@ -28,7 +28,8 @@ EXPORTED = (
     "joker_key_to_double", "joker_accept_workspace", "joker_accept", "joker_accept_refined",
     "joker_refine_max", "joker_iter_create", "joker_iter_destroy", "joker_iter_round",
     "joker_iter_outputs", "joker_iter_read", "joker_iter_create_pool", "joker_iter_admit",
-    "joker_iter_set_round_budget", "joker_accept_noalloc",
+    "joker_iter_set_round_budget", "joker_accept_noalloc", "joker_linear_posterior",
+    "joker_unmarginalized_lnl",
 )
 
 
@@ -98,6 +99,10 @@ _SIGS = {
                                         ctypes.POINTER(ctypes.c_uint64), _vp]),
     "joker_iter_set_round_budget": (ctypes.c_int, [_vp, _i64]),
     "joker_cache_create_view": (ctypes.c_int, [ctypes.POINTER(_vp), _vp, _i64]),
+    "joker_linear_posterior": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _i64, ctypes.c_int,
+                                              _vp, _vp, _vp, _vp]),
+    "joker_unmarginalized_lnl": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64, ctypes.c_int,
+                                                ctypes.c_double, _vp, _vp]),
     "joker_accept_noalloc": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                             ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

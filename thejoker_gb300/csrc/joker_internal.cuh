@@ -34,6 +34,7 @@ struct alignas(16) StarRec {
     double Cinv[MAXL * MAXL];   // C^-1            (entries 1..L-1)
     // Jitter applied: everything is per sample.
     double lam[MAXL];           // prior variances (lam[0] = lam0)
+    double mu[MAXL];            // prior means (mu[0] = mu0)
     double log_norm_rest;       // N log 2pi + sum_{j>=1} log lambda_j
     double sum_log_ivar;        // sum log ivar
     // float-float copies for the mixed kernel's tail

@@ -381,3 +381,41 @@ def accept(lnl_buf, max_keys, segments, u_source="pcg64", u=None, out_idx=None, 
     if stream is not None:
         work.record_stream(stream)
     return out_idx, out_lnl, counts
+
+
+# ----------------------------------------------------------- after acceptance
+def linear_posterior(table, cache, star, rows=None, k_clip=False, stream=None):
+    """Posterior of the linear parameters of cache rows ``rows`` (an int64
+    CUDA tensor; all rows when None) of one star (joker_linear_posterior):
+    (a (n, L), A (n, L, L), ln L (n)) as CUDA float64 tensors."""
+    if rows is None:
+        rows = torch.arange(cache.size, dtype=torch.int64, device="cuda")
+    rows = rows.to(device="cuda", dtype=torch.int64).contiguous()
+    n = rows.numel()
+    L = table.n_linear
+    a = torch.empty((n, L), dtype=torch.float64, device="cuda")
+    A = torch.empty((n, L, L), dtype=torch.float64, device="cuda")
+    ll = torch.empty(n, dtype=torch.float64, device="cuda")
+    nat.check(nat.lib().joker_linear_posterior(
+        table.handle, cache.handle, int(star), ctypes.c_void_p(rows.data_ptr()), n,
+        int(bool(k_clip)), ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(A.data_ptr()),
+        ctypes.c_void_p(ll.data_ptr()), stream_handle(stream)), "joker_linear_posterior")
+    return a, A, ll
+
+
+def unmarginalized_lnl(table, star, pars, n_trend, dt_shift=0.0, stream=None):
+    """ln of the unmarginalized likelihood of full samples
+    (joker_unmarginalized_lnl); ``pars``: (n, 6 + n_trend) float64 rows
+    P, e, omega, M0, s, K, v_0.. (numpy or CUDA).  Returns a CUDA tensor."""
+    if isinstance(pars, np.ndarray):
+        pars = torch.from_numpy(_f64(pars))
+    pars = pars.to(device="cuda", dtype=torch.float64).contiguous()
+    if pars.dim() != 2 or pars.shape[1] != 6 + int(n_trend):
+        raise ValueError("pars must have shape (n, 6 + n_trend)")
+    n = pars.shape[0]
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    nat.check(nat.lib().joker_unmarginalized_lnl(
+        table.handle, int(star), ctypes.c_void_p(pars.data_ptr()), n, int(n_trend),
+        float(dt_shift), ctypes.c_void_p(out.data_ptr()), stream_handle(stream)),
+        "joker_unmarginalized_lnl")
+    return out

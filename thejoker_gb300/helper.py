@@ -11,7 +11,7 @@ import numpy as np
 import torch
 
 from . import device as dev
-from .linear import posterior_linear_samples
+from .linear import multivariate_normal_draws
 from .samples import PACKED_ORDER
 
 __all__ = ["GPUJokerHelper"]
@@ -103,12 +103,21 @@ class GPUJokerHelper:
 
     # ------------------------------------------------------ linear parameters
     def batch_get_posterior_samples(self, chunk, n_linear_samples_per, rng):
-        """(samples (S*n, n_pars), ll (S*n)) as fast_likelihood.pyx:471-545."""
+        """(samples (S*n, 5 + L), ll (S*n)) as fast_likelihood.pyx:471-545: the
+        posterior mean and covariance of the linear parameters of every row
+        come from the device (joker_linear_posterior, FP64, the K prior
+        variance unclipped as there); the draws use ``rng`` in the
+        reference's order (one multivariate_normal block per row)."""
         chunk = np.ascontiguousarray(chunk, dtype=np.float64)
-        S = chunk.shape[0]
-        ll = np.repeat(self.batch_marginal_ln_likelihood(chunk) if S else np.zeros(0),
-                       n_linear_samples_per)
-        samples, _, _ = posterior_linear_samples(
-            chunk, n_linear_samples_per, rng, self.data._t_bmjd, self.data.rv, self.data.ivar,
-            self.data._t_ref_bmjd, self.trend_M, self.mu, self.lam, self.k_prior)
-        return samples, ll
+        if chunk.ndim != 2 or chunk.shape[1] != 5:
+            raise ValueError("chunk must have shape (n_samples, 5)")
+        S, L, n = chunk.shape[0], self.n_linear, int(n_linear_samples_per)
+        if S == 0:
+            return np.zeros((0, 5 + L)), np.zeros(0)
+        d = torch.from_numpy(chunk).to("cuda")
+        a, A, ll = dev.linear_posterior(self._stars, dev.PriorCache.view(d), 0, k_clip=False)
+        draws = multivariate_normal_draws(rng, a.cpu().numpy(), A.cpu().numpy(), n)
+        samples = np.empty((S, n, 5 + L))
+        samples[:, :, :5] = chunk[:, None, :]
+        samples[:, :, 5:] = draws
+        return samples.reshape(S * n, 5 + L), np.repeat(ll.cpu().numpy(), n)

@@ -1,18 +1,17 @@
-"""Linear-parameter posterior for accepted samples (host, FP64).
+"""Host helpers around the linear parameters.
 
-Restates CJokerHelper.batch_get_posterior_samples
-(thejoker/src/fast_likelihood.pyx:471-545): for each nonlinear sample,
-a = (Lambda^-1 + M C^-1 M^T)^-1 (M C^-1 y + Lambda^-1 mu) and
-A = (Lambda^-1 + M C^-1 M^T)^-1, then
-rng.multivariate_normal(a, A, size=n_linear_samples_per), drawn from the
-caller's generator in the same order as the reference so that the draws match.
-As in the reference, the jitter is not applied here (:516 computes it, nothing
-reads it) and the FixedCompanionMass variance is not clipped at max_K
-(:519-521).  This runs only on the accepted samples; it is not the hot path.
+* ``rv_unit_columns``: the unit-K Kepler RV column in NumPy FP64 (Markley's
+  solver), for building synthetic data sets.
+* ``multivariate_normal_draws``: the draws of
+  CJokerHelper.batch_get_posterior_samples (thejoker/src/fast_likelihood.pyx
+  :529-530), rng.multivariate_normal(a, A, size=n) for each accepted sample in
+  turn, batched over the samples.  They stay on the host so that they come
+  from the caller's numpy generator in the reference's order; the means and
+  covariances come from the device (joker_linear_posterior).
 """
 import numpy as np
 
-__all__ = ["rv_unit_columns", "posterior_linear_samples"]
+__all__ = ["rv_unit_columns", "multivariate_normal_draws"]
 
 
 def _kepler_E(M, e):
@@ -49,27 +48,17 @@ def rv_unit_columns(t, t_ref, P, e, omega, M0):
     return np.cos(omega + f) + e * np.cos(omega)
 
 
-def posterior_linear_samples(chunk, n_per, rng, t, rv, ivar, t_ref, trend_M, mu, lam, k_prior):
-    """Reference-order posterior draws; returns (samples (S*n, 5+L), a, A)."""
-    chunk = np.asarray(chunk, dtype=np.float64)
-    S = chunk.shape[0]
-    L = len(mu)
-    cols = rv_unit_columns(t, t_ref, chunk[:, 0], chunk[:, 1], chunk[:, 2], chunk[:, 3])
-    out = np.zeros((S, n_per, 5 + L))
-    a_all = np.zeros((S, L))
-    A_all = np.zeros((S, L, L))
-    lam = np.array(lam, dtype=np.float64)
-    for n in range(S):
-        P, e = chunk[n, 0], chunk[n, 1]
-        if k_prior[0]:
-            lam[0] = k_prior[1] ** 2 / (1 - e ** 2) * (P / k_prior[2]) ** (-2 / 3)
-        M = np.vstack([cols[n][None, :], np.asarray(trend_M).T]) if L > 1 else cols[n][None, :]
-        Ainv = np.diag(1.0 / lam) + (M * ivar) @ M.T
-        rhs = (M * ivar) @ rv + mu / lam
-        a = np.linalg.solve(Ainv, rhs)
-        A = np.linalg.inv(Ainv)
-        draws = rng.multivariate_normal(a, A, size=n_per)
-        out[n, :, :5] = chunk[n]
-        out[n, :, 5:] = draws
-        a_all[n], A_all[n] = a, A
-    return out.reshape(S * n_per, 5 + L), a_all, A_all
+def multivariate_normal_draws(rng, a, A, n_per):
+    """rng.multivariate_normal(a[i], A[i], size=n_per) for every i in turn,
+    batched: the same standard normals in the same order (one block of
+    n_per * L per sample) and numpy's default SVD factor of each covariance,
+    x = z @ (sqrt(s)[:, None] * vh) + a.  Returns (S, n_per, L)."""
+    a = np.asarray(a, dtype=np.float64)
+    A = np.asarray(A, dtype=np.float64)
+    S, L = a.shape
+    z = rng.standard_normal((S, n_per, L))
+    if S == 0:
+        return z
+    _, sv, vh = np.linalg.svd(A)
+    factor = np.sqrt(sv)[:, :, None] * vh
+    return np.matmul(z, factor) + a[:, None, :]

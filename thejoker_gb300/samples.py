@@ -100,5 +100,33 @@ class JokerSamples:
                 out[k[4:]] = z[k]
         return out
 
+    def ln_unmarginalized_likelihood(self, data):
+        """ln of the unmarginalized likelihood of ``data`` (an RVData) for each
+        sample (samples.py:611-632 of the reference): the sum over epochs of
+        ln N(rv | K m(t) + sum_k v_k (t - t_ref)^k, rv_err^2 + s^2), with the
+        Keplerian and trend of each sample and no offset terms, as the
+        reference's get_orbit builds them.  Evaluated on the GPU
+        (joker_unmarginalized_lnl)."""
+        from . import device as dev
+        n = len(self)
+        if n == 0:
+            return np.zeros(0)
+        nt = self.poly_trend
+        pars = np.zeros((n, 6 + nt))
+        for i, k in enumerate(["P", "e", "omega", "M0"]):
+            pars[:, i] = self[k]
+        if "s" in self:
+            pars[:, 4] = self["s"]
+        pars[:, 5] = self["K"]
+        for j in range(nt):
+            pars[:, 6 + j] = self[f"v{j}"]
+        star = dict(t=data._t_bmjd, rv=data.rv, ivar=data.ivar, t_ref=data._t_ref_bmjd,
+                    trend_M=np.zeros((len(data), 0)), mu=np.zeros(1), lam=np.ones(1),
+                    k_prior=np.zeros(4))
+        table = dev.StarTable([star])
+        t_ref = data._t_ref_bmjd if self.t_ref is None else float(self.t_ref)
+        out = dev.unmarginalized_lnl(table, 0, pars, nt, dt_shift=t_ref - data._t_ref_bmjd)
+        return out.cpu().numpy()
+
     def __repr__(self):
         return f"<JokerSamples [{', '.join(self._cols)}] ({len(self)} samples)>"
