@@ -269,6 +269,31 @@ int joker_iter_set_round_budget(joker_iter *it, int64_t samples);
 int joker_iter_read(const joker_iter *it, int64_t *h_state, int64_t *h_idx, double *h_lnl,
                     int *h_done, uint64_t *h_n_refined);
 
+/* ---- prior samples on the device ------------------------------------------
+ * The producer of the prior cache (JokerPrior.sample, thejoker/prior.py
+ * :297-407; UniformLog and Kipping13Global, thejoker/distributions.py:19-28,
+ * 171-176): n samples of the default prior's nonlinear parameters drawn on
+ * the device into cache rows [row0, row0 + n) (FP64 columns and the mixed
+ * kernel's prepared form), and into d_packed (n x 5, P e omega M0 s) when not
+ * NULL.  Sample g = first_index + i depends only on (seed, g): Philox4x32-10
+ * counters (g, block) under the 64-bit seed.  P ~ log-uniform(P_min, P_max),
+ * e ~ Beta(e_alpha, e_beta), omega and M0 ~ U[0, 2 pi), s fixed or
+ * log-normal.  The draws follow these distributions, not numpy's streams.
+ * JOKER_ERANGE if a gamma rejection loop ran out of tries for some sample
+ * (its e is clamped to [0, 1)); JOKER_EINVAL for a bad spec or a cache view. */
+#define JOKER_S_FIXED 0
+#define JOKER_S_LOGNORMAL 1
+typedef struct {
+    double P_min, P_max;     /* days, 0 < P_min < P_max */
+    double e_alpha, e_beta;  /* Beta shape parameters, > 0 */
+    int32_t s_kind;          /* JOKER_S_FIXED or JOKER_S_LOGNORMAL */
+    int32_t pad;
+    double s_value;          /* JOKER_S_FIXED: s */
+    double s_mu, s_sigma;    /* JOKER_S_LOGNORMAL: ln s ~ N(s_mu, s_sigma) */
+} joker_prior_spec;
+int joker_prior_sample(joker_cache *cache, int64_t row0, int64_t n, const joker_prior_spec *spec,
+                       uint64_t seed, int64_t first_index, double *d_packed, void *stream);
+
 /* ---- after acceptance ----------------------------------------------------
  * joker_linear_posterior: for the n cache rows d_rows[i] (device array) of
  * star `star`, the Gaussian posterior of the linear parameters (K, v0,

@@ -17,6 +17,8 @@ JOKER_JITTER_REFERENCE = 0
 JOKER_JITTER_APPLIED = 1
 JOKER_U_ARRAY = 0
 JOKER_U_PCG64 = 1
+JOKER_S_FIXED = 0
+JOKER_S_LOGNORMAL = 1
 JOKER_MAX_LINEAR = 6
 
 # every extern "C" symbol of include/joker_gb300.h
@@ -29,12 +31,21 @@ EXPORTED = (
     "joker_refine_max", "joker_iter_create", "joker_iter_destroy", "joker_iter_round",
     "joker_iter_outputs", "joker_iter_read", "joker_iter_create_pool", "joker_iter_admit",
     "joker_iter_set_round_budget", "joker_accept_noalloc", "joker_linear_posterior",
-    "joker_unmarginalized_lnl",
+    "joker_unmarginalized_lnl", "joker_prior_sample",
 )
 
 
 class JokerError(RuntimeError):
     """A libjoker_gb300 call returned a non-zero status."""
+
+
+class PriorSpec(ctypes.Structure):
+    """joker_prior_spec (include/joker_gb300.h)."""
+    _fields_ = [("P_min", ctypes.c_double), ("P_max", ctypes.c_double),
+                ("e_alpha", ctypes.c_double), ("e_beta", ctypes.c_double),
+                ("s_kind", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("s_value", ctypes.c_double), ("s_mu", ctypes.c_double),
+                ("s_sigma", ctypes.c_double)]
 
 
 class AcceptSeg(ctypes.Structure):
@@ -99,6 +110,8 @@ _SIGS = {
                                         ctypes.POINTER(ctypes.c_uint64), _vp]),
     "joker_iter_set_round_budget": (ctypes.c_int, [_vp, _i64]),
     "joker_cache_create_view": (ctypes.c_int, [ctypes.POINTER(_vp), _vp, _i64]),
+    "joker_prior_sample": (ctypes.c_int, [_vp, _i64, _i64, ctypes.POINTER(PriorSpec), ctypes.c_uint64,
+                                          _i64, _vp, _vp]),
     "joker_linear_posterior": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _i64, ctypes.c_int,
                                               _vp, _vp, _vp, _vp]),
     "joker_unmarginalized_lnl": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64, ctypes.c_int,

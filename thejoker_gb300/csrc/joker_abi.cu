@@ -63,6 +63,7 @@ struct joker_cache {
     bool view = false;           // FP64 columns alias the caller's chunk; no prepared form
     float4 *mx_a = nullptr, *mx_b = nullptr;
     float *mx_s2 = nullptr;
+    int *flag = nullptr;         // device word for joker_prior_sample's status
 };
 
 namespace joker {
@@ -421,7 +422,8 @@ extern "C" int joker_cache_create(joker_cache **out, int64_t capacity) {
         (e = cudaMalloc(&c->S, 8 * n)) != cudaSuccess ||
         (e = cudaMalloc(&c->mx_a, 16 * n)) != cudaSuccess ||
         (e = cudaMalloc(&c->mx_b, 16 * n)) != cudaSuccess ||
-        (e = cudaMalloc(&c->mx_s2, 4 * n)) != cudaSuccess) {
+        (e = cudaMalloc(&c->mx_s2, 4 * n)) != cudaSuccess ||
+        (e = cudaMalloc(&c->flag, sizeof(int))) != cudaSuccess) {
         joker_cache_destroy(c);
         return fail(JOKER_ENOMEM, "joker_cache_create(%lld): %s", (long long)capacity,
                     cudaGetErrorString(e));
@@ -435,12 +437,55 @@ extern "C" int joker_cache_destroy(joker_cache *c) {
     if (!c->view) {
         cudaFree(c->P); cudaFree(c->E); cudaFree(c->OM); cudaFree(c->M0); cudaFree(c->S);
     }
-    cudaFree(c->mx_a); cudaFree(c->mx_b); cudaFree(c->mx_s2);
+    cudaFree(c->mx_a); cudaFree(c->mx_b); cudaFree(c->mx_s2); cudaFree(c->flag);
     delete c;
     return JOKER_OK;
 }
 
 extern "C" int64_t joker_cache_capacity(const joker_cache *c) { return c ? c->cap : -1; }
+
+namespace joker {
+cudaError_t launch_prior_sample(const joker_prior_spec &spec, uint64_t seed, int64_t first_index,
+                                int64_t n, int64_t row0, double *P, double *E, double *OM,
+                                double *M0, double *S, float4 *mx_a, float4 *mx_b, float *mx_s2,
+                                double *packed, int *bad, cudaStream_t st);
+}  // namespace joker
+
+// Prior samples drawn on the device into cache rows [row0, row0 + n).  Waits
+// for the stream to read the status word.
+extern "C" int joker_prior_sample(joker_cache *c, int64_t row0, int64_t n,
+                                  const joker_prior_spec *spec, uint64_t seed,
+                                  int64_t first_index, double *d_packed, void *stream) {
+    if (!c || !spec) return fail(JOKER_EINVAL, "joker_prior_sample: NULL argument");
+    if (c->view) return fail(JOKER_EINVAL, "joker_prior_sample: a cache view holds no storage");
+    if (n < 0 || row0 < 0 || row0 + n > c->cap || first_index < 0)
+        return fail(JOKER_ERANGE, "joker_prior_sample: rows [%lld, %lld) outside the cache (%lld)",
+                    (long long)row0, (long long)(row0 + n), (long long)c->cap);
+    if (!(spec->P_min > 0.0 && spec->P_max > spec->P_min && std::isfinite(spec->P_max)))
+        return fail(JOKER_EINVAL, "joker_prior_sample: need 0 < P_min < P_max");
+    if (!(spec->e_alpha > 0.0 && spec->e_beta > 0.0 && std::isfinite(spec->e_alpha) &&
+          std::isfinite(spec->e_beta)))
+        return fail(JOKER_EINVAL, "joker_prior_sample: Beta shapes must be > 0");
+    if (spec->s_kind == JOKER_S_FIXED) {
+        if (!std::isfinite(spec->s_value) || spec->s_value < 0.0)
+            return fail(JOKER_EINVAL, "joker_prior_sample: fixed s must be finite and >= 0");
+    } else if (spec->s_kind == JOKER_S_LOGNORMAL) {
+        if (!std::isfinite(spec->s_mu) || !(spec->s_sigma >= 0.0) || !std::isfinite(spec->s_sigma))
+            return fail(JOKER_EINVAL, "joker_prior_sample: bad log-normal s parameters");
+    } else {
+        return fail(JOKER_EINVAL, "joker_prior_sample: unknown s_kind %d", spec->s_kind);
+    }
+    if (n == 0) return JOKER_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    int bad = 0;
+    CUDA_TRY(cudaMemsetAsync(c->flag, 0, sizeof(int), st));
+    CUDA_TRY(launch_prior_sample(*spec, seed, first_index, n, row0, c->P, c->E, c->OM, c->M0, c->S,
+                                 c->mx_a, c->mx_b, c->mx_s2, d_packed, c->flag, st));
+    CUDA_TRY(cudaMemcpyAsync(&bad, c->flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (bad) return fail(JOKER_ERANGE, "joker_prior_sample: %d samples hit the gamma retry limit", bad);
+    return JOKER_OK;
+}
 
 // A cache over the caller's packed (n, 5) FP64 chunk, without a copy: the
 // FP64 columns alias it (stride 5) and the mixed kernel prepares each sample

@@ -152,6 +152,26 @@ class PriorCache:
         c = cls(len(chunk))
         return c.load(chunk, 0, stream)
 
+    def sample_prior(self, prior, n=None, seed=0, row0=0, first_index=0, packed=None,
+                     stream=None):
+        """Draw ``n`` prior samples on the device into rows [row0, row0 + n)
+        (joker_prior_sample).  ``prior``: a JokerPrior with the default
+        nonlinear priors (LogUniform P, Beta e, uniform angles, s Fixed or
+        LogNormal) or a joker_prior_spec field dict.  ``packed``: optional
+        (n, 5) float64 CUDA tensor that also receives the samples."""
+        n = self.capacity - row0 if n is None else int(n)
+        spec = prior_spec(prior)
+        if packed is not None:
+            if packed.dtype != torch.float64 or tuple(packed.shape) != (n, 5) or \
+                    not packed.is_cuda or not packed.is_contiguous():
+                raise ValueError("packed must be a contiguous (n, 5) float64 CUDA tensor")
+        nat.check(nat.lib().joker_prior_sample(
+            self.handle, int(row0), n, ctypes.byref(spec), ctypes.c_uint64(int(seed)),
+            int(first_index), ctypes.c_void_p(packed.data_ptr()) if packed is not None else None,
+            stream_handle(stream)), "joker_prior_sample")
+        self.size = max(self.size, int(row0) + n)
+        return self
+
     @classmethod
     def view(cls, chunk):
         """A cache over a packed (n, 5) float64 chunk without a copy
@@ -419,3 +439,30 @@ def unmarginalized_lnl(table, star, pars, n_trend, dt_shift=0.0, stream=None):
         float(dt_shift), ctypes.c_void_p(out.data_ptr()), stream_handle(stream)),
         "joker_unmarginalized_lnl")
     return out
+
+
+def prior_spec(prior):
+    """joker_prior_spec of a JokerPrior (or of a dict of its fields)."""
+    if isinstance(prior, dict):
+        f = dict(prior)
+        spec = nat.PriorSpec()
+        for k, v in f.items():
+            setattr(spec, k, v)
+        return spec
+    from .prior import Beta, Fixed, LogNormal, LogUniform, UniformAngle
+    pars = prior.pars
+    P, e, om, M0, s = (pars.get(k) for k in ("P", "e", "omega", "M0", "s"))
+    if not (isinstance(P, LogUniform) and isinstance(e, Beta) and
+            isinstance(om, UniformAngle) and isinstance(M0, UniformAngle) and
+            isinstance(s, (Fixed, LogNormal))):
+        raise NotImplementedError("device prior sampling covers the default nonlinear priors: "
+                                  "LogUniform P, Beta e, uniform omega and M0, Fixed or "
+                                  "LogNormal s")
+    spec = nat.PriorSpec()
+    spec.P_min, spec.P_max = P.a, P.b
+    spec.e_alpha, spec.e_beta = e.alpha, e.beta
+    if isinstance(s, Fixed):
+        spec.s_kind, spec.s_value = nat.JOKER_S_FIXED, s.value
+    else:
+        spec.s_kind, spec.s_mu, spec.s_sigma = nat.JOKER_S_LOGNORMAL, s.mu, s.sigma
+    return spec
