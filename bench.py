@@ -571,21 +571,17 @@ def run_serving(args, rank, world):
     from thejoker_gb300 import build as tb
     from thejoker_gb300 import device as dev
     from thejoker_gb300.serve import Request, ServingEngine
-    from thejoker_gb300.synthetic import fill_prior_cache
     tb.build()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     S = args.samples
-    host = torch.empty((S, 5), dtype=torch.float64).pin_memory()
-    fill_prior_cache(host.numpy(), SEED_CACHE + 2)
+    # the resident cache is drawn on the device (P log-uniform [2, 1024] d,
+    # e ~ Beta(0.867, 3.03), uniform angles, s = 0)
     cache = dev.PriorCache(S)
-    stage = torch.empty((1 << 24, 5), dtype=torch.float64, device="cuda")
-    for a in range(0, S, 1 << 24):
-        b = min(S, a + (1 << 24))
-        stage[: b - a].copy_(host[a:b], non_blocking=True)
-        cache.load(stage[: b - a], row0=a)
+    t0 = time.perf_counter()
+    cache.sample_prior(dict(P_min=2.0, P_max=1024.0, e_alpha=0.867, e_beta=3.03, s_kind=0,
+                            s_value=0.0), S, seed=SEED_CACHE + 2)
     torch.cuda.synchronize()
-    del stage, host
-    torch.cuda.empty_cache()
+    cache_s = time.perf_counter() - t0
     n_all = args.requests
     stars, budgets, n_reqs = _serving_requests(n_all, 11 + rank)
 
@@ -652,10 +648,75 @@ def run_serving(args, rank, world):
                                f"2^{int(math.log2(S))} cache, n_requested in {{1,128,512}}",
                    "slots": args.slots, "round_budget": args.round_budget,
                    "requests_max": n_all, "window_s": args.window},
-        "sweep": sweep, "rounds": rounds,
+        "sweep": sweep, "rounds": rounds, "cache_sample_s": cache_s,
         "fp64_per_star": fp64,
         "clocks": clk.summary(),
     }
+
+
+def run_small(args, rank, world):
+    """The reference's own small case: one star, 16 epochs at 2456000 +
+    U(0, 1000) d, sigma ~ U(0.1, 1) km/s, a Keplerian drawn from the prior plus
+    noise; a 2^20-sample prior cache (s = 0); the plain FP64 GPU path, the
+    mixed path and the reference's CPU likelihood over all 2^20 samples; ln L
+    differences and accept-mask agreement."""
+    import torch
+    from thejoker_gb300 import build as tb
+    from thejoker_gb300 import device as dev
+    from thejoker_gb300.batch import BatchRejection
+    from thejoker_gb300.linear import rv_unit_columns
+    from thejoker_gb300.synthetic import fill_prior_cache
+    tb.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    rng = np.random.default_rng(0)
+    N, S = 16, args.samples
+    t = np.sort(2456000.0 + rng.uniform(0, 1000.0, N))
+    err = rng.uniform(0.1, 1.0, N)
+    P = np.exp(rng.uniform(np.log(2), np.log(1024)))
+    e = rng.beta(0.867, 3.03)
+    om, M0 = rng.uniform(0, 2 * np.pi, 2)
+    K = 30.0 * (P / 365.25) ** (-1 / 3) / np.sqrt(1 - e ** 2) * rng.normal()
+    rv = K * rv_unit_columns(t, t.min(), [P], [e], [om], [M0])[0] + rng.normal(0, 100.0) \
+        + rng.normal(0, err)
+    star = dict(t=t, rv=rv, ivar=1 / err ** 2, t_ref=t.min(), trend_M=np.ones((N, 1)),
+                mu=np.zeros(2), lam=np.array([0.0, 100.0 ** 2]),
+                k_prior=np.array([1.0, 30.0, 365.25, 500.0]))
+    chunk = fill_prior_cache(np.empty((S, 5)), 0)
+    cache = dev.PriorCache.from_samples(chunk)
+    table = dev.StarTable([star])
+    res = {}
+    for prec in ("fp64", "mixed"):
+        br = BatchRejection(table, cache, precision=prec, max_out=S, seeds=[1])
+        for _ in range(args.warmup):
+            br.run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            br.run()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        counts, idx, _ = br.results()
+        res[prec] = (ms, idx[0], br.lnl[0, :S].cpu().numpy())
+    d = np.abs(res["mixed"][2] - res["fp64"][2])
+    near = res["fp64"][2] > res["fp64"][2].max() - 40
+    line = {
+        "metric": "prior samples/s (lnL+accept)", "value": S / (res["mixed"][0] * 1e-3),
+        "unit": "samples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": res["mixed"][0], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64 (mixed)",
+        "data": "synthetic (seeded star and prior cache)",
+        "config": {"workload": f"1 star x {N} epochs over 1000 d, prior cache 2^"
+                               f"{int(math.log2(S))} (s = 0)"},
+        "fp64": {"value": S / (res["fp64"][0] * 1e-3), "ms_per_step": res["fp64"][0]},
+        "max_abs_dlnl": float(d.max()), "max_abs_dlnl_within_40_of_max": float(d[near].max()),
+        "accepted": int(len(res["fp64"][1])),
+        "accept_identical": bool(np.array_equal(res["fp64"][1], res["mixed"][1])),
+    }
+    if not args.no_cpu:
+        v, kind, cores, secs = cpu_baseline(star, S, seed=0)
+        line["cpu_baseline"] = {"value": v, "unit": "samples/s", "cores": cores, "kind": kind,
+                                "sample": f"all {S} prior samples ({secs:.2f} s wall)"}
+    return line
 
 
 def run_reference(args, rank):
@@ -699,7 +760,7 @@ def main():
     p.add_argument("--traffic", type=float, default=None)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--config", default="single",
-                   choices=["single", "batched", "iterative", "serving"])
+                   choices=["single", "small", "batched", "iterative", "serving"])
     p.add_argument("--stars", type=int, default=None)
     p.add_argument("--n-requested", type=int, default=256)
     p.add_argument("--requests", type=int, default=20000)
@@ -707,13 +768,13 @@ def main():
     p.add_argument("--window", type=float, default=4.0)
     p.add_argument("--slots", type=int, default=1024)
     p.add_argument("--round-budget", type=int, default=1 << 26)
-    p.add_argument("--fp64-requests", type=int, default=32)
+    p.add_argument("--fp64-requests", type=int, default=128)
     p.add_argument("--group", type=int, default=None)
     p.add_argument("--subset-stars", type=int, default=64)
     args = p.parse_args()
     if args.samples is None:
-        args.samples = {"single": 1 << 28, "batched": 1 << 24, "iterative": 1 << 22,
-                        "serving": 1 << 28}[args.config]
+        args.samples = {"single": 1 << 28, "small": 1 << 20, "batched": 1 << 24,
+                        "iterative": 1 << 22, "serving": 1 << 28}[args.config]
     if args.stars is None:
         args.stars = {"batched": 4096, "iterative": 1024}.get(args.config, 1)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -730,6 +791,8 @@ def main():
             dist = tdist
         if args.config == "batched":
             line = run_batched(args, rank, world)
+        elif args.config == "small":
+            line = run_small(args, rank, world)
         elif args.config == "iterative":
             line = run_iterative(args, rank, world)
         elif args.config == "serving":
