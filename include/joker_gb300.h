@@ -45,6 +45,8 @@ extern "C" {
 
 /* limits */
 #define JOKER_MAX_LINEAR 6  /* K + poly_trend + n_offsets */
+#define JOKER_MIXED_LNL_TOL 1e-4  /* joker_accept_refined: |ln L - FP64 ln L| of every
+                                     kept sample is at most this */
 
 /* precision of the likelihood kernels */
 #define JOKER_FP64 0        /* plain FP64 throughout */
@@ -201,10 +203,13 @@ int joker_accept(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
  * max_slot) receives the FP64 maxima -- or, with max_given != 0, already holds
  * them (from joker_refine_max, e.g. combined over ranks that each own a range
  * of the same star's samples).  d_n_refined (optional) counts the re-evaluated
- * samples.  Same workspace as joker_accept. */
+ * samples.  Every kept sample whose bound exceeds JOKER_MIXED_LNL_TOL is
+ * re-evaluated as well, so every kept ln L (d_out_lnl) is within that of the
+ * FP64 value.  Each re-evaluated sample's FP64 ln L is written back to d_lnl
+ * and its bound in d_err set to 0.  Same workspace as joker_accept. */
 int joker_accept_refined(const joker_stars *stars, const joker_cache *cache,
-                         const joker_accept_seg *segs, int n_segs, const double *d_lnl,
-                         const float *d_err, const uint64_t *d_bound_key,
+                         const joker_accept_seg *segs, int n_segs, double *d_lnl,
+                         float *d_err, const uint64_t *d_bound_key,
                          uint64_t *d_exact_key, int n_slots, int max_given, int u_source,
                          const double *d_u, int64_t *d_out_idx, double *d_out_lnl,
                          int64_t *d_count, uint64_t *d_n_refined, void *d_work,

@@ -176,3 +176,41 @@ def test_refined_accept_equals_fp64_accept(cuda, n_ep, K, jitter):
     # site; its maximum matches the FP64 kernel's to rounding
     np.testing.assert_allclose(exact.values()[0], k64.values()[0], rtol=1e-13)
     assert int(nref[0]) < S // 50
+
+
+@pytest.mark.parametrize("K,sig", [(198.0, (0.1, 1.0)), (0.0, (2.0, 5.0))])
+def test_refined_kept_lnl_within_tolerance(cuda, K, sig):
+    """Every kept sample's ln L (out_lnl) is within JOKER_MIXED_LNL_TOL of the FP64
+    value: kept samples whose bound is looser are re-evaluated in FP64.  The
+    first star is so well constrained that the best prior sample still has
+    chi2 ~ 4e4 (mixed error ~1e-3 there); the second is constant with broad
+    errors (many kept samples)."""
+    from thejoker_gb300 import device as dev
+    from thejoker_gb300.synthetic import fill_prior_cache
+    rng = np.random.default_rng(0)
+    st = synth_star(rng, 16, K=K, sig=sig)
+    S = 1 << 20
+    chunk = fill_prior_cache(np.empty((S, 5)), 0)
+    cache = dev.PriorCache.from_samples(chunk)
+    table = dev.StarTable([st])
+    f64 = torch.empty((1, S), dtype=torch.float64, device="cuda")
+    dev.lnl(table, cache, f64, precision="fp64")
+    mix = torch.empty((1, S), dtype=torch.float64, device="cuda")
+    err = torch.empty((1, S), dtype=torch.float32, device="cuda")
+    bk = dev.MaxKeys(2)
+    dev.lnl(table, cache, mix, precision="mixed", err=err, bound_keys=bk)
+    st_, inc = dev.pcg64_state(np.random.default_rng(5))
+    seg = dict(lnl_off=0, n=S, idx_base=0, out_off=0, max_out=S, max_slot=0, star=0, row0=0,
+               pcg=(st_, inc, 0))
+    out_lnl = torch.empty(S, dtype=torch.float64, device="cuda")
+    idx, _, cnt, _, _ = dev.accept_refined(table, cache, mix.view(-1), err.view(-1), bk, [seg],
+                                           out_lnl=out_lnl)
+    c = int(cnt[0])
+    assert c > 0
+    kept = idx[:c].cpu().numpy()
+    ref = f64[0].cpu().numpy()
+    got = out_lnl[:c].cpu().numpy()
+    assert np.max(np.abs(got - ref[kept])) <= 1e-4
+    # the FP64 acceptance keeps the same samples
+    idx64, _, cnt64 = dev.accept(f64.view(-1), _keys_for([float(ref.max())]), [seg])
+    np.testing.assert_array_equal(kept, idx64[:int(cnt64[0])].cpu().numpy())

@@ -819,8 +819,8 @@ extern "C" int joker_refine_max(const joker_stars *s, const joker_cache *c,
 }
 
 extern "C" int joker_accept_refined(const joker_stars *s, const joker_cache *c,
-                                    const joker_accept_seg *segs, int n_segs, const double *d_lnl,
-                                    const float *d_err, const uint64_t *d_bound_key,
+                                    const joker_accept_seg *segs, int n_segs, double *d_lnl,
+                                    float *d_err, const uint64_t *d_bound_key,
                                     uint64_t *d_exact_key, int n_slots, int max_given,
                                     int u_source, const double *d_u, int64_t *d_out_idx,
                                     double *d_out_lnl, int64_t *d_count, uint64_t *d_n_refined,

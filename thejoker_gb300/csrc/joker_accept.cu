@@ -208,6 +208,9 @@ __global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
             } else {
                 u = a.u[sg.u_off + i];
             }
+            // the FP64 value replaces the mixed one (exact, so its bound is 0)
+            const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
+            const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
             if (accept_test(v - mx, u)) {
                 const int64_t gblk = seg_base(a, si) + i / ACC_BLOCK;
                 atomicOr(a.words + gblk * ACC_THREADS + (i % ACC_BLOCK) / 32, 1u << (i & 31));
@@ -270,6 +273,8 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
                 } else {
                     u = a.u[sg.u_off + i];
                 }
+                const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
+                const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
                 if (accept_test(v - mx, u)) add |= 1u << b;
             }
         }
@@ -343,6 +348,9 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
                     dec = interval_test(v, er, mx, u);
                 }
             }
+            // an accepted sample whose bound exceeds JOKER_MIXED_LNL_TOL is
+            // re-evaluated in FP64 too, so that every kept ln L is that close
+            if (refine && dec == 1 && !(er <= (float)JOKER_MIXED_LNL_TOL)) dec = -1;
             keep = dec == 1;
             amb = dec < 0;
         }
