@@ -217,6 +217,10 @@ def run_ours(args, rank, world, dist):
     pcg_state, pcg_inc = dev.pcg64_state(gen)
     del stage
     torch.cuda.empty_cache()
+    # work-item size from the autotuner, measured here on this workload
+    from thejoker_gb300 import autotune
+    tuned, tune_ms = autotune.tune(table, cache, precision="mixed", count=min(S, 1 << 26),
+                                   reps=2)
     if world > 1:
         runner = ShardedRejection(table, cache, row0=rank * S, precision="mixed", max_out=S)
     else:
@@ -338,7 +342,8 @@ def run_ours(args, rank, world, dist):
                    "prior_samples_per_gpu": S, "n_epochs": N_EPOCHS, "n_linear": 2,
                    "l2": "inputs larger than L2 (cache 76 B/sample resident, 2^28 samples)",
                    "precision": "mixed", "u_source": "numpy PCG64 stream regenerated on device",
-                   "accept": "refined to the FP64 decisions"},
+                   "accept": "refined to the FP64 decisions",
+                   "autotune": {"chunk": tuned, "ms_per_2^26_samples": tune_ms}},
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "samples/s",
                 "h2d_bytes_per_step": S * 40, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms},
@@ -389,6 +394,11 @@ def run_batched(args, rank, world):
     fill_prior_cache(host.numpy(), SEED_CACHE)
     cache = dev.PriorCache(S).load(host.cuda())
     table = dev.StarTable(stars)
+    from thejoker_gb300 import autotune
+    sub_t = dev.StarTable(stars[:256])
+    sub_t.n_epochs = table.n_epochs            # tune for the survey's epoch counts
+    tuned, tune_ms = autotune.tune(sub_t, cache, precision="mixed", count=min(S, 1 << 22),
+                                   reps=1)
     br = BatchRejection(table, cache, precision="mixed", max_out=256,
                         seeds=np.arange(n_stars) + rank * n_stars, group=args.group)
     for _ in range(args.warmup):
@@ -425,7 +435,8 @@ def run_batched(args, rank, world):
         "config": {"workload": f"{n_stars} stars x 2^{int(math.log2(S))} shared prior samples, "
                                f"epochs log-uniform [3,256] (mean {n_ep.mean():.1f}), 30% "
                                "companions; acceptance refined to FP64 decisions",
-                   "stars_per_gpu": n_stars, "prior_samples": S, "group": br.group},
+                   "stars_per_gpu": n_stars, "prior_samples": S, "group": br.group,
+                   "autotune": {"chunk": tuned, "ms_256_stars_2^22_samples": tune_ms}},
         "subset": {"stars": sub, "samples": Ssub,
                    "mixed_samples_per_s": sub * Ssub / res["mixed"][0],
                    "fp64_samples_per_s": sub * Ssub / res["fp64"][0],

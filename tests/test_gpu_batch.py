@@ -82,3 +82,25 @@ def test_host_pipeline_matches_batch(cuda):
         np.testing.assert_array_equal(counts, c2)
         for k in range(6):
             np.testing.assert_array_equal(idx[k], i2[k])
+
+
+def test_autotune_records_fastest_chunk(cuda, tmp_path):
+    from thejoker_gb300 import autotune as at
+    from thejoker_gb300 import device as dev
+    from thejoker_gb300.batch import BatchRejection
+    from thejoker_gb300.synthetic import fill_prior_cache, survey_stars
+    stars = survey_stars(8, seed=5, n_min=10, n_max=40)
+    cache = dev.PriorCache.from_samples(fill_prior_cache(np.empty((1 << 18, 5)), 3))
+    table = dev.StarTable(stars)
+    path = str(tmp_path / "tune.json")
+    best, times = at.tune(table, cache, precision="mixed", candidates=(256, 1024, 4096), reps=1,
+                          path=path)
+    assert best in (256, 1024, 4096) and times[best] == min(times.values())
+    assert at.chunk_for(table.n_linear, table.jitter, "mixed", table.n_epochs, path=path) == best
+    # an engine built without a chunk picks the tuned size
+    import os
+    os.environ["JOKER_AUTOTUNE"] = path
+    try:
+        assert BatchRejection(table, cache, max_out=4).chunk == best
+    finally:
+        del os.environ["JOKER_AUTOTUNE"]

@@ -39,16 +39,21 @@ class BatchRejection:
     "fp64".  group: stars per launch (bounded by device memory: 12 bytes per
     star and sample for the mixed path).  seeds: one seed per star for its
     numpy PCG64 generator (its first ``n`` uniforms are the star's ``uu``).
+    chunk: samples per ln L work item (None: the autotuned size, autotune.py).
     """
 
     def __init__(self, stars, cache, precision="mixed", jitter="reference", group=None,
-                 max_out=256, seeds=None, chunk=0, timing=False):
+                 max_out=256, seeds=None, chunk=None, timing=False):
         self.table = stars if isinstance(stars, dev.StarTable) else dev.StarTable(stars,
                                                                                   jitter=jitter)
         self.cache = cache
         self.precision = precision
         self.n_stars = self.table.n_stars
         self.max_out = int(max_out)
+        if chunk is None:                      # the autotuned work-item size
+            from .autotune import chunk_for
+            chunk = chunk_for(self.table.n_linear, self.table.jitter, precision,
+                              self.table.n_epochs)
         self.chunk = int(chunk)
         S = cache.size
         if group is None:

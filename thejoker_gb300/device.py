@@ -81,6 +81,7 @@ class StarTable:
         self.n_linear = int(n_linear)
         self.jitter = jitter
         self.max_epochs = int(max_epochs)
+        self.n_epochs = None               # filled slot by slot
         return self
 
     def set(self, slot, star, stream=None):

@@ -32,7 +32,7 @@ class IterativeBatch:
 
     def __init__(self, table, cache, n_requested, precision="mixed", lib_row0=0, lib_size=None,
                  seeds=None, init_batch_size=None, growth_factor=128, safety_factor=1.0,
-                 maxiter=128, chunk=1024, round_budget=0):
+                 maxiter=128, chunk=None, round_budget=0):
         self.table, self.cache = table, cache
         self.n = table.n_stars
         self.n_requested = int(n_requested)
@@ -45,6 +45,9 @@ class IterativeBatch:
                              f"cache file. You have, or have limited to, {lib_size} samples.")
         if seeds is None:
             seeds = np.arange(self.n)
+        if chunk is None:                      # the autotuned work-item size
+            from .autotune import chunk_for
+            chunk = chunk_for(table.n_linear, table.jitter, precision, table.n_epochs)
         pcg = self._pcg(seeds)
         self.lib_size, self.init = lib_size, init
         h = ctypes.c_void_p()

@@ -33,13 +33,17 @@ class HostRejection:
     host prior chunks of up to ``capacity`` rows."""
 
     def __init__(self, table, capacity, precision="mixed", slice_rows=1 << 24, max_out=256,
-                 zero_copy=True):
+                 zero_copy=True, chunk=None):
         self.table = table
         self.precision = precision
         self.capacity = int(capacity)
         self.slice_rows = int(min(slice_rows, capacity))
         self.max_out = int(max_out)
         self.zero_copy = bool(zero_copy)
+        if chunk is None:                      # the autotuned work-item size
+            from .autotune import chunk_for
+            chunk = chunk_for(table.n_linear, table.jitter, precision, table.n_epochs)
+        self.chunk = int(chunk)
         n = table.n_stars
         self.cache = None if self.zero_copy else dev.PriorCache(self.capacity)
         self.stage = [] if self.zero_copy else \
@@ -79,7 +83,7 @@ class HostRejection:
                 self.freed[k % 2].record(ks)
                 dev.lnl(self.table, self.cache, self.lnl, precision=self.precision, row0=a,
                         count=b - a, max_keys=self.keys, err=self.err, bound_keys=self.bkeys,
-                        out_offset=a, stream=ks)
+                        out_offset=a, chunk=self.chunk, stream=ks)
         return self.cache
 
     def run(self, host_chunk, pcg_states):
@@ -105,7 +109,8 @@ class HostRejection:
             cache = dev.PriorCache.view(host_chunk.contiguous())
             with torch.cuda.stream(ks):
                 dev.lnl(self.table, cache, self.lnl, precision=self.precision, row0=0, count=S,
-                        max_keys=self.keys, err=self.err, bound_keys=self.bkeys, stream=ks)
+                        max_keys=self.keys, err=self.err, bound_keys=self.bkeys,
+                        chunk=self.chunk, stream=ks)
         else:
             cache = self._staged(host_chunk, S, ks)
         n = self.table.n_stars
