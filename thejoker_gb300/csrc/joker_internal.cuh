@@ -146,15 +146,22 @@ struct AcceptArgs {
 };
 
 // ---------------------------------------------------------------- helpers
+// Order-preserving key of a double from its bits (integer operations only).
+__host__ __device__ __forceinline__ unsigned long long key_of_bits(long long b) {
+    if ((b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL)
+        return 0xFFFFFFFFFFFFFFFFull;          // NaN dominates, as numpy's max
+    return (b < 0) ? ~(unsigned long long)b : ((unsigned long long)b | 0x8000000000000000ull);
+}
+
 __host__ __device__ __forceinline__ unsigned long long double_to_key(double x) {
 #ifdef __CUDA_ARCH__
     long long b = __double_as_longlong(x);
 #else
     long long b; memcpy(&b, &x, 8);
 #endif
-    if (x != x) return 0xFFFFFFFFFFFFFFFFull;  // NaN dominates, as numpy's max
-    return (b < 0) ? ~(unsigned long long)b : ((unsigned long long)b | 0x8000000000000000ull);
+    return key_of_bits(b);
 }
+
 
 __host__ __device__ __forceinline__ double key_to_double(unsigned long long k) {
     unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
