@@ -1,6 +1,6 @@
 """The two forms of the mixed kernel (GB300 only): two samples per thread on
-the paired FP32 instructions (the default for L <= 3) and one sample per
-thread.  Each must keep |ln L - FP64 ln L| within its own per-sample bound, and
+the paired FP32 instructions (the default for L <= 3, and for any L without
+jitter) and one sample per thread.  Each must keep |ln L - FP64 ln L| within its own per-sample bound, and
 the two agree within the sum of their bounds.  The form is fixed per process
 (JOKER_MIXED_PAIRED=0 selects one sample per thread), so each runs in a child
 process."""
@@ -63,5 +63,3 @@ def test_paired_and_scalar_within_bounds(cuda, tmp_path):
                 assert np.all(d <= r[name + prec + "_err"]), (name, prec)
             gap = np.abs(a[name + prec] - b[name + prec])
             assert np.all(gap <= a[name + prec + "_err"] + b[name + prec + "_err"]), (name, prec)
-        if name == "ref4":                 # L = 4: both processes use one sample per thread
-            np.testing.assert_array_equal(a["ref4mixed"], b["ref4mixed"])

@@ -120,11 +120,11 @@ static cudaError_t launch_fp64_L(bool jit, const LnlArgs &a, int block, cudaStre
 
 template <int L, int VAR>
 static cudaError_t launch_mixed_LV(bool jit, const LnlArgs &a, int block, cudaStream_t st) {
-    if constexpr (L <= 3) {
-        if (mixed_paired(L)) {
+    if (mixed_paired(L, jit)) {
+        if constexpr (L <= 3) {
             if (jit) return launch_persistent(lnl_mixed2_kernel<L, true, VAR, false>, a, block, st);
-            return launch_persistent(lnl_mixed2_kernel<L, false, VAR, false>, a, block, st);
         }
+        return launch_persistent(lnl_mixed2_kernel<L, false, VAR, false>, a, block, st);
     }
     if (jit) return launch_persistent(lnl_mixed_kernel<L, true, VAR, false>, a, block, st);
     return launch_persistent(lnl_mixed_kernel<L, false, VAR, false>, a, block, st);

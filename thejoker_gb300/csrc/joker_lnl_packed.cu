@@ -9,11 +9,11 @@ namespace joker {
 
 template <int L, int VAR>
 static cudaError_t launch_packed_LV(bool jit, const LnlArgs &a, int block, cudaStream_t st) {
-    if constexpr (L <= 3) {
-        if (mixed_paired(L)) {
+    if (mixed_paired(L, jit)) {
+        if constexpr (L <= 3) {
             if (jit) return launch_persistent(lnl_mixed2_kernel<L, true, VAR, true>, a, block, st);
-            return launch_persistent(lnl_mixed2_kernel<L, false, VAR, true>, a, block, st);
         }
+        return launch_persistent(lnl_mixed2_kernel<L, false, VAR, true>, a, block, st);
     }
     if (jit) return launch_persistent(lnl_mixed_kernel<L, true, VAR, true>, a, block, st);
     return launch_persistent(lnl_mixed_kernel<L, false, VAR, true>, a, block, st);

@@ -703,14 +703,15 @@ inline cudaError_t launch_persistent(K kern, const LnlArgs &a, int block, cudaSt
 }  // namespace joker
 
 namespace joker {
-// Paired form for L <= 3 unless JOKER_MIXED_PAIRED=0 (the one-sample-per-thread
-// form, kept for comparison).
-inline bool mixed_paired(int L) {
+// Paired form for L <= 3, and without jitter for any L (its epoch sums are
+// L + 1 float pairs), unless JOKER_MIXED_PAIRED=0 (the one-sample-per-thread
+// form, kept for comparison and for larger systems with jitter).
+inline bool mixed_paired(int L, bool jit) {
     static int env = -1;
     if (env < 0) {
         const char *v = getenv("JOKER_MIXED_PAIRED");
         env = (v && v[0] == '0') ? 0 : 1;
     }
-    return env == 1 && L <= 3;
+    return env == 1 && (L <= 3 || !jit);
 }
 }  // namespace joker
