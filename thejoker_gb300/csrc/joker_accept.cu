@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
             if (a.u_source == JOKER_U_PCG64) {
                 const u128 s0 = ((u128)sg.pcg_state_hi << 64) | (u128)sg.pcg_state_lo;
                 const u128 inc = ((u128)sg.pcg_inc_hi << 64) | (u128)sg.pcg_inc_lo;
-                u = pcg_uniform(pcg_output(pcg_advance(s0, inc, (uint64_t)i + 1)));
+                u = pcg_uniform(pcg_output(pcg_jump(s0, inc, (uint64_t)i + 1)));
             } else {
                 u = a.u[sg.u_off + i];
             }
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
                 if (a.u_source == JOKER_U_PCG64) {
                     const u128 s0 = ((u128)sg.pcg_state_hi << 64) | (u128)sg.pcg_state_lo;
                     const u128 inc = ((u128)sg.pcg_inc_hi << 64) | (u128)sg.pcg_inc_lo;
-                    u = pcg_uniform(pcg_output(pcg_advance(s0, inc, (uint64_t)i + 1)));
+                    u = pcg_uniform(pcg_output(pcg_jump(s0, inc, (uint64_t)i + 1)));
                 } else {
                     u = a.u[sg.u_off + i];
                 }
@@ -300,24 +300,29 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
                              : key_to_double(a.max_key[sg.max_slot]);
     const double *lnl = a.lnl + sg.lnl_off;
 
-    u128 st = 0, inc = 0, Am = 1, Cp = 0;
+    // four independent PCG64 chains per lane (k = 4 kk + c, c = 0..3), each
+    // stepping 128 positions: draw at position p is output(state after p + 1 steps)
+    u128 stc[4] = {0, 0, 0, 0}, inc = 0, A128 = 1, C128 = 0;
     if (a.u_source == JOKER_U_PCG64) {
         const u128 s0 = ((u128)sg.pcg_state_hi << 64) | (u128)sg.pcg_state_lo;
         inc = ((u128)sg.pcg_inc_hi << 64) | (u128)sg.pcg_inc_lo;
-        // draw at position p is output(state after p + 1 steps)
-        st = pcg_advance(s0, inc, (uint64_t)(wbase + lane + 1));
-        // affine map for 32 steps: s -> Am s + Cp
-        u128 cm = pcg_mult(), cp = inc;
+        const u128 sw = pcg_jump(s0, inc, (uint64_t)(wbase + 1));     // uniform over the warp
+        stc[0] = u128_of(g_pcg.lane_a[lane]) * sw + u128_of(g_pcg.lane_s[lane]) * inc;
+        const u128 A32 = u128_of(g_pcg.lane_a[32]), C32 = u128_of(g_pcg.lane_s[32]) * inc;
 #pragma unroll
-        for (int b = 0; b < 5; ++b) { cp = (cm + 1) * cp; cm *= cm; }
-        Am = cm;
-        Cp = cp;
+        for (int c = 1; c < 4; ++c) stc[c] = A32 * stc[c - 1] + C32;
+        A128 = u128_of(g_pcg.dbl_a[7]);
+        C128 = u128_of(g_pcg.dbl_s[7]) * inc;
     }
     float mxf;
     const bool fast = dbl_to_float_trunc(mx, mxf);
     uint32_t my_word = 0, my_amb = 0;
     int my_count = 0;
-    for (int k = 0; k < 32; ++k) {
+    for (int kk = 0; kk < 8; ++kk) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const int k = 4 * kk + c;
+        const u128 st = stc[c];
         const int64_t i = wbase + (int64_t)k * 32 + lane;
         bool keep = false, amb = false;
         if (i < sg.n) {
@@ -354,7 +359,7 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
             keep = dec == 1;
             amb = dec < 0;
         }
-        if (a.u_source == JOKER_U_PCG64) st = Am * st + Cp;
+        if (a.u_source == JOKER_U_PCG64) stc[c] = A128 * stc[c] + C128;
         const uint32_t bal = __ballot_sync(0xffffffffu, keep);
         const bool fit = !refine || flag_append(a, 1, amb, si, i);
         const uint32_t abal = __ballot_sync(0xffffffffu, !fit);
@@ -363,6 +368,7 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
             my_amb = abal;
         }
         my_count += __popc(bal);
+    }
     }
     // word index within the CTA: warp * 32 + lane
     a.words[gblk * ACC_THREADS + threadIdx.x] = my_word;

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(1024) iter_plan_kernel(IterParams p, int zero_
                     // its earlier ones in its generator's stream
                     const u128 s0 = ((u128)p.pcg0[4 * s] << 64) | (u128)p.pcg0[4 * s + 1];
                     const u128 inc = ((u128)p.pcg0[4 * s + 2] << 64) | (u128)p.pcg0[4 * s + 3];
-                    const u128 sr = pcg_advance(s0, inc, (uint64_t)st[ST_UCONS]);
+                    const u128 sr = pcg_jump(s0, inc, (uint64_t)st[ST_UCONS]);
                     g.pcg_state_hi = (uint64_t)(sr >> 64);
                     g.pcg_state_lo = (uint64_t)sr;
                     g.pcg_inc_hi = p.pcg0[4 * s + 2];

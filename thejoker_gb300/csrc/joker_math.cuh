@@ -163,6 +163,47 @@ __device__ __forceinline__ u128 pcg_advance(u128 s, u128 inc, uint64_t delta) {
     return am * s + ap;
 }
 
+// Stepping the LCG n times maps s -> A^n s + S_n inc, S_n = 1 + A + ... + A^(n-1).
+// Tables of (A^n, S_n) for n = 2^k and for n = 0..32, computed at compile time:
+// (A^2n, S_2n) = (A^n A^n, S_n (1 + A^n)), (A^(l+1), S_(l+1)) = (A A^l, S_l + A^l).
+struct PcgTables {
+    unsigned long long dbl_a[64][2], dbl_s[64][2];
+    unsigned long long lane_a[33][2], lane_s[33][2];
+};
+
+constexpr PcgTables make_pcg_tables() {
+    PcgTables t{};
+    const u128 A = ((u128)0x2360ED051FC65DA4ull << 64) | (u128)0x4385DF649FCCF645ull;
+    u128 a = A, sum = 1;
+    for (int k = 0; k < 64; ++k) {
+        t.dbl_a[k][0] = (unsigned long long)a; t.dbl_a[k][1] = (unsigned long long)(a >> 64);
+        t.dbl_s[k][0] = (unsigned long long)sum; t.dbl_s[k][1] = (unsigned long long)(sum >> 64);
+        sum = sum * (a + 1);
+        a = a * a;
+    }
+    u128 al = 1, sl = 0;
+    for (int l = 0; l <= 32; ++l) {
+        t.lane_a[l][0] = (unsigned long long)al; t.lane_a[l][1] = (unsigned long long)(al >> 64);
+        t.lane_s[l][0] = (unsigned long long)sl; t.lane_s[l][1] = (unsigned long long)(sl >> 64);
+        sl = sl + al;
+        al = al * A;
+    }
+    return t;
+}
+
+__constant__ PcgTables g_pcg = make_pcg_tables();
+
+__device__ __forceinline__ u128 u128_of(const unsigned long long (&v)[2]) {
+    return ((u128)v[1] << 64) | (u128)v[0];
+}
+
+// Advance by n steps with the doubling table (popcount(n) multiply-adds).
+__device__ __forceinline__ u128 pcg_jump(u128 s, u128 inc, uint64_t n) {
+    for (int k = 0; n; ++k, n >>= 1)
+        if (n & 1) s = u128_of(g_pcg.dbl_a[k]) * s + u128_of(g_pcg.dbl_s[k]) * inc;
+    return s;
+}
+
 __device__ __forceinline__ double pcg_uniform(uint64_t x) {
     return (double)(x >> 11) * (1.0 / 9007199254740992.0);
 }
