@@ -326,6 +326,19 @@ int joker_linear_posterior(const joker_stars *stars, const joker_cache *cache, i
 int joker_unmarginalized_lnl(const joker_stars *stars, int star, const double *d_pars, int64_t n,
                              int n_trend, double dt_shift, double *d_out, void *stream);
 
+/* ---- radial velocity of Keplerian orbits ---------------------------------
+ * Replaces twobody's c_rv_from_elements(t, rv, N_t, P, K, e, omega, phi0,
+ * t0, tol, maxiter) as bound at thejoker/src/fast_likelihood.pyx:27-30 and
+ * called at :453-455, batched over n element sets on the device:
+ *   d_rv[i * n_t + j] = K_i (cos(omega_i + f_ij) + e_i cos omega_i),
+ *   M_ij = 2 pi (d_t[j] - t0) / P_i - M0_i,
+ * f the true anomaly.  d_elems: n x 5 row-major FP64 rows (P, K, e, omega,
+ * M0), 0 <= e < 1.  The FP64 solver is the one the ln L kernels use
+ * (non-iterative, converged to FP64), so tol and maxiter have no
+ * counterpart.  All pointers are device pointers. */
+int joker_rv_from_elements(const double *d_t, int n_t, const double *d_elems, int64_t n,
+                           double t0, double *d_rv, void *stream);
+
 /* ---- acceptance without allocation ---------------------------------------
  * No counterpart in the reference.  joker_accept_noalloc is joker_accept for
  * callers that must not allocate device memory: a serving loop with

@@ -114,3 +114,21 @@ def test_reference_module_reproduces_fixture(golden_dir):
     out = np.array(h.batch_marginal_ln_likelihood(np.ascontiguousarray(z["chunk"][:256])))
     assert L == 4
     np.testing.assert_array_equal(out, z["lnl_ref"][:256])
+
+
+def _kepler_hp(golden_dir):
+    z = np.load(os.path.join(golden_dir, "kepler_rv_hp.npz"))
+    # FP64 rounding of the phase (|M| ulps) carried through dm/dM, plus the
+    # result's own rounding: the conditioning of the RV model
+    scale = 2.0 ** -52 * (1.0 + z["dmdM"] * (z["Mabs"] + 1.0))
+    return z, scale
+
+
+def test_oracle_rv_matches_40_digit_values(golden_dir):
+    """The C oracle's Kepler solve and unit RV against 40-digit values
+    (tests/golden/make_kepler_golden.py), e up to 1 - 1e-9."""
+    z, scale = _kepler_hp(golden_dir)
+    el = z["elems"]
+    chunk = np.stack([el[:, 0], el[:, 2], el[:, 3], el[:, 4], np.zeros(len(el))], axis=1)
+    m = oracle.rv_unit(z["t"], float(z["t0"]), chunk)
+    assert np.all(np.abs(m - z["m_hp"]) <= 8.0 * scale)

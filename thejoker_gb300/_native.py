@@ -31,7 +31,7 @@ EXPORTED = (
     "joker_refine_max", "joker_iter_create", "joker_iter_destroy", "joker_iter_round",
     "joker_iter_outputs", "joker_iter_read", "joker_iter_create_pool", "joker_iter_admit",
     "joker_iter_set_round_budget", "joker_accept_noalloc", "joker_linear_posterior",
-    "joker_unmarginalized_lnl", "joker_prior_sample",
+    "joker_unmarginalized_lnl", "joker_prior_sample", "joker_rv_from_elements",
 )
 
 
@@ -116,6 +116,8 @@ _SIGS = {
                                               _vp, _vp, _vp, _vp]),
     "joker_unmarginalized_lnl": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64, ctypes.c_int,
                                                 ctypes.c_double, _vp, _vp]),
+    "joker_rv_from_elements": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64, ctypes.c_double,
+                                              _vp, _vp]),
     "joker_accept_noalloc": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                             ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

@@ -16,32 +16,65 @@ __device__ __forceinline__ double log_mixed(double x) {
     return (double)ex * 0.69314718055994530942 + (double)logf((float)m);
 }
 
-// Per-sample FP64 state: the epoch sums and the sample's constants.
-template <int L, bool JIT>
-struct Acc64 {
-    double e, Ac, Bc, Dc, k2p, M0, s2, mu0;
-    double A00, b0, A0[MAXL];            // no jitter
-    double G[L][L], q[L], rWr, slw;      // jitter: full system, sum log w
+// One Keplerian orbit in FP64: the unit-K radial velocity
+//   m(dt) = cos(omega + f) + e cos(omega),  M = 2 pi dt / P - M0,
+// in terms of the eccentric anomaly, m = (A cos E + B sin E - D)/(1 - e cos E) + D
+// with A = cos omega, B = -sin omega sqrt(1 - e^2), D = e cos omega (the model
+// twobody's c_rv_from_elements evaluates for thejoker/src/fast_likelihood.pyx
+// :453-455).
+struct OrbitF64 {
+    double e, Ac, Bc, Dc, k2p, M0;
+    float ef, omef, a1f;                 // the Kepler solver's FP32 constants
 
-    __device__ __forceinline__ void init(const StarRec &st, double P, double e_, double om,
-                                         double M0_, double s_) {
+    __device__ __forceinline__ void init(double P, double e_, double om, double M0_) {
         e = e_;
         M0 = M0_;
-        s2 = s_ * s_;
-        mu0 = st.mu0;
         k2p = TWO_PI_D / P;
         double sw, cw;
         sincos(om, &sw, &cw);
-        const double sq1me2 = sqrt((1.0 - e) * (1.0 + e));
         Ac = cw;
-        Bc = -sw * sq1me2;
+        Bc = -sw * sqrt((1.0 - e) * (1.0 + e));
         Dc = e * cw;
+        kepler_consts_f32(e, ef, omef, a1f);
+    }
+
+    __device__ __forceinline__ double rv_unit(double dt) const {
+        double M = fma(dt, k2p, -M0);
+        const double nrev = rint(M * INV_TWO_PI_D);
+        M = fma(-nrev, TWO_PI_HI_D, M);
+        M = fma(-nrev, TWO_PI_LO_D, M);
+        double sE, cE;
+        kepler_sincos_f64(M, e, ef, omef, a1f, sE, cE);
+        return fma(fma(Ac, cE, fma(Bc, sE, -Dc)), rcp_newton(fma(-e, cE, 1.0)), Dc);
+    }
+};
+
+// Per-sample FP64 state: the epoch sums and the sample's constants.
+template <int L, bool JIT>
+struct Acc64 {
+    OrbitF64 orb;
+    double s2, mu0;
+    double A00, b0, A0[MAXL];            // no jitter
+    double G[L][L], q[L], rWr;           // jitter: full system
+    // jitter: prod_j (1 + s^2 ivar_j) = pj 2^ej (pj in [1, 2) after each
+    // epoch) plus slog, the logs already summed (warp_sum); sum log w_j is
+    // sum log ivar_j - log of the product.
+    double pj, slog;
+    int ej;
+
+    __device__ __forceinline__ void init(const StarRec &st, double P, double e_, double om,
+                                         double M0_, double s_) {
+        orb.init(P, e_, om, M0_);
+        s2 = s_ * s_;
+        mu0 = st.mu0;
         A00 = 0.0;
         b0 = 0.0;
 #pragma unroll
         for (int k = 0; k < MAXL; ++k) A0[k] = 0.0;
         rWr = 0.0;
-        slw = 0.0;
+        pj = 1.0;
+        slog = 0.0;
+        ej = 0;
         if (JIT) {
 #pragma unroll
             for (int i = 0; i < L; ++i) {
@@ -54,14 +87,7 @@ struct Acc64 {
 
     // one epoch: dt = t - t_ref, y' = y - sum_{j>=1} mu_j T_j, ivar, T_1..T_{L-1}
     __device__ __forceinline__ void add(double dt, double yp, double iv, const double *T) {
-        double M = fma(dt, k2p, -M0);
-        const double nrev = rint(M * INV_TWO_PI_D);
-        M = fma(-nrev, TWO_PI_HI_D, M);
-        M = fma(-nrev, TWO_PI_LO_D, M);
-        double sE, cE;
-        kepler_sincos_f64(M, e, sE, cE);
-        const double den = 1.0 - e * cE;
-        const double m = fma(Ac, cE, fma(Bc, sE, -Dc)) / den + Dc;
+        const double m = orb.rv_unit(dt);
         if (!JIT) {
             const double wm = iv * m;
             A00 = fma(wm, m, A00);
@@ -69,8 +95,14 @@ struct Acc64 {
 #pragma unroll
             for (int k = 1; k < L; ++k) A0[k] = fma(wm, T[k - 1], A0[k]);
         } else {
-            const double wj = iv / (1.0 + s2 * iv);
-            slw += log(wj);
+            const double dj = fma(s2, iv, 1.0);
+            const double wj = iv * rcp_newton(dj);
+            // pj *= dj, then the binary exponent moves to ej (integer ops);
+            // dj >= 1 keeps pj >= 1, a positive normal number
+            pj *= dj;
+            const int hi = __double2hiint(pj);
+            ej += (hi >> 20) - 1023;
+            pj = __hiloint2double((hi & 0x000fffff) | 0x3ff00000, __double2loint(pj));
             double x[L];
             x[0] = m;
 #pragma unroll
@@ -96,7 +128,9 @@ struct Acc64 {
             for (int k = 1; k < L; ++k) A0[k] = wsum(A0[k]);
         } else {
             rWr = wsum(rWr);
-            slw = wsum(slw);
+            slog = wsum(log_prod());
+            pj = 1.0;
+            ej = 0;
 #pragma unroll
             for (int ii = 0; ii < L; ++ii) {
                 q[ii] = wsum(q[ii]);
@@ -104,6 +138,16 @@ struct Acc64 {
                 for (int k = 0; k <= ii; ++k) G[ii][k] = wsum(G[ii][k]);
             }
         }
+    }
+
+    // sum_j log(1 + s^2 ivar_j) over the epochs this accumulator has seen
+    __device__ __forceinline__ double log_prod() const {
+        return fma((double)ej, 0.69314718055994530942, slog + log(pj));
+    }
+
+    // sum_j log w_j, w_j = ivar_j / (1 + s^2 ivar_j)
+    __device__ __forceinline__ double sum_log_w(const StarRec &st) const {
+        return st.sum_log_ivar - log_prod();
     }
 
     static __device__ __forceinline__ double wsum(double x) {
@@ -184,7 +228,7 @@ __device__ __forceinline__ double k_prior_variance(const StarRec &st, double P, 
 
 template <int L, bool JIT>
 __device__ __forceinline__ double Acc64<L, JIT>::finish(const StarRec &st, double P) const {
-    const double lam0 = k_prior_variance(st, P, e);
+    const double lam0 = k_prior_variance(st, P, orb.e);
     if constexpr (!JIT) {
         return tail_schur_d<L, false>(st, A00, A0, b0, lam0, log(lam0));
     } else {
@@ -195,7 +239,7 @@ __device__ __forceinline__ double Acc64<L, JIT>::finish(const StarRec &st, doubl
             for (int k = 0; k <= ii; ++k) { Gs[ii][k] = G[ii][k]; Gs[k][ii] = G[ii][k]; }
             Gs[ii][ii] += 1.0 / (ii == 0 ? lam0 : st.lam[ii]);
         }
-        return tail_full_d<L, false>(Gs, q, rWr, st.log_norm_rest + log(lam0) - slw);
+        return tail_full_d<L, false>(Gs, q, rWr, st.log_norm_rest + log(lam0) - sum_log_w(st));
     }
 }
 

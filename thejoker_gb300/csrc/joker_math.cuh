@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include "joker_sincos_table.cuh"
 
 namespace joker {
 
@@ -17,43 +18,6 @@ constexpr float TWO_PI_LO_F = -1.7484556e-07f;              // 2 pi - TWO_PI_HI_
 // Markley (1995) starter: alpha = (3 pi^2 + 1.6 pi (pi - |M|) / (1 + e)) / (pi^2 - 6)
 constexpr double MK_A0_D = 3.0 * PI_D * PI_D / (PI_D * PI_D - 6.0);
 constexpr double MK_A1_D = 1.6 * PI_D / (PI_D * PI_D - 6.0);
-
-// ----------------------------------------------------------------- FP64 Kepler
-// Eccentric anomaly by Markley's non-iterative method (F. L. Markley, 1995,
-// "Kepler equation solver", Celestial Mechanics and Dynamical Astronomy 63,
-// 101-111): a cubic-root starter followed by one fifth-order Householder-type
-// correction.  M must lie in [-pi, pi], 0 <= e < 1.  Returns sin E and cos E;
-// the correction is applied by rotating (sin E1, cos E1) through the small
-// angle delta with its Taylor series (|delta| < 4e-4).
-__device__ __forceinline__ void kepler_sincos_f64(double M, double e, double &sinE,
-                                                  double &cosE) {
-    const double x = fabs(M);
-    const double ome = 1.0 - e;
-    const double alpha = MK_A0_D + MK_A1_D * (PI_D - x) / (1.0 + e);
-    const double d = 3.0 * ome + alpha * e;
-    const double q = 2.0 * alpha * d * ome - x * x;
-    const double r = 3.0 * alpha * d * (d - ome) * x + x * x * x;
-    double w = cbrt(fabs(r) + sqrt(q * q * q + r * r));
-    w = w * w;
-    const double E1 = (2.0 * r * w / (w * w + w * q + q * q) + x) / d;
-    double s1, c1;
-    sincos(E1, &s1, &c1);
-    const double f0 = E1 - e * s1 - x;
-    const double f1 = 1.0 - e * c1;
-    const double f2 = e * s1;
-    const double f3 = 1.0 - f1;
-    const double f4 = -f2;
-    const double d3 = -f0 / (f1 - 0.5 * f0 * f2 / f1);
-    const double d4 = -f0 / (f1 + 0.5 * d3 * f2 + d3 * d3 * f3 * (1.0 / 6.0));
-    const double d5 = -f0 / (f1 + 0.5 * d4 * f2 + d4 * d4 * f3 * (1.0 / 6.0) +
-                             d4 * d4 * d4 * f4 * (1.0 / 24.0));
-    const double dd = d5 * d5;
-    const double cd = 1.0 - dd * (0.5 - dd * (1.0 / 24.0 - dd * (1.0 / 720.0)));
-    const double sd = d5 * (1.0 - dd * (1.0 / 6.0 - dd * (1.0 / 120.0 - dd * (1.0 / 5040.0))));
-    const double sE = s1 * cd + c1 * sd;
-    cosE = c1 * cd - s1 * sd;
-    sinE = (M < 0.0) ? -sE : sE;
-}
 
 // --------------------------------------------------------- float-float helpers
 // Error-free transformations (Knuth two-sum, FMA two-product).  The _rn
@@ -130,6 +94,110 @@ __device__ __forceinline__ void kepler_sincos_f32(float M, float e, float ome, f
     const float sE = __fmaf_rn(delta, c1, __fmaf_rn(-hd2, s1, s1));
     cosE = __fmaf_rn(-delta, s1, __fmaf_rn(-hd2, c1, c1));
     sinE = (M < 0.0f) ? -sE : sE;
+}
+
+// ----------------------------------------------------------------- FP64 Kepler
+// On this GPU an FP64 instruction costs as much issue time as about 64 FP32
+// ones, so the FP64 solver does in FP64 only what needs FP64 resolution: the
+// starter is FP32, sin and cos come from a table plus short Taylor series,
+// and the reciprocals from Newton's iteration.
+
+// Reciprocal by Newton-Raphson: the hardware estimate (PTX rcp.approx.ftz.f64)
+// refined by two steps r <- r + r (1 - x r), each of which squares the
+// relative error.  For the callers' arguments (positive, >= 2^-60) the result
+// is within about an ulp of 1/x.
+__device__ __forceinline__ double rcp_newton(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    r = fma(r, fma(-x, r, 1.0), r);
+    return fma(r, fma(-x, r, 1.0), r);
+}
+
+// sin and cos, to FP64 accuracy, of an FP32 angle a in [0, 403.5/128]: with
+// k = round(128 a), r = a - k/128 is exact in FP32 and |r| <= 1/256, so
+// sin r = r - r^3/6 + r^5/120 and cos r - 1 = -r^2/2 + r^4/24 leave
+// truncation errors below 2^-60; the angle-addition formulas combine them
+// with the tabulated sin, cos of k/128.  k is clamped to the table, so any
+// input (NaN included) reads inside it.
+__device__ __forceinline__ void sincos_f32arg(float a, double &s, double &c) {
+    int k = __float2int_rn(a * 128.0f);
+    k = min(max(k, 0), SINCOS_TAB_N - 1);
+    const double r = (double)__fmaf_rn((float)k, -0.0078125f, a);
+    const double2 t = __ldg(&kSinCos128[k]);
+    const double r2 = r * r;
+    const double sr = fma(r * r2, fma(r2, 1.0 / 120.0, -1.0 / 6.0), r);
+    const double cm1 = r2 * fma(r2, 1.0 / 24.0, -0.5);
+    s = fma(t.x, cm1, fma(t.y, sr, t.x));
+    c = fma(t.y, cm1, fma(-t.x, sr, t.y));
+}
+
+// Markley's starter (F. L. Markley, 1995, "Kepler equation solver", Celestial
+// Mechanics and Dynamical Astronomy 63, 101-111) in FP32 for x = |M| in
+// [0, pi]: the root of a cubic model of Kepler's equation, within about 4e-4
+// rad of E.  ome = 1 - e and a1 = 1.6 pi / ((1 + e)(pi^2 - 6)) are the
+// sample's constants.  The discriminant is clamped at zero (it is >= 0 in
+// exact arithmetic), so x = 0 gives E1 = 0.
+__device__ __forceinline__ float markley_starter_f32(float x, float e, float ome, float a1) {
+    const float alpha = __fmaf_rn(a1, PI_F - x, (float)MK_A0_D);
+    const float d = __fmaf_rn(alpha, e, 3.0f * ome);
+    const float x2 = x * x;
+    const float ad = alpha * d;
+    const float q = __fmaf_rn(2.0f * ad, ome, -x2);
+    const float r = x * __fmaf_rn(3.0f * ad, d - ome, x2);
+    const float sq = sqrtf(fmaxf(__fmaf_rn(q * q, q, r * r), 0.0f));
+    const float w = exp2f(0.6666667f * __log2f(r + sq));          // (r + sq)^(2/3)
+    const float den3 = __fmaf_rn(w, w + q, q * q);
+    return __fmaf_rn(x, den3, 2.0f * r * w) * fast_rcp(den3 * d);
+}
+
+// FP64 eccentric anomaly of M in [-pi, pi] for 0 <= e < 1, returned as
+// (sin E, cos E).  ef, omef = 1 - e and a1f (markley_starter_f32) are the
+// sample's FP32 constants.  From the FP32 starter E1 (exact as a double) and
+// its FP64 sin and cos, the root of f(E) = E - e sin E - |M| is E1 + delta,
+// delta from the reversion of f's Taylor series about E1 to fourth order in
+// u = -f/f': with t2 = f''/f' and t3 = f'''/f' (and f'''' = -f''),
+//   delta = u - (t2/2) u^2 + (t2^2/2 - t3/6) u^3
+//             + t2 (1/24 + 5 t3/12 - 5 t2^2/8) u^4,
+// whose error is of order u^5 (the order of Markley's own fifth-order
+// correction); (sin E1, cos E1) are then rotated through delta by its Taylor
+// series (|delta| < 5e-4).
+__device__ __forceinline__ void kepler_sincos_f64(double M, double e, float ef, float omef,
+                                                  float a1f, double &sinE, double &cosE) {
+    const double x = fabs(M);
+    const float E1f = markley_starter_f32((float)x, ef, omef, a1f);
+    double s1, c1;
+    sincos_f32arg(E1f, s1, c1);
+    const double f2 = e * s1;
+    const double f3 = e * c1;
+    const double f0 = ((double)E1f - x) - f2;
+    const double i1 = rcp_newton(1.0 - f3);
+    const double u = -f0 * i1;
+    const double t2 = f2 * i1;
+    const double t3 = f3 * i1;
+    const double t22 = t2 * t2;
+    const double c3 = fma(t22, 0.5, t3 * (-1.0 / 6.0));
+    const double c4 = t2 * fma(t22, -0.625, fma(t3, 5.0 / 12.0, 1.0 / 24.0));
+    const double d = u * fma(u, fma(u, fma(u, c4, c3), -0.5 * t2), 1.0);
+    const double dd = d * d;
+    const double cm1 = dd * fma(dd, 1.0 / 24.0, -0.5);
+    const double sd = d * fma(dd, -1.0 / 6.0, 1.0);
+    const double sE = fma(s1, cm1, fma(c1, sd, s1));
+    cosE = fma(c1, cm1, fma(-s1, sd, c1));
+    sinE = (M < 0.0) ? -sE : sE;
+}
+
+// The FP32 constants of kepler_sincos_f64 for eccentricity e.
+__device__ __forceinline__ void kepler_consts_f32(double e, float &ef, float &omef, float &a1f) {
+    ef = (float)e;
+    omef = (float)(1.0 - e);
+    a1f = (float)(MK_A1_D / (1.0 + e));
+}
+
+__device__ __forceinline__ void kepler_sincos_f64(double M, double e, double &sinE,
+                                                  double &cosE) {
+    float ef, omef, a1f;
+    kepler_consts_f32(e, ef, omef, a1f);
+    kepler_sincos_f64(M, e, ef, omef, a1f, sinE, cosE);
 }
 
 // ------------------------------------------------------------------- PCG64

@@ -98,7 +98,7 @@ __device__ __noinline__ void posterior_one(const StarRec &st, const double *ep64
         for (int k = 0; k < L; ++k) A_out[k * L + c] = ok ? col[k] : NAN;
     }
     if (lnl_out)
-        *lnl_out = ok ? -0.5 * (acc.rWr - quad + st.log_norm_rest + log(lam0) - acc.slw + logdetG)
+        *lnl_out = ok ? -0.5 * (acc.rWr - quad + st.log_norm_rest + log(lam0) - acc.sum_log_w(st) + logdetG)
                       : INFINITY;
 }
 
@@ -134,10 +134,8 @@ __global__ void __launch_bounds__(256) unmarginalized_kernel(const StarRec *star
          i += nw) {
         const double *p = pars + i * np;
         const double P = p[0], e = p[1], om = p[2], M0 = p[3], s2 = p[4] * p[4], K = p[5];
-        double sw, cw;
-        sincos(om, &sw, &cw);
-        const double Ac = cw, Bc = -sw * sqrt((1.0 - e) * (1.0 + e)), Dc = e * cw;
-        const double k2p = TWO_PI_D / P;
+        OrbitF64 orb;
+        orb.init(P, e, om, M0);
         double acc = 0.0;
         const double *rec0 = ep64 + (size_t)st.epoch_off * REC64;
         for (int j = lane; j < st.n_epochs; j += 32) {
@@ -147,13 +145,7 @@ __global__ void __launch_bounds__(256) unmarginalized_kernel(const StarRec *star
             double y = __ldg(rec + 1);
             for (int k = 1; k < L; ++k) y += st.mu[k] * __ldg(rec + 2 + k);
             const double var = 1.0 / __ldg(rec + 2) + s2;
-            double Mn = fma(dt, k2p, -M0);
-            const double nrev = rint(Mn * INV_TWO_PI_D);
-            Mn = fma(-nrev, TWO_PI_HI_D, Mn);
-            Mn = fma(-nrev, TWO_PI_LO_D, Mn);
-            double sE, cE;
-            kepler_sincos_f64(Mn, e, sE, cE);
-            const double m = fma(Ac, cE, fma(Bc, sE, -Dc)) / (1.0 - e * cE) + Dc;
+            const double m = orb.rv_unit(dt);
             // trend polynomial in (t - t_ref of the samples), Horner
             double tr = 0.0;
             for (int k = nt - 1; k >= 0; --k) tr = fma(tr, dt, p[6 + k]);
@@ -164,6 +156,32 @@ __global__ void __launch_bounds__(256) unmarginalized_kernel(const StarRec *star
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) out[i] = acc;
     }
+}
+
+// rv[i * n_t + j] = K_i m_i(t_j - t0) for element rows (P, K, e, omega, M0):
+// one thread per (orbit, time) pair.
+__global__ void __launch_bounds__(256) rv_elements_kernel(const double *t, int n_t,
+                                                          const double *el, int64_t n, double t0,
+                                                          double *rv) {
+    const int64_t total = n * n_t;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = g / n_t;
+        const int j = (int)(g - i * n_t);
+        const double *p = el + i * 5;
+        OrbitF64 orb;
+        orb.init(p[0], p[2], p[3], p[4]);
+        rv[g] = p[1] * orb.rv_unit(t[j] - t0);
+    }
+}
+
+cudaError_t launch_rv_elements(const double *t, int n_t, const double *el, int64_t n, double t0,
+                               double *rv, cudaStream_t st) {
+    const int64_t total = n * n_t;
+    const int64_t blocks = (total + 255) / 256;
+    const unsigned grid = (unsigned)(blocks < 152 * 16 ? blocks : 152 * 16);
+    rv_elements_kernel<<<grid, 256, 0, st>>>(t, n_t, el, n, t0, rv);
+    return cudaGetLastError();
 }
 
 template <int L>
@@ -258,6 +276,17 @@ extern "C" int joker_unmarginalized_lnl(const joker_stars *stars, int star, cons
         return post_fail(JOKER_EINVAL, "joker_unmarginalized_lnl: star out of range");
     const cudaError_t e = launch_unmarginalized(recs, ep64, star, L, d_pars, n, n_trend, dt_shift,
                                                 d_out, (cudaStream_t)stream);
+    if (e != cudaSuccess) return post_fail(JOKER_ECUDA, cudaGetErrorString(e));
+    return JOKER_OK;
+}
+
+extern "C" int joker_rv_from_elements(const double *d_t, int n_t, const double *d_elems,
+                                      int64_t n, double t0, double *d_rv, void *stream) {
+    if (n < 0 || n_t < 0) return post_fail(JOKER_EINVAL, "joker_rv_from_elements: n < 0 or n_t < 0");
+    if (n == 0 || n_t == 0) return JOKER_OK;
+    if (!d_t || !d_elems || !d_rv)
+        return post_fail(JOKER_EINVAL, "joker_rv_from_elements: NULL device pointer");
+    const cudaError_t e = launch_rv_elements(d_t, n_t, d_elems, n, t0, d_rv, (cudaStream_t)stream);
     if (e != cudaSuccess) return post_fail(JOKER_ECUDA, cudaGetErrorString(e));
     return JOKER_OK;
 }

@@ -442,6 +442,26 @@ def unmarginalized_lnl(table, star, pars, n_trend, dt_shift=0.0, stream=None):
     return out
 
 
+def rv_from_elements(t, elems, t0=0.0, stream=None):
+    """Radial velocities of Keplerian orbits (joker_rv_from_elements, the
+    device counterpart of twobody's c_rv_from_elements): ``t`` (n_t,) times,
+    ``elems`` (n, 5) float64 rows P, K, e, omega, M0 (numpy or CUDA).
+    Returns an (n, n_t) CUDA tensor, row i = K_i (cos(omega_i + f) + e_i cos
+    omega_i) at M = 2 pi (t - t0) / P_i - M0_i."""
+    t = torch.as_tensor(_f64(t) if isinstance(t, np.ndarray) else t)
+    t = t.to(device="cuda", dtype=torch.float64).reshape(-1).contiguous()
+    el = torch.as_tensor(_f64(elems) if isinstance(elems, np.ndarray) else elems)
+    el = el.to(device="cuda", dtype=torch.float64).contiguous()
+    if el.dim() != 2 or el.shape[1] != 5:
+        raise ValueError("elems must have shape (n, 5): P, K, e, omega, M0")
+    n, n_t = el.shape[0], t.shape[0]
+    out = torch.empty((n, n_t), dtype=torch.float64, device="cuda")
+    nat.check(nat.lib().joker_rv_from_elements(
+        ctypes.c_void_p(t.data_ptr()), int(n_t), ctypes.c_void_p(el.data_ptr()), n, float(t0),
+        ctypes.c_void_p(out.data_ptr()), stream_handle(stream)), "joker_rv_from_elements")
+    return out
+
+
 def prior_spec(prior):
     """joker_prior_spec of a JokerPrior (or of a dict of its fields)."""
     if isinstance(prior, dict):
