@@ -155,6 +155,9 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
     r.log_kscale = r.k_scaled ? std::log(r.sigK0sq) + 2.0 / 3.0 * std::log(r.P0) : 0.0;
     r.log_maxK2 = r.k_scaled ? std::log(r.maxK2) : 0.0;
     for (int j = 0; j < L; ++j) r.lam[j] = lamk[j];
+    for (int j = 0; j < L; ++j)
+        r.ilam[j] = lamk[j] > 0.0 ? (double)(1.0L / (long double)lamk[j]) : 0.0;
+    r.iP0 = r.k_scaled ? (double)(1.0L / (long double)r.P0) : 0.0;
     for (int j = 0; j < L; ++j) r.mu[j] = muk[j];
     std::vector<long double> C(T * T, 0.0L), c(T, 0.0L), Cinv(T * T, 0.0L);
     long double Syy = 0.0L, slog_ivar = 0.0L, slog_lam = 0.0L, sw = 0.0L;

@@ -29,9 +29,9 @@ struct OrbitF64 {
     __device__ __forceinline__ void init(double P, double e_, double om, double M0_) {
         e = e_;
         M0 = M0_;
-        k2p = TWO_PI_D / P;
+        k2p = TWO_PI_D / P;                  // correctly rounded: it scales every phase
         double sw, cw;
-        sincos(om, &sw, &cw);
+        sincos_f64_table(om, sw, cw);
         Ac = cw;
         Bc = -sw * sqrt((1.0 - e) * (1.0 + e));
         Dc = e * cw;
@@ -173,22 +173,31 @@ __device__ __forceinline__ double tail_schur_d(const StarRec &st, double A00, co
         gcC = fma(A0[j], st.cC[j], gcC);
     }
     const double a_minus = A00 - gv;           // s - 1/Lambda0
-    const double s = a_minus + 1.0 / lam0;
     const double u = b0 - gcC;
     const double mu0 = st.mu0;
     const double t = fma(-mu0, a_minus, u);
     double chi2 = st.chi2_0;
     if (mu0 != 0.0) chi2 = fma(mu0 * mu0, a_minus, fma(-2.0 * mu0, u, chi2));
-    chi2 -= t * t / s;
-    const double logdet = st.logdet_const + log_lam0 + (MIXED_LOG ? log_mixed(s) : log(s));
-    return -0.5 * (chi2 + logdet);
+    if constexpr (MIXED_LOG) {
+        const double s = a_minus + 1.0 / lam0;
+        chi2 -= t * t / s;
+        return -0.5 * (chi2 + st.logdet_const + log_lam0 + log_mixed(s));
+    } else {
+        // Lambda0 s = Lambda0 (s - 1/Lambda0) + 1: t^2 / s and log Lambda0 + log s
+        // from one reciprocal and one log
+        const double ls = fma(lam0, a_minus, 1.0);
+        chi2 = fma(-t * t * lam0, rcp_newton(ls), chi2);
+        return -0.5 * (chi2 + st.logdet_const + log(ls));
+    }
 }
 
 // Full tail (jitter applied), FP64: LDL^T of G, quadratic form, log det.
+// logdet_const + log(scale * det G) is the log-determinant term.
 template <int L, bool MIXED_LOG>
 __device__ __forceinline__ double tail_full_d(const double (&G)[L][L], const double (&q)[L],
-                                              double rWr, double logdet_const) {
-    double D[L], Lw[L][L];
+                                              double rWr, double logdet_const,
+                                              double scale = 1.0) {
+    double D[L], rD[L], Lw[L][L];
     double quad = 0.0, detp = 1.0;
 #pragma unroll
     for (int k = 0; k < L; ++k) {
@@ -196,7 +205,8 @@ __device__ __forceinline__ double tail_full_d(const double (&G)[L][L], const dou
 #pragma unroll
         for (int m = 0; m < k; ++m) dk = fma(-Lw[k][m] * Lw[k][m], D[m], dk);
         D[k] = dk;
-        const double rdk = 1.0 / dk;
+        const double rdk = rcp_newton(dk);
+        rD[k] = rdk;
 #pragma unroll
         for (int i = k + 1; i < L; ++i) {
             double v = G[i][k];
@@ -213,16 +223,17 @@ __device__ __forceinline__ double tail_full_d(const double (&G)[L][L], const dou
 #pragma unroll
         for (int m = 0; m < k; ++m) v = fma(-Lw[k][m], z[m], v);
         z[k] = v;
-        quad = fma(v * v, 1.0 / D[k], quad);
+        quad = fma(v * v, rD[k], quad);
     }
-    const double logdet = logdet_const + (MIXED_LOG ? log_mixed(detp) : log(detp));
+    const double logdet = logdet_const + (MIXED_LOG ? log_mixed(detp) : log(scale * detp));
     return -0.5 * (rWr - quad + logdet);
 }
 
 // K prior variance per sample (fast_likelihood.pyx:461-464)
 __device__ __forceinline__ double k_prior_variance(const StarRec &st, double P, double e) {
     if (!st.k_scaled) return st.lam0;
-    const double v = st.sigK0sq / (1.0 - e * e) * pow(P / st.P0, -2.0 / 3.0);
+    const double y = rcbrt_newton(P * st.iP0);                  // (P / P0)^(-1/3)
+    const double v = st.sigK0sq * (y * y) * rcp_newton(1.0 - e * e);
     return fmin(st.maxK2, v);
 }
 
@@ -230,16 +241,22 @@ template <int L, bool JIT>
 __device__ __forceinline__ double Acc64<L, JIT>::finish(const StarRec &st, double P) const {
     const double lam0 = k_prior_variance(st, P, orb.e);
     if constexpr (!JIT) {
-        return tail_schur_d<L, false>(st, A00, A0, b0, lam0, log(lam0));
+        return tail_schur_d<L, false>(st, A00, A0, b0, lam0, 0.0);
     } else {
         double Gs[L][L];
+        const double ilam0 = st.k_scaled ? rcp_newton(lam0) : st.ilam[0];
 #pragma unroll
         for (int ii = 0; ii < L; ++ii) {
 #pragma unroll
             for (int k = 0; k <= ii; ++k) { Gs[ii][k] = G[ii][k]; Gs[k][ii] = G[ii][k]; }
-            Gs[ii][ii] += 1.0 / (ii == 0 ? lam0 : st.lam[ii]);
+            Gs[ii][ii] += ii == 0 ? ilam0 : st.ilam[ii];
         }
-        return tail_full_d<L, false>(Gs, q, rWr, st.log_norm_rest + log(lam0) - sum_log_w(st));
+        // log det term: log_norm_rest + log Lambda0 - sum log w + log det G, with
+        // -sum log w = -sum log ivar + slog + ej ln 2 + log pj
+        return tail_full_d<L, false>(
+            Gs, q, rWr,
+            fma((double)ej, 0.69314718055994530942, st.log_norm_rest - st.sum_log_ivar + slog),
+            lam0 * pj);
     }
 }
 

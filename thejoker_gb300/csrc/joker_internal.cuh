@@ -37,6 +37,8 @@ struct alignas(16) StarRec {
     double mu[MAXL];            // prior means (mu[0] = mu0)
     double log_norm_rest;       // N log 2pi + sum_{j>=1} log lambda_j
     double sum_log_ivar;        // sum log ivar
+    double ilam[MAXL];          // 1 / lambda_j (j >= 1; j = 0 when the K prior is not scaled)
+    double iP0;                 // 1 / P0 of the scaled K prior
     // float-float copies for the mixed kernel's tail
     float chi2_0_hi, chi2_0_lo;
     float cC_hi[MAXL], cC_lo[MAXL];

@@ -190,7 +190,47 @@ __device__ __forceinline__ void kepler_sincos_f64(double M, double e, float ef, 
 __device__ __forceinline__ void kepler_consts_f32(double e, float &ef, float &omef, float &a1f) {
     ef = (float)e;
     omef = (float)(1.0 - e);
-    a1f = (float)(MK_A1_D / (1.0 + e));
+    a1f = (float)MK_A1_D * fast_rcp(1.0f + ef);
+}
+
+// sin and cos of a double angle a to about an ulp (for |a| up to ~1e6 rad;
+// NaN in, NaN out): a is reduced to x in [-pi, pi] with the two-part 2 pi,
+// |x| = k/128 + r with |r| <= 1/256 (exact by Sterbenz's lemma), and sin r,
+// cos r - 1 from the same Taylor series as sincos_f32arg.
+__device__ __forceinline__ void sincos_f64_table(double a, double &s, double &c) {
+    const double nrev = rint(a * INV_TWO_PI_D);
+    double x = fma(-nrev, TWO_PI_HI_D, a);
+    x = fma(-nrev, TWO_PI_LO_D, x);
+    const double ax = fabs(x);
+    int k = __float2int_rn((float)ax * 128.0f);
+    k = min(max(k, 0), SINCOS_TAB_N - 1);
+    const double r = fma((double)k, -0.0078125, ax);
+    const double2 t = __ldg(&kSinCos128[k]);
+    const double r2 = r * r;
+    const double sr = fma(r * r2, fma(r2, 1.0 / 120.0, -1.0 / 6.0), r);
+    const double cm1 = r2 * fma(r2, 1.0 / 24.0, -0.5);
+    const double sa = fma(t.x, cm1, fma(t.y, sr, t.x));
+    c = fma(t.y, cm1, fma(-t.x, sr, t.y));
+    s = (x < 0.0) ? -sa : sa;
+}
+
+// x^(-1/3) (other x: the library pow).  For a positive normal x = v 2^(3q), v in [1, 8)
+// (integer exponent arithmetic), an FP32 estimate of v^(-1/3) is refined by
+// two Newton-Raphson steps on f(y) = y^-3 - v, y <- y (4 - v y^3) / 3, each
+// of which squares the relative error (2^-21 -> 2^-41 -> below rounding);
+// the result is y 2^-q.
+__device__ __forceinline__ double rcbrt_newton(double x) {
+    const int hi = __double2hiint(x);
+    const int ex = ((hi >> 20) & 0x7ff) - 1023;
+    if (hi < 0 || ex == -1023 || ex == 1024) return pow(x, -1.0 / 3.0);   // <= 0, subnormal, inf, NaN
+    const int q = (ex + 3072) / 3 - 1024;                 // floor(ex / 3)
+    const int rr = ex - 3 * q;                             // 0, 1, 2
+    const double v = __hiloint2double((hi & 0x000fffff) | ((rr + 1023) << 20),
+                                      __double2loint(x));
+    double y = (double)exp2f(-0.33333334f * __log2f((float)v));
+    y = y * (fma(-v, y * y * y, 4.0) * (1.0 / 3.0));
+    y = y * (fma(-v, y * y * y, 4.0) * (1.0 / 3.0));
+    return y * __hiloint2double((1023 - q) << 20, 0);
 }
 
 __device__ __forceinline__ void kepler_sincos_f64(double M, double e, double &sinE,
