@@ -132,3 +132,19 @@ def test_oracle_rv_matches_40_digit_values(golden_dir):
     chunk = np.stack([el[:, 0], el[:, 2], el[:, 3], el[:, 4], np.zeros(len(el))], axis=1)
     m = oracle.rv_unit(z["t"], float(z["t0"]), chunk)
     assert np.all(np.abs(m - z["m_hp"]) <= 8.0 * scale)
+
+
+def test_sincos_table_is_correctly_rounded():
+    """The committed table of the FP64 Kepler solver
+    (thejoker_gb300/csrc/joker_sincos_table.cuh, written by
+    gen_sincos_table.py): sin and cos of k/128 within an ulp of numpy's."""
+    import re
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "thejoker_gb300", "csrc", "joker_sincos_table.cuh")
+    text = open(path).read()
+    pairs = re.findall(r"\{(-?0x[0-9a-fp.+-]+), (-?0x[0-9a-fp.+-]+)\},", text)
+    assert len(pairs) == 404
+    for k, (s, c) in enumerate(pairs):
+        a = k / 128.0
+        for got, want in ((float.fromhex(s), np.sin(a)), (float.fromhex(c), np.cos(a))):
+            assert abs(got - want) <= np.spacing(abs(want)) + 1e-300
