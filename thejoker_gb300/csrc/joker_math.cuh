@@ -97,8 +97,8 @@ __device__ __forceinline__ void kepler_sincos_f32(float M, float e, float ome, f
 }
 
 // ----------------------------------------------------------------- FP64 Kepler
-// On this GPU an FP64 instruction costs as much issue time as about 64 FP32
-// ones, so the FP64 solver does in FP64 only what needs FP64 resolution: the
+// This GPU's FP64 throughput is about 1/74 of its FP32 throughput (measured
+// FMA rates), so the FP64 solver does in FP64 only what needs FP64 resolution: the
 // starter is FP32, sin and cos come from a table plus short Taylor series,
 // and the reciprocals from Newton's iteration.
 
