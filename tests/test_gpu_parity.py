@@ -227,3 +227,25 @@ def test_mixed_bound_holds_on_many_samples(cuda, n_ep, poly, noff, jitter):
               np.abs(got[0] - ref64)[near].max(), "median bound near max",
               np.median(err[0][near]))
         assert ok, ratio
+
+
+@pytest.mark.parametrize("jitter", ["reference", "applied"])
+def test_fp64_extreme_elements(cuda, jitter):
+    """Periods over 2 d .. 1e7 d (P / P0 across 22 binary exponents of the
+    scaled K prior's (P / P0)^(-2/3)), omega and M0 well outside [0, 2 pi),
+    eccentricities up to 0.9999: the FP64 path against the oracle at 1e-9,
+    and the mixed path within its per-sample bound."""
+    rng = np.random.default_rng(31)
+    st = synth_star(rng, 33)
+    ch = synth_chunk(rng, 1 << 14, P_min=2.0, P_max=1e7, jitter=True)
+    ch[:, 2] = rng.uniform(-30.0, 30.0, len(ch))
+    ch[:, 3] = rng.uniform(-30.0, 30.0, len(ch))
+    ch[::7, 1] = 1.0 - 10.0 ** rng.uniform(-4, -1, len(ch[::7]))
+    ch[::11, 1] = 0.0
+    table = _table([st], jitter=jitter)
+    ref = oracle_lnl(st, ch, jitter=jitter == "applied")
+    got64 = _lnl(table, ch, "fp64")[0]
+    assert rel_err(got64, ref).max() <= 1e-9
+    got, err = _lnl(table, ch, "mixed", with_err=True)
+    ok, ratio = within_bound(got[0], err[0], got64)
+    assert ok, f"largest |mixed - FP64| / bound {ratio:.3g}"
