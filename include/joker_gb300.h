@@ -149,6 +149,15 @@ int joker_cache_destroy(joker_cache *cache);
  * Replaces the staging of batch_marginal_ln_likelihood's chunk
  * (fast_likelihood.pyx:428-451) for callers that keep it pinned. */
 int joker_cache_create_view(joker_cache **out, const double *chunk, int64_t n);
+/* The same view over five separate FP64 columns of n samples each (P, e,
+ * omega, M0, s in the reference's internal units), for callers that hold
+ * the prior samples column by column (JokerSamples keeps one array per
+ * parameter, samples.py:404-445, which pack() interleaves into the chunk of
+ * fast_likelihood.pyx:428).  Each column may be device memory or pinned host
+ * memory and must outlive the view; s is read only with the jitter applied
+ * but must be given. */
+int joker_cache_bind(joker_cache **out, const double *P, const double *e, const double *omega,
+                     const double *M0, const double *s, int64_t n);
 int joker_cache_load(joker_cache *cache, const double *d_chunk, int64_t n,
                      int64_t row0, void *stream);
 int64_t joker_cache_capacity(const joker_cache *cache);

@@ -1,8 +1,8 @@
 """Cache views (GB300 only): the mixed kernel reading the reference's packed
-(S, 5) chunk directly -- from device memory or from pinned host memory over
-the host link -- gives bit-identical ln L, error bounds and accepted samples
-to the prepared device cache, and the zero-copy host pipeline equals the
-staged one."""
+(S, 5) chunk directly, or five separate columns (joker_cache_bind) -- from
+device memory or from pinned host memory over the host link -- gives
+bit-identical ln L, error bounds and accepted samples to the prepared device
+cache, and the zero-copy host pipeline equals the staged one."""
 import numpy as np
 import pytest
 import torch
@@ -39,8 +39,13 @@ def test_view_equals_cache(cuda, jitter, poly, precision):
     ref = _lnl(table, dev.PriorCache.from_samples(chunk), S, precision)
     d_chunk = torch.from_numpy(chunk).cuda()
     h_chunk = torch.from_numpy(chunk).pin_memory()
-    for src in (d_chunk, h_chunk):
-        got = _lnl(table, dev.PriorCache.view(src), S, precision)
+    caches = [dev.PriorCache.view(d_chunk), dev.PriorCache.view(h_chunk)]
+    # the column form (joker_cache_bind), device and pinned host columns
+    d_cols = [d_chunk[:, k].contiguous() for k in range(5)]
+    h_cols = [torch.from_numpy(np.ascontiguousarray(chunk[:, k])).pin_memory() for k in range(5)]
+    caches += [dev.PriorCache.bind(*d_cols), dev.PriorCache.bind(*h_cols)]
+    for cache in caches:
+        got = _lnl(table, cache, S, precision)
         for a, b in zip(ref, got):
             if a is not None:
                 np.testing.assert_array_equal(a, b)
@@ -75,6 +80,29 @@ def test_view_refined_accept_and_errors(cuda):
         view.load(torch.from_numpy(chunk[:10]).cuda())
     with pytest.raises(ValueError):
         dev.PriorCache.view(torch.from_numpy(chunk))            # pageable CPU tensor
+    cols = [torch.from_numpy(np.ascontiguousarray(chunk[:, k])).cuda() for k in range(5)]
+    with pytest.raises(ValueError):
+        dev.PriorCache.bind(*cols[:4], cols[4][:-1])            # ragged columns
+    with pytest.raises(ValueError):
+        dev.PriorCache.bind(*cols[:4], torch.from_numpy(chunk[:, 4].copy()))   # pageable
+    from thejoker_gb300 import _native as nat
+    from thejoker_gb300._native import JokerError
+    import ctypes
+    h = ctypes.c_void_p()
+    with pytest.raises(JokerError):
+        nat.check(nat.lib().joker_cache_bind(ctypes.byref(h), ctypes.c_void_p(cols[0].data_ptr()),
+                                             None, None, None, None, S), "joker_cache_bind")
+    # a bound cache feeds the refined acceptance like the others
+    bound = dev.PriorCache.bind(*cols)
+    out = torch.empty((1, S), dtype=torch.float64, device="cuda")
+    err = torch.empty((1, S), dtype=torch.float32, device="cuda")
+    bk = dev.MaxKeys(2)
+    dev.lnl(table, bound, out, precision="mixed", err=err, bound_keys=bk)
+    st, inc = dev.pcg64_state(np.random.default_rng(3))
+    seg = dict(lnl_off=0, n=S, idx_base=0, out_off=0, max_out=S, max_slot=0, star=0, row0=0,
+               pcg=(st, inc, 0))
+    idx, _, cnt, _, _ = dev.accept_refined(table, bound, out.view(-1), err.view(-1), bk, [seg])
+    np.testing.assert_array_equal(idx[:int(cnt[0])].cpu().numpy(), res[0][1])
 
 
 def test_zero_copy_pipeline_equals_staged(cuda):

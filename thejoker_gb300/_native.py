@@ -25,7 +25,7 @@ JOKER_MAX_LINEAR = 6
 EXPORTED = (
     "joker_abi_version", "joker_last_error", "joker_stars_create", "joker_stars_destroy",
     "joker_stars_info", "joker_stars_create_slots", "joker_stars_set", "joker_cache_create", "joker_cache_destroy", "joker_cache_load",
-    "joker_cache_create_view",
+    "joker_cache_create_view", "joker_cache_bind",
     "joker_cache_capacity", "joker_batch_marginal_ln_likelihood", "joker_lnl",
     "joker_key_to_double", "joker_accept_workspace", "joker_accept", "joker_accept_refined",
     "joker_refine_max", "joker_iter_create", "joker_iter_destroy", "joker_iter_round",
@@ -110,6 +110,7 @@ _SIGS = {
                                         ctypes.POINTER(ctypes.c_uint64), _vp]),
     "joker_iter_set_round_budget": (ctypes.c_int, [_vp, _i64]),
     "joker_cache_create_view": (ctypes.c_int, [ctypes.POINTER(_vp), _vp, _i64]),
+    "joker_cache_bind": (ctypes.c_int, [ctypes.POINTER(_vp), _vp, _vp, _vp, _vp, _vp, _i64]),
     "joker_prior_sample": (ctypes.c_int, [_vp, _i64, _i64, ctypes.POINTER(PriorSpec), ctypes.c_uint64,
                                           _i64, _vp, _vp]),
     "joker_linear_posterior": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _i64, ctypes.c_int,

@@ -496,35 +496,70 @@ extern "C" int joker_prior_sample(joker_cache *c, int64_t row0, int64_t n,
 // the device reads through its mapped address (every ln L call then streams
 // 40 bytes per sample over the host link).  Pageable host memory is taken
 // only where the device can address it (cudaDevAttrPageableMemoryAccess).
-extern "C" int joker_cache_create_view(joker_cache **out, const double *chunk, int64_t n) {
-    if (!out) return fail(JOKER_EINVAL, "joker_cache_create_view: out is NULL");
-    *out = nullptr;
-    if (!chunk || n <= 0) return fail(JOKER_EINVAL, "joker_cache_create_view: empty chunk");
-    if (((uintptr_t)chunk) % 8) return fail(JOKER_EINVAL, "joker_cache_create_view: chunk not 8-byte aligned");
+// The device address through which a kernel reads caller memory p: p itself
+// for device or managed memory and on systems with pageable-memory access, the
+// mapped address for pinned host memory.
+static int device_view_ptr(const double *p, const double **dptr, const char *who) {
+    if (((uintptr_t)p) % 8) return fail(JOKER_EINVAL, "%s: pointer not 8-byte aligned", who);
     cudaPointerAttributes at;
-    CUDA_TRY(cudaPointerGetAttributes(&at, chunk));
-    const double *dptr = nullptr;
+    CUDA_TRY(cudaPointerGetAttributes(&at, p));
     if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
-        dptr = chunk;
+        *dptr = p;
     } else if (at.type == cudaMemoryTypeHost) {
         void *d = nullptr;
-        CUDA_TRY(cudaHostGetDevicePointer(&d, const_cast<double *>(chunk), 0));
-        dptr = (const double *)d;
+        CUDA_TRY(cudaHostGetDevicePointer(&d, const_cast<double *>(p), 0));
+        *dptr = (const double *)d;
     } else {
         int dev = 0, pageable = 0;
         CUDA_TRY(cudaGetDevice(&dev));
         CUDA_TRY(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
         if (!pageable)
-            return fail(JOKER_EINVAL, "joker_cache_create_view: host memory must be pinned "
-                                      "(cudaHostAlloc / cudaHostRegister) on this system");
-        dptr = chunk;
+            return fail(JOKER_EINVAL, "%s: host memory must be pinned (cudaHostAlloc / "
+                                      "cudaHostRegister) on this system", who);
+        *dptr = p;
     }
+    return JOKER_OK;
+}
+
+extern "C" int joker_cache_create_view(joker_cache **out, const double *chunk, int64_t n) {
+    if (!out) return fail(JOKER_EINVAL, "joker_cache_create_view: out is NULL");
+    *out = nullptr;
+    if (!chunk || n <= 0) return fail(JOKER_EINVAL, "joker_cache_create_view: empty chunk");
+    const double *dptr = nullptr;
+    const int rc = device_view_ptr(chunk, &dptr, "joker_cache_create_view");
+    if (rc != JOKER_OK) return rc;
     joker_cache *c = new joker_cache();
     c->cap = n;
     c->view = true;
     c->stride = 5;
     c->P = const_cast<double *>(dptr);
     c->E = c->P + 1; c->OM = c->P + 2; c->M0 = c->P + 3; c->S = c->P + 4;
+    *out = c;
+    return JOKER_OK;
+}
+
+extern "C" int joker_cache_bind(joker_cache **out, const double *P, const double *e,
+                                const double *omega, const double *M0, const double *s,
+                                int64_t n) {
+    if (!out) return fail(JOKER_EINVAL, "joker_cache_bind: out is NULL");
+    *out = nullptr;
+    if (n <= 0) return fail(JOKER_EINVAL, "joker_cache_bind: n must be > 0");
+    if (!P || !e || !omega || !M0 || !s) return fail(JOKER_EINVAL, "joker_cache_bind: NULL column");
+    const double *cols[5] = {P, e, omega, M0, s};
+    const double *d[5];
+    for (int k = 0; k < 5; ++k) {
+        const int rc = device_view_ptr(cols[k], &d[k], "joker_cache_bind");
+        if (rc != JOKER_OK) return rc;
+    }
+    joker_cache *c = new joker_cache();
+    c->cap = n;
+    c->view = true;
+    c->stride = 1;
+    c->P = const_cast<double *>(d[0]);
+    c->E = const_cast<double *>(d[1]);
+    c->OM = const_cast<double *>(d[2]);
+    c->M0 = const_cast<double *>(d[3]);
+    c->S = const_cast<double *>(d[4]);
     *out = c;
     return JOKER_OK;
 }

@@ -198,6 +198,32 @@ class PriorCache:
         self._chunk = chunk
         return self
 
+    @classmethod
+    def bind(cls, P, e, omega, M0, s):
+        """A cache over five float64 columns without a copy (joker_cache_bind):
+        1-D tensors of one length, each CUDA or pinned CPU, in the reference's
+        internal units.  The view keeps references to the columns."""
+        cols = (P, e, omega, M0, s)
+        if not all(isinstance(c, torch.Tensor) for c in cols):
+            raise TypeError("joker_cache_bind takes torch tensors (CUDA, or pinned CPU)")
+        n = int(P.shape[0]) if P.dim() == 1 else -1
+        for c in cols:
+            if c.dtype != torch.float64 or c.dim() != 1 or c.shape[0] != n or \
+                    not c.is_contiguous():
+                raise ValueError("columns must be contiguous 1-D float64 tensors of one length")
+            if not c.is_cuda and not c.is_pinned():
+                raise ValueError("a CPU column must be pinned (tensor.pin_memory())")
+        torch.cuda.init()
+        self = cls.__new__(cls)
+        h = ctypes.c_void_p()
+        nat.check(nat.lib().joker_cache_bind(ctypes.byref(h),
+                                             *[ctypes.c_void_p(c.data_ptr()) for c in cols], n),
+                  "joker_cache_bind")
+        self._h = h
+        self.capacity = self.size = n
+        self._chunk = cols
+        return self
+
     def close(self):
         if getattr(self, "_h", None) is not None:
             nat.lib().joker_cache_destroy(self._h)
