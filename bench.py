@@ -244,13 +244,16 @@ def run_ours(args, rank, world, dist):
     barrier()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
+    from thejoker_gb300 import _native as nat
     with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
         barrier()
+        launches0 = nat.lib().joker_launch_count()
         t0.record()
         for _ in range(args.steps):
             step()
         t1.record()
         barrier()
+        launches = nat.lib().joker_launch_count() - launches0
     ms = t0.elapsed_time(t1) / args.steps
     if world == 1:
         lnl_ms.append(runner.lnl_ms())
@@ -350,7 +353,7 @@ def run_ours(args, rank, world, dist):
         "fp64": {"value": S64 * world / (fp64_ms * 1e-3), "unit": "samples/s",
                  "samples": S64, "ms_per_step": fp64_ms},
         "accepted_per_step": n_acc,
-        "gpu_launches": 6 * args.steps,
+        "gpu_launches": int(launches),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak,
                      "traffic": args.traffic if args.traffic else DRAM_BYTES_PER_SAMPLE * S,

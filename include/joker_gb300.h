@@ -91,6 +91,10 @@ typedef struct {
 
 int joker_abi_version(void);
 const char *joker_last_error(void);
+/* Kernels this library has launched since it was loaded, counted on the host
+ * at each launch (all devices, all threads).  A CUDA graph that captured
+ * launches replays them without counting.  No counterpart in the reference. */
+uint64_t joker_launch_count(void);
 
 /* ---- star table -----------------------------------------------------------
  * Mirrors CJokerHelper.__init__ (fast_likelihood.pyx:125-253) for n_stars

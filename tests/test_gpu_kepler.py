@@ -104,3 +104,15 @@ def test_rv_edge_inputs(cuda):
     with pytest.raises(JokerError):
         nat.check(nat.lib().joker_rv_from_elements(None, -1, None, 1, 0.0, None, None),
                   "joker_rv_from_elements")
+
+
+def test_launch_counter(cuda):
+    """joker_launch_count counts the library's kernel launches on the host."""
+    from thejoker_gb300 import _native as nat
+    from thejoker_gb300 import device as dev
+    el = np.array([[10.0, 2.0, 0.3, 0.3, 0.0]])
+    c0 = nat.lib().joker_launch_count()
+    dev.rv_from_elements(np.linspace(0, 5, 7), el)
+    assert nat.lib().joker_launch_count() - c0 == 1
+    dev.rv_from_elements(np.zeros(0), el)                       # empty: no launch
+    assert nat.lib().joker_launch_count() - c0 == 1

@@ -23,7 +23,8 @@ JOKER_MAX_LINEAR = 6
 
 # every extern "C" symbol of include/joker_gb300.h
 EXPORTED = (
-    "joker_abi_version", "joker_last_error", "joker_stars_create", "joker_stars_destroy",
+    "joker_abi_version", "joker_last_error", "joker_launch_count", "joker_stars_create",
+    "joker_stars_destroy",
     "joker_stars_info", "joker_stars_create_slots", "joker_stars_set", "joker_cache_create", "joker_cache_destroy", "joker_cache_load",
     "joker_cache_create_view", "joker_cache_bind",
     "joker_cache_capacity", "joker_batch_marginal_ln_likelihood", "joker_lnl",
@@ -67,6 +68,7 @@ _lp = ctypes.POINTER(ctypes.c_int64)
 _SIGS = {
     "joker_abi_version": (ctypes.c_int, []),
     "joker_last_error": (ctypes.c_char_p, []),
+    "joker_launch_count": (ctypes.c_uint64, []),
     "joker_stars_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int, _lp,
                                           _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int]),
     "joker_stars_destroy": (ctypes.c_int, [_vp]),

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <atomic>
 #include "joker_internal.cuh"
 
 namespace joker {
@@ -69,7 +70,12 @@ struct joker_cache {
 namespace joker {
 // lets the other translation units report through joker_last_error()
 void set_last_error(const char *msg) { g_err = msg; }
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 }  // namespace joker
+
+extern "C" uint64_t joker_launch_count(void) { return (uint64_t)joker::g_launches.load(); }
 
 extern "C" int joker_abi_version(void) { return JOKER_ABI_VERSION; }
 extern "C" const char *joker_last_error(void) { return g_err.c_str(); }

@@ -461,6 +461,7 @@ static cudaError_t launch_fp64_words(int mode, const AcceptArgs &a, int64_t tota
     const unsigned lgrid = 152 * 4;
     if (mode == 0) accept_fp64_list_kernel<0><<<lgrid, 256, 0, st>>>(a);
     else accept_fp64_list_kernel<1><<<lgrid, 256, 0, st>>>(a);
+    count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int64_t n_words = total_blocks * ACC_THREADS;
@@ -468,6 +469,7 @@ static cudaError_t launch_fp64_words(int mode, const AcceptArgs &a, int64_t tota
     const unsigned grid = (unsigned)((threads + 127) / 128);
     if (mode == 0) accept_fp64_words_kernel<0><<<grid, 128, 0, st>>>(a, n_words);
     else accept_fp64_words_kernel<1><<<grid, 128, 0, st>>>(a, n_words);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -476,6 +478,7 @@ cudaError_t launch_refine_max(const AcceptArgs &a, int64_t total_blocks, cudaStr
     cudaError_t e = cudaMemsetAsync(a.flag_count, 0, 2 * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
     accept_candidates_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
+    count_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_fp64_words(0, a, total_blocks, st);
@@ -493,6 +496,7 @@ cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_
             (e = cudaMemsetAsync(a.flag_count + 1, 0, sizeof(unsigned long long), st)) != cudaSuccess)
             return e;
         accept_mark_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
+        count_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         if (a.err != nullptr) {
@@ -501,9 +505,11 @@ cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_
         }
     }
     accept_scan_kernel<<<a.n_segs, ACC_THREADS, 0, st>>>(a);
+    count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || total_blocks == 0) return e;
     accept_emit_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
+    count_launch();
     return cudaGetLastError();
 }
 

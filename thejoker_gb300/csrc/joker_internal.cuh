@@ -8,6 +8,9 @@
 namespace joker {
 
 constexpr int MAXL = JOKER_MAX_LINEAR;
+
+// Host-side count of the kernels this library has launched (joker_launch_count).
+void count_launch();
 constexpr int TILE = 256;          // epochs staged in shared memory at a time
 constexpr int REC32 = 20;          // floats per epoch record of the mixed kernel
 constexpr int REC64 = 8;           // doubles per epoch record of the FP64 kernel

@@ -430,6 +430,7 @@ extern "C" int joker_iter_admit(joker_iter *it, int slot, int64_t budget, int n_
     iter_admit_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(
         it->p, it->max_key, it->bound_key, slot, budget, n_requested, init_batch, pool_off,
         pcg_state[0], pcg_state[1], pcg_state[2], pcg_state[3]);
+    count_launch();
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
     return JOKER_OK;
@@ -504,6 +505,7 @@ extern "C" int joker_iter_round(joker_iter *it, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     const bool mixed = it->precision != JOKER_FP64;
     iter_plan_kernel<<<1, 1024, 0, st>>>(it->p, mixed ? 1 : 0);
+    count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
     // ln L over the planned items
@@ -569,6 +571,7 @@ extern "C" int joker_iter_round(joker_iter *it, void *stream) {
     if ((e = launch_accept(c, grid, st, false)) != cudaSuccess)
         return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
     iter_update_kernel<<<(n_stars + 255) / 256, 256, 0, st>>>(it->p);
+    count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
     return JOKER_OK;
 }

@@ -174,6 +174,7 @@ cudaError_t launch_prepare(const double *chunk, int64_t n, int64_t row0, double 
     if (blocks > 152 * 16) blocks = 152 * 16;
     prepare_cache_kernel<<<(int)blocks, 256, 0, st>>>(chunk, n, row0, P, E, OM, M0, S, mx_a, mx_b,
                                                       mx_s2);
+    count_launch();
     return cudaGetLastError();
 }
 

@@ -697,6 +697,7 @@ inline cudaError_t launch_persistent(K kern, const LnlArgs &a, int block, cudaSt
     if (!a.n_items_dev && grid > a.n_items) grid = a.n_items;
     if (grid < 1) return cudaSuccess;
     kern<<<grid, block, 0, st>>>(a);
+    count_launch();
     return cudaGetLastError();
 }
 

@@ -181,6 +181,7 @@ cudaError_t launch_rv_elements(const double *t, int n_t, const double *el, int64
     const int64_t blocks = (total + 255) / 256;
     const unsigned grid = (unsigned)(blocks < 152 * 16 ? blocks : 152 * 16);
     rv_elements_kernel<<<grid, 256, 0, st>>>(t, n_t, el, n, t0, rv);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -194,6 +195,7 @@ static cudaError_t launch_posterior_L(const StarRec *stars, const double *ep64, 
     const unsigned grid = (unsigned)((warps + 7) / 8);
     posterior_kernel<L><<<grid, 256, 0, st>>>(stars, ep64, star, P, E, OM, M0, S, stride, rows,
                                               n, jit, k_clip, a, A, lnl);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -219,6 +221,7 @@ cudaError_t launch_unmarginalized(const StarRec *stars, const double *ep64, int 
     const int64_t warps = n < 152 * 8 * 4 ? n : 152 * 8 * 4;
     const unsigned grid = (unsigned)((warps + 7) / 8);
     unmarginalized_kernel<<<grid, 256, 0, st>>>(stars, ep64, star, L, pars, n, nt, dt_shift, out);
+    count_launch();
     return cudaGetLastError();
 }
 

@@ -143,6 +143,7 @@ cudaError_t launch_prior_sample(const joker_prior_spec &spec, uint64_t seed, int
     if (blocks > 152 * 16) blocks = 152 * 16;
     prior_sample_kernel<<<(int)blocks, 256, 0, st>>>(spec, seed, first_index, n, row0, P, E, OM,
                                                      M0, S, mx_a, mx_b, mx_s2, packed, bad);
+    count_launch();
     return cudaGetLastError();
 }
 
