@@ -407,12 +407,15 @@ def run_batched(args, rank, world):
     for _ in range(args.warmup):
         br.run()
     torch.cuda.synchronize()
+    from thejoker_gb300 import _native as nat
     with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        launches0 = nat.lib().joker_launch_count()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             br.run()
         torch.cuda.synchronize()
         ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        launches = nat.lib().joker_launch_count() - launches0
     counts, _, _ = br.results()
     # mixed vs FP64 on the same subset
     sub = args.subset_stars
@@ -446,6 +449,7 @@ def run_batched(args, rank, world):
                    "speedup_mixed_vs_fp64": res["fp64"][0] / res["mixed"][0],
                    "accept_counts_identical": same},
         "accepted_total": int(counts.sum()),
+        "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
 
@@ -699,17 +703,20 @@ def run_small(args, rank, world):
     chunk = fill_prior_cache(np.empty((S, 5)), 0)
     cache = dev.PriorCache.from_samples(chunk)
     table = dev.StarTable([star])
+    from thejoker_gb300 import _native as nat
     res = {}
     for prec in ("fp64", "mixed"):
         br = BatchRejection(table, cache, precision=prec, max_out=S, seeds=[1])
         for _ in range(args.warmup):
             br.run()
         torch.cuda.synchronize()
+        launches0 = nat.lib().joker_launch_count()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             br.run()
         torch.cuda.synchronize()
         ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        launches = nat.lib().joker_launch_count() - launches0
         counts, idx, ll = br.results()
         res[prec] = (ms, idx[0], br.lnl[0, :S].cpu().numpy(), ll[0])
     d = np.abs(res["mixed"][2] - res["fp64"][2])
@@ -725,6 +732,7 @@ def run_small(args, rank, world):
         "config": {"workload": f"1 star x {N} epochs over 1000 d, prior cache 2^"
                                f"{int(math.log2(S))} (s = 0)"},
         "fp64": {"value": S / (res["fp64"][0] * 1e-3), "ms_per_step": res["fp64"][0]},
+        "gpu_launches": int(launches),
         "max_abs_dlnl": float(d.max()), "max_abs_dlnl_within_40_of_max": float(d[near].max()),
         "max_abs_dlnl_kept": float(kept_d.max()),
         "accepted": int(len(res["fp64"][1])),
