@@ -745,6 +745,136 @@ def run_small(args, rank, world):
     return line
 
 
+def _gpu_ms(fn, reps=3, warmup=1):
+    """Mean CUDA-event time of fn() on the current stream, after warm-up."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_posterior(args, rank, world):
+    """The paths either side of the likelihood, each timed on the GPU beside a
+    CPU statement of the same work on the host cores:
+    - prior draws on the device (joker_prior_sample; JokerPrior.sample,
+      prior.py:297-407), against numpy draws of the same distributions;
+    - the linear-parameter posterior of accepted samples with one draw each
+      (joker_linear_posterior plus host draws in the reference's rng order;
+      batch_get_posterior_samples, fast_likelihood.pyx:471-545), against the
+      reference's own Cython batch_get_posterior_samples;
+    - the unmarginalized ln L (joker_unmarginalized_lnl;
+      samples.py:611-632), against NumPy over the oracle's RV model;
+    - the RV model on its own (joker_rv_from_elements; c_rv_from_elements),
+      against the oracle's C statement."""
+    import torch
+    from thejoker_gb300 import _native as nat
+    from thejoker_gb300 import build as tb
+    from thejoker_gb300 import device as dev
+    from thejoker_gb300.linear import multivariate_normal_draws
+    from oracle import build as ob, oracle, ref_cython
+    tb.build()
+    ob.build_all()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    star = make_star()
+    cores = os.cpu_count() or 1
+    out = {}
+    # ---- prior draws
+    n_pr = min(args.samples, 1 << 28)
+    cache = dev.PriorCache(n_pr)
+    spec = dict(P_min=2.0, P_max=1024.0, e_alpha=0.867, e_beta=3.03,
+                s_kind=nat.JOKER_S_LOGNORMAL, s_mu=float(np.log(0.5)), s_sigma=1.0)
+    ms = _gpu_ms(lambda: cache.sample_prior(spec, n_pr, seed=11))
+    n_cpu = 1 << 22
+    t0 = time.perf_counter()
+    fill_cache_host(np.empty((n_cpu, 5)), 5, threads=cores)
+    dt = time.perf_counter() - t0
+    out["prior_draws"] = {
+        "gpu": n_pr / (ms * 1e-3), "cpu": n_cpu / dt, "unit": "samples/s",
+        "gpu_samples": n_pr, "cpu_samples": n_cpu, "cpu_cores": cores, "cpu_kind": "port",
+        "hbm_gbs": 76 * n_pr / (ms * 1e-3) / 1e9,
+        "note": "76 B written per sample (FP64 columns + prepared mixed form); numpy draws "
+                "of the same distributions on the CPU (the reference samples through pymc)"}
+    del cache
+    torch.cuda.empty_cache()
+    # ---- linear posterior of accepted rows, one draw each
+    n_po = 1 << 20
+    chunk = fill_cache_host(np.empty((n_po, 5)), 6)
+    table = dev.StarTable([star], jitter="reference")
+    pc = dev.PriorCache.from_samples(chunk)
+    rows = torch.arange(n_po, dtype=torch.int64, device="cuda")
+    ms_dev = _gpu_ms(lambda: dev.linear_posterior(table, pc, 0, rows))
+    t0 = time.perf_counter()
+    a, A, ll = dev.linear_posterior(table, pc, 0, rows)
+    draws = multivariate_normal_draws(np.random.default_rng(3), a.cpu().numpy(),
+                                      A.cpu().numpy(), 1)
+    dt_e2e = time.perf_counter() - t0
+    n_ref = 1 << 14
+    h = ref_cython.make_helper(star["t"], star["rv"], star["ivar"], star["t_ref"],
+                               star["trend_M"], 1, 0, star["mu"], np.sqrt(star["lam"]), True,
+                               *star["k_prior"][1:]) if ref_cython.available() else None
+    if h is not None:
+        t0 = time.perf_counter()
+        h.batch_get_posterior_samples(np.ascontiguousarray(chunk[:n_ref]), 1,
+                                      np.random.default_rng(3))
+        dt_ref = time.perf_counter() - t0
+        cpu = {"cpu": n_ref / dt_ref, "cpu_rows": n_ref, "cpu_cores": 1, "cpu_kind": "reference"}
+    else:
+        cpu = {"cpu": None, "cpu_kind": "unavailable"}
+    out["linear_posterior"] = dict(
+        {"gpu_device": n_po / (ms_dev * 1e-3), "gpu_with_host_draws": n_po / dt_e2e,
+         "unit": "rows/s", "gpu_rows": n_po, "draws_shape": list(draws.shape)}, **cpu)
+    del pc, a, A, ll
+    torch.cuda.empty_cache()
+    # ---- unmarginalized ln L
+    n_un = 1 << 20
+    rng = np.random.default_rng(7)
+    pars = np.column_stack([chunk[:n_un], rng.normal(0, 30, n_un), rng.normal(0, 100, n_un)])
+    table_j = dev.StarTable([star], jitter="applied")
+    d_pars = torch.from_numpy(np.ascontiguousarray(pars)).cuda()
+    ms_un = _gpu_ms(lambda: dev.unmarginalized_lnl(table_j, 0, d_pars, 1))
+    n_c = 1 << 14
+    t0 = time.perf_counter()
+    m = oracle.rv_unit(star["t"], star["t_ref"], pars[:n_c, :5])
+    model = pars[:n_c, 5:6] * m + pars[:n_c, 6:7]
+    var = 1.0 / star["ivar"][None, :] + pars[:n_c, 4:5] ** 2
+    _ = -0.5 * np.sum(np.log(2 * np.pi * var) + (star["rv"][None, :] - model) ** 2 / var, axis=1)
+    dt_un = time.perf_counter() - t0
+    out["unmarginalized_lnl"] = {"gpu": n_un / (ms_un * 1e-3), "cpu": n_c / dt_un,
+                                 "unit": "rows/s", "gpu_rows": n_un, "cpu_rows": n_c,
+                                 "cpu_cores": 1, "cpu_kind": "port"}
+    # ---- RV model alone
+    el = np.column_stack([chunk[:, 0], rng.normal(0, 30, n_po), chunk[:, 1], chunk[:, 2],
+                          chunk[:, 3]])
+    d_el = torch.from_numpy(np.ascontiguousarray(el)).cuda()
+    d_t = torch.from_numpy(star["t"]).cuda()
+    ms_rv = _gpu_ms(lambda: dev.rv_from_elements(d_t, d_el, star["t_ref"]))
+    t0 = time.perf_counter()
+    oracle.rv_unit(star["t"], star["t_ref"], chunk[:n_c])
+    dt_rv = time.perf_counter() - t0
+    ne = len(star["t"])
+    out["rv_from_elements"] = {"gpu": n_po * ne / (ms_rv * 1e-3), "cpu": n_c * ne / dt_rv,
+                               "unit": "orbit-epochs/s", "gpu_orbits": n_po, "epochs": ne,
+                               "cpu_cores": 1, "cpu_kind": "port"}
+    return {
+        "metric": "rows/s of the paths around the likelihood (linear posterior with draws)",
+        "value": out["linear_posterior"]["gpu_with_host_draws"], "unit": "rows/s",
+        "n_gpus": world, "steps": 3, "warmup": 1, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded star and prior samples)",
+        "config": {"workload": f"1 star x {N_EPOCHS} epochs over {SPAN_D:.0f} d; prior draws "
+                               f"2^{int(math.log2(n_pr))}, posterior / unmarginalized / RV "
+                               f"rows 2^20"},
+        **out,
+    }
+
+
 def run_reference(args, rank):
     if rank != 0:
         return None
@@ -786,7 +916,8 @@ def main():
     p.add_argument("--traffic", type=float, default=None)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--config", default="single",
-                   choices=["single", "small", "batched", "iterative", "serving"])
+                   choices=["single", "small", "batched", "iterative", "serving",
+                            "posterior"])
     p.add_argument("--stars", type=int, default=None)
     p.add_argument("--n-requested", type=int, default=256)
     p.add_argument("--requests", type=int, default=20000)
@@ -800,7 +931,8 @@ def main():
     args = p.parse_args()
     if args.samples is None:
         args.samples = {"single": 1 << 28, "small": 1 << 20, "batched": 1 << 24,
-                        "iterative": 1 << 22, "serving": 1 << 28}[args.config]
+                        "iterative": 1 << 22, "serving": 1 << 28,
+                        "posterior": 1 << 27}[args.config]
     if args.stars is None:
         args.stars = {"batched": 4096, "iterative": 1024}.get(args.config, 1)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -823,6 +955,8 @@ def main():
             line = run_iterative(args, rank, world)
         elif args.config == "serving":
             line = run_serving(args, rank, world)
+        elif args.config == "posterior":
+            line = run_posterior(args, rank, world)
         else:
             line = run_ours(args, rank, world, dist)
         if dist is not None:
