@@ -9,15 +9,19 @@
 // counter-based generator: sample g's draws come from counters
 // (g_lo, g_hi, block, STREAM_TAG) under key (seed_lo, seed_hi), so every
 // sample is reproducible from (seed, g) whatever the launch shape.  Each
-// block yields two uniform doubles u = (x >> 11) 2^-53 from its two 64-bit
-// halves.  Per sample, in order: u_P, u_omega, u_M0, [one Box-Muller pair
-// for ln s], then the two gamma variates of the beta draw.
-//   P     = exp(ln P_min + u_P (ln P_max - ln P_min))
-//   omega = 2 pi u_omega,  M0 = 2 pi u_M0
+// block yields two 64-bit halves, each one uniform: a double
+// u = (x >> 11) 2^-53 for P and the angles, a float with 24 significant bits
+// for the rest.  Per sample, in order: u_P, u_omega, u_M0, [one Box-Muller
+// pair for ln s], then the two gamma variates of the beta draw.
+//   P     = exp(ln P_min + u_P (ln P_max - ln P_min))          (FP64)
+//   omega = 2 pi u_omega,  M0 = 2 pi u_M0                      (FP64)
 //   e     = X / (X + Y),  X ~ Gamma(alpha), Y ~ Gamma(beta)   (Marsaglia and
 //           Tsang, ACM TOMS 26, 2000; shape < 1 through
-//           Gamma(a) = Gamma(a + 1) U^(1/a))
-//   s     = s_value, or exp(s_mu + s_sigma z)
+//           Gamma(a) = Gamma(a + 1) U^(1/a))                   (FP32)
+//   s     = s_value, or exp(s_mu + s_sigma z)                  (FP32)
+// The beta and log-normal draws run in FP32: they are random draws whose
+// distribution FP32 rounding does not change measurably, and FP64 (1/74 of
+// the FP32 rate here) made them the bound of the kernel.
 #include "joker_internal.cuh"
 #include "joker_math.cuh"
 
@@ -44,7 +48,7 @@ __host__ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k
 // Sequential uniforms of one sample.
 struct SampleRng {
     uint32_t g_lo, g_hi, k0, k1, block;
-    double spare;
+    uint64_t spare;
     bool have_spare;
 
     __device__ void init(uint64_t seed, uint64_t g) {
@@ -53,47 +57,56 @@ struct SampleRng {
         block = 0;
         have_spare = false;
     }
-    __device__ double uniform() {
+    // the next 64-bit half of the sample's Philox stream
+    __device__ uint64_t bits() {
         if (have_spare) { have_spare = false; return spare; }
         uint32_t c[4] = {g_lo, g_hi, block++, STREAM_TAG};
         philox4x32_10(c, k0, k1);
-        const uint64_t x0 = ((uint64_t)c[1] << 32) | c[0], x1 = ((uint64_t)c[3] << 32) | c[2];
-        spare = (double)(x1 >> 11) * 0x1.0p-53;
+        spare = ((uint64_t)c[3] << 32) | c[2];
         have_spare = true;
-        return (double)(x0 >> 11) * 0x1.0p-53;
+        return ((uint64_t)c[1] << 32) | c[0];
     }
-    // standard normal (Box-Muller; the second variate of the pair is dropped)
-    __device__ double normal() {
-        double u1 = uniform();
-        const double u2 = uniform();
-        if (u1 <= 0.0) u1 = 0x1.0p-53;
-        double s, c;
-        sincospi(2.0 * u2, &s, &c);
-        return sqrt(-2.0 * log(u1)) * c;
+    __device__ double uniform() { return (double)(bits() >> 11) * 0x1.0p-53; }
+    // A uniform float in (0, 1): the 24 bits of x / 2^64 below its leading
+    // one, so the resolution follows the magnitude (down to 2^-64) and
+    // log u reaches -44 (a Box-Muller normal is not cut off at 5.8 sigma).
+    // Integer operations only.
+    __device__ float uniform_f() {
+        const uint64_t x = bits();
+        if (x == 0) return 0x1.0p-65f;
+        const int lz = __clzll(x);
+        const uint32_t m = (uint32_t)((x << lz) >> 40);
+        return __uint_as_float(((uint32_t)(126 - lz) << 23) | (m & 0x7fffffu));
     }
-    // Gamma(a, 1), a > 0; *ok = false if the rejection loop ran out of tries
-    __device__ double gamma(double a, bool *ok) {
-        const bool boost = a < 1.0;
-        const double k = boost ? a + 1.0 : a;
-        const double d = k - 1.0 / 3.0, c = 1.0 / sqrt(9.0 * d);
-        double v = 0.0;
+    // standard normal (Box-Muller in FP32; the second variate of the pair is dropped)
+    __device__ float normal_f() {
+        const float u1 = uniform_f();
+        const float u2 = uniform_f();
+        float s, c;
+        sincospif(2.0f * u2, &s, &c);
+        return sqrtf(-2.0f * logf(u1)) * c;
+    }
+    // Gamma(a, 1) in FP32, a > 0; *ok = false if the rejection loop ran out
+    // of tries
+    __device__ float gamma_f(float a, bool *ok) {
+        const bool boost = a < 1.0f;
+        const float k = boost ? a + 1.0f : a;
+        const float d = k - 1.0f / 3.0f, c = 1.0f / sqrtf(9.0f * d);
+        float v = 0.0f;
         bool got = false;
         for (int t = 0; t < GAMMA_MAX_TRIES && !got; ++t) {
-            const double x = normal();
-            const double w = 1.0 + c * x;
-            if (w <= 0.0) continue;
+            const float x = normal_f();
+            const float w = fmaf(c, x, 1.0f);
+            if (w <= 0.0f) continue;
             v = w * w * w;
-            const double u = uniform();
-            const double x2 = x * x;
-            got = (u < 1.0 - 0.0331 * x2 * x2) || (log(u) < 0.5 * x2 + d * (1.0 - v + log(v)));
+            const float u = uniform_f();
+            const float x2 = x * x;
+            got = (u < 1.0f - 0.0331f * x2 * x2) ||
+                  (logf(u) < 0.5f * x2 + d * (1.0f - v + logf(v)));
         }
         if (!got) *ok = false;
-        double g = d * v;
-        if (boost) {
-            double u = uniform();
-            if (u <= 0.0) u = 0x1.0p-53;
-            g *= pow(u, 1.0 / a);
-        }
+        float g = d * v;
+        if (boost) g *= powf(uniform_f(), 1.0f / a);
         return g;
     }
 };
@@ -111,10 +124,12 @@ __global__ void prior_sample_kernel(joker_prior_spec spec, uint64_t seed, int64_
         const double om = rng.uniform() * TWO_PI_D;
         const double m0 = rng.uniform() * TWO_PI_D;
         double s = spec.s_value;
-        if (spec.s_kind == JOKER_S_LOGNORMAL) s = exp(fma(spec.s_sigma, rng.normal(), spec.s_mu));
+        if (spec.s_kind == JOKER_S_LOGNORMAL)
+            s = (double)expf(fmaf((float)spec.s_sigma, rng.normal_f(), (float)spec.s_mu));
         bool ok = true;
-        const double x = rng.gamma(spec.e_alpha, &ok), y = rng.gamma(spec.e_beta, &ok);
-        double e = x / (x + y);
+        const float x = rng.gamma_f((float)spec.e_alpha, &ok);
+        const float y = rng.gamma_f((float)spec.e_beta, &ok);
+        double e = (double)(x / (x + y));
         if (!ok || !(e >= 0.0 && e < 1.0)) {
             atomicAdd(bad, 1);
             e = e >= 1.0 ? 0x1.fffffffffffffp-1 : (e >= 0.0 ? e : 0.0);
