@@ -352,6 +352,27 @@ int joker_unmarginalized_lnl(const joker_stars *stars, int star, const double *d
 int joker_rv_from_elements(const double *d_t, int n_t, const double *d_elems, int64_t n,
                            double t0, double *d_rv, void *stream);
 
+/* ---- one-call rejection step ----------------------------------------------
+ * For stars [star0, star0 + n_sel) over cache rows [row0, row0 + count): the
+ * ln L of every (star, sample) at `precision`, each star's maximum, and the
+ * acceptance exp(lnl - max) > u against the star's numpy PCG64 stream (pcg:
+ * n_sel x 4 {state_hi, state_lo, inc_hi, inc_lo}, positioned so that the
+ * next draw is the uniform of row row0), refined to the FP64 decisions for
+ * the mixed precisions.  Star k's kept cache rows go to d_out_idx[k * max_out
+ * ...] (ascending, at most max_out), their ln L to d_out_lnl (optional), the
+ * number kept to d_count[k].  d_work: joker_rejection_workspace(n_sel,
+ * count, max_out, precision) bytes of device memory, 256-byte aligned.
+ * Replaces, for a batch of stars, marginal_ln_likelihood_inmem plus the
+ * acceptance of rejection_sample (thejoker/likelihood_helpers.py:40-66,
+ * 107-109; thejoker/multiproc_helpers.py:63-120, 256-258): the sequence
+ * joker_lnl + joker_accept / joker_accept_refined in one call. */
+int64_t joker_rejection_workspace(int n_sel, int64_t count, int64_t max_out, int precision);
+int joker_rejection_sample(const joker_stars *stars, const joker_cache *cache, int star0,
+                           int n_sel, int64_t row0, int64_t count, int precision,
+                           const uint64_t *pcg, int64_t max_out, int64_t *d_out_idx,
+                           double *d_out_lnl, int64_t *d_count, void *d_work,
+                           int64_t work_bytes, void *stream);
+
 /* ---- acceptance without allocation ---------------------------------------
  * No counterpart in the reference.  joker_accept_noalloc is joker_accept for
  * callers that must not allocate device memory: a serving loop with

@@ -104,3 +104,55 @@ def test_autotune_records_fastest_chunk(cuda, tmp_path):
         assert BatchRejection(table, cache, max_out=4).chunk == best
     finally:
         del os.environ["JOKER_AUTOTUNE"]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_one_call_rejection_equals_engine(cuda, precision):
+    """joker_rejection_sample (ln L + maxima + acceptance in one C call) keeps
+    the same rows, counts and ln L as the BatchRejection engine, including a
+    star longer than one epoch tile."""
+    import ctypes
+    from gpu_util import synth_chunk, synth_star
+    from thejoker_gb300 import _native as nat
+    from thejoker_gb300 import device as dev
+    from thejoker_gb300._native import JokerError
+    from thejoker_gb300.batch import BatchRejection
+    rng = np.random.default_rng(17)
+    stars = [synth_star(rng, n) for n in (12, 40, 300)]
+    S, max_out, seeds = 1 << 18, 512, [11, 22, 33]
+    cache = dev.PriorCache.from_samples(synth_chunk(rng, S, jitter=True))
+    table = dev.StarTable(stars, jitter="applied")
+    counts, idx, ll = BatchRejection(table, cache, precision=precision, max_out=max_out,
+                                     seeds=seeds).run().results()
+    prec = nat.JOKER_MIXED if precision == "mixed" else nat.JOKER_FP64
+    mask = (1 << 64) - 1
+    words = []
+    for sd in seeds:
+        st, inc = dev.pcg64_state(np.random.default_rng(sd))
+        words += [st >> 64, st & mask, inc >> 64, inc & mask]
+    pcg = (ctypes.c_uint64 * len(words))(*words)
+    nbytes = nat.lib().joker_rejection_workspace(len(stars), S, max_out, prec)
+    work = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out_idx = torch.empty(len(stars) * max_out, dtype=torch.int64, device="cuda")
+    out_lnl = torch.empty(len(stars) * max_out, dtype=torch.float64, device="cuda")
+    cnt = torch.empty(len(stars), dtype=torch.int64, device="cuda")
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    nat.check(nat.lib().joker_rejection_sample(table.handle, cache.handle, 0, len(stars), 0, S,
+                                               prec, pcg, max_out, p(out_idx), p(out_lnl),
+                                               p(cnt), p(work), nbytes, stream),
+              "joker_rejection_sample")
+    got_c = cnt.cpu().numpy()
+    np.testing.assert_array_equal(got_c, counts)
+    oi = out_idx.view(len(stars), max_out).cpu().numpy()
+    ol = out_lnl.view(len(stars), max_out).cpu().numpy()
+    for k in range(len(stars)):
+        n = min(int(counts[k]), max_out)
+        np.testing.assert_array_equal(oi[k, :n], idx[k])
+        np.testing.assert_array_equal(ol[k, :n], ll[k])
+    assert counts.sum() > 0
+    with pytest.raises(JokerError):
+        nat.check(nat.lib().joker_rejection_sample(table.handle, cache.handle, 0, len(stars), 0,
+                                                   S, prec, pcg, max_out, p(out_idx), p(out_lnl),
+                                                   p(cnt), p(work), nbytes - 256, stream),
+                  "joker_rejection_sample")

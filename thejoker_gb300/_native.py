@@ -33,6 +33,7 @@ EXPORTED = (
     "joker_iter_outputs", "joker_iter_read", "joker_iter_create_pool", "joker_iter_admit",
     "joker_iter_set_round_budget", "joker_accept_noalloc", "joker_linear_posterior",
     "joker_unmarginalized_lnl", "joker_prior_sample", "joker_rv_from_elements",
+    "joker_rejection_workspace", "joker_rejection_sample",
 )
 
 
@@ -121,6 +122,10 @@ _SIGS = {
                                                 ctypes.c_double, _vp, _vp]),
     "joker_rv_from_elements": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64, ctypes.c_double,
                                               _vp, _vp]),
+    "joker_rejection_workspace": (_i64, [ctypes.c_int, _i64, _i64, ctypes.c_int]),
+    "joker_rejection_sample": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _i64, _i64,
+                                              ctypes.c_int, ctypes.POINTER(ctypes.c_uint64),
+                                              _i64, _vp, _vp, _vp, _vp, _i64, _vp]),
     "joker_accept_noalloc": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,
                                             ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
 }

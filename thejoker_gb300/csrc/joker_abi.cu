@@ -891,3 +891,92 @@ extern "C" int joker_accept_refined(const joker_stars *s, const joker_cache *c,
     CUDA_TRY(launch_accept(a, nb, st, max_given != 0));
     return JOKER_OK;
 }
+
+// ------------------------------------------------- one-call rejection step
+// The sequence the host engines run, as one entry: ln L of every (star,
+// sample), the running maxima, and the acceptance against each star's PCG64
+// stream, refined to FP64 decisions for the mixed precisions.
+static void rejection_segs(int star0, int n_sel, int64_t row0, int64_t count, int64_t max_out,
+                           const uint64_t *pcg, std::vector<joker_accept_seg> &segs) {
+    segs.assign(n_sel, joker_accept_seg{});
+    for (int k = 0; k < n_sel; ++k) {
+        joker_accept_seg &g = segs[k];
+        g.lnl_off = (int64_t)k * count;
+        g.n = count;
+        g.idx_base = row0;
+        g.out_off = (int64_t)k * max_out;
+        g.max_out = max_out;
+        g.u_off = 0;
+        if (pcg) {
+            g.pcg_state_hi = pcg[4 * k + 0];
+            g.pcg_state_lo = pcg[4 * k + 1];
+            g.pcg_inc_hi = pcg[4 * k + 2];
+            g.pcg_inc_lo = pcg[4 * k + 3];
+        }
+        g.max_slot = k;
+        g.star = star0 + k;
+        g.row0 = row0;
+    }
+}
+
+// Scratch layout: ln L (n_sel x count doubles), bounds (n_sel x count
+// floats, mixed only), 4 n_sel keys (running maxima, two bound maxima,
+// FP64 maxima), then the acceptance workspace.
+static int64_t rejection_bytes(int n_sel, int64_t count, int64_t max_out, int precision,
+                               int64_t *off_err, int64_t *off_keys, int64_t *off_acc) {
+    std::vector<joker_accept_seg> segs;
+    rejection_segs(0, n_sel, 0, count, max_out, nullptr, segs);
+    const int64_t lnl = align256(8 * (int64_t)n_sel * count);
+    const int64_t err = precision == JOKER_FP64 ? 0 : align256(4 * (int64_t)n_sel * count);
+    const int64_t keys = align256(8 * 4 * (int64_t)n_sel);
+    if (off_err) *off_err = lnl;
+    if (off_keys) *off_keys = lnl + err;
+    if (off_acc) *off_acc = lnl + err + keys;
+    return lnl + err + keys + joker_accept_workspace(segs.data(), n_sel);
+}
+
+extern "C" int64_t joker_rejection_workspace(int n_sel, int64_t count, int64_t max_out,
+                                             int precision) {
+    if (n_sel <= 0 || count <= 0 || max_out < 0) return 0;
+    return rejection_bytes(n_sel, count, max_out, precision, nullptr, nullptr, nullptr);
+}
+
+extern "C" int joker_rejection_sample(const joker_stars *s, const joker_cache *c, int star0,
+                                      int n_sel, int64_t row0, int64_t count, int precision,
+                                      const uint64_t *pcg, int64_t max_out, int64_t *d_out_idx,
+                                      double *d_out_lnl, int64_t *d_count, void *d_work,
+                                      int64_t work_bytes, void *stream) {
+    if (!s || !c) return fail(JOKER_EINVAL, "joker_rejection_sample: NULL handle");
+    if (n_sel < 0 || count < 0 || max_out < 0)
+        return fail(JOKER_EINVAL, "joker_rejection_sample: negative size");
+    if (n_sel == 0 || count == 0) return JOKER_OK;
+    if (!pcg || !d_out_idx || !d_count || !d_work)
+        return fail(JOKER_EINVAL, "joker_rejection_sample: NULL argument");
+    int64_t off_err, off_keys, off_acc;
+    const int64_t need = rejection_bytes(n_sel, count, max_out, precision, &off_err, &off_keys,
+                                         &off_acc);
+    if (work_bytes < need)
+        return fail(JOKER_EINVAL, "joker_rejection_sample: workspace %lld bytes, needs %lld",
+                    (long long)work_bytes, (long long)need);
+    if (((uintptr_t)d_work) % 256)
+        return fail(JOKER_EINVAL, "joker_rejection_sample: workspace not 256-byte aligned");
+    char *w = (char *)d_work;
+    double *lnl = (double *)w;
+    float *err = precision == JOKER_FP64 ? nullptr : (float *)(w + off_err);
+    uint64_t *keys = (uint64_t *)(w + off_keys);
+    uint64_t *max_key = keys, *bound_key = keys + n_sel, *exact_key = keys + 3 * n_sel;
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemsetAsync(keys, 0, 8 * 4 * (size_t)n_sel, st));
+    int rc = joker_lnl(s, c, star0, n_sel, row0, count, precision, lnl, count, max_key, err,
+                       bound_key, 0, 0, stream);
+    if (rc != JOKER_OK) return rc;
+    std::vector<joker_accept_seg> segs;
+    rejection_segs(star0, n_sel, row0, count, max_out, pcg, segs);
+    const int64_t acc_bytes = work_bytes - off_acc;
+    if (precision == JOKER_FP64)
+        return joker_accept(segs.data(), n_sel, lnl, max_key, JOKER_U_PCG64, nullptr, d_out_idx,
+                            d_out_lnl, d_count, w + off_acc, acc_bytes, stream);
+    return joker_accept_refined(s, c, segs.data(), n_sel, lnl, err, bound_key, exact_key, n_sel, 0,
+                                JOKER_U_PCG64, nullptr, d_out_idx, d_out_lnl, d_count, nullptr,
+                                w + off_acc, acc_bytes, stream);
+}
