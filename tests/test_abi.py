@@ -110,3 +110,18 @@ def test_workspace_size(native_lib):
     segs[1].n = 1
     ws = native_lib.joker_accept_workspace(segs, 2)
     assert ws >= 4 * 256 * 4 + 8 * 4
+
+
+def test_rejection_workspace_size(native_lib):
+    """joker_rejection_workspace is host arithmetic: ln L (8 B) and, for the
+    mixed precisions, bounds (4 B) per (star, sample), keys and the acceptance
+    workspace, each 256-byte aligned; nothing for an empty batch."""
+    from thejoker_gb300 import _native as nat
+    ws = nat.lib().joker_rejection_workspace
+    assert ws(0, 1000, 16, nat.JOKER_MIXED) == 0 and ws(3, 0, 16, nat.JOKER_MIXED) == 0
+    m = ws(3, 1 << 20, 256, nat.JOKER_MIXED)
+    f = ws(3, 1 << 20, 256, nat.JOKER_FP64)
+    assert m % 256 == 0 and f % 256 == 0
+    assert m - f == 3 * 4 * (1 << 20)                      # the FP32 bounds
+    assert f >= 3 * 8 * (1 << 20) + 4 * 8 * 3              # ln L and the keys
+    assert ws(3, 1 << 21, 256, nat.JOKER_MIXED) > m
