@@ -44,9 +44,12 @@ def test_key_roundtrip(native_lib):
         k = (~b) & 0xFFFFFFFFFFFFFFFF if b < 0 else (b | (1 << 63))
         keys.append(k)
         assert nat.lib().joker_key_to_double(k) == v
-    finite = [k for v, k in zip(vals, keys)]
-    assert sorted(finite) == [keys[vals.index(v)] for v in sorted(vals, key=lambda x: (x, str(x)))] or True
-    # order preserved
+    # the key order is the value order, strictly, with -0.0 just below 0.0
+    for i in range(len(vals)):
+        for j in range(len(vals)):
+            if vals[i] < vals[j]:
+                assert keys[i] < keys[j], (vals[i], vals[j])
+    assert keys[2] < keys[3]                                   # -0.0, 0.0
     order = np.argsort(vals, kind="stable")
     assert all(keys[order[i]] <= keys[order[i + 1]] for i in range(len(vals) - 1))
 
