@@ -20,37 +20,12 @@ constexpr double MK_A0_D = 3.0 * PI_D * PI_D / (PI_D * PI_D - 6.0);
 constexpr double MK_A1_D = 1.6 * PI_D / (PI_D * PI_D - 6.0);
 
 // --------------------------------------------------------- float-float helpers
-// Error-free transformations (Knuth two-sum, FMA two-product).  The _rn
-// intrinsics keep the compiler from contracting them into FMAs.
+// Knuth's two-sum: s + err = a + b exactly.  The _rn intrinsics keep the
+// compiler from contracting it into FMAs.
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &err) {
     s = __fadd_rn(a, b);
     const float bb = __fsub_rn(s, a);
     err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// acc (hi, lo) += (c_hi + c_lo) * m, with the product c_hi * m exact.
-__device__ __forceinline__ void ff_acc(float &hi, float &lo, float c_hi, float c_lo, float m) {
-    const float p = __fmul_rn(c_hi, m);
-    float pe = __fmaf_rn(c_hi, m, -p);
-    pe = __fmaf_rn(c_lo, m, pe);
-    float s, e;
-    two_sum(hi, p, s, e);
-    hi = s;
-    lo = __fadd_rn(lo, __fadd_rn(e, pe));
-}
-
-// acc += (c_hi + c_lo), exact high part.
-__device__ __forceinline__ void ff_add(float &hi, float &lo, float c_hi, float c_lo) {
-    float s, e;
-    two_sum(hi, c_hi, s, e);
-    hi = s;
-    lo = __fadd_rn(lo, __fadd_rn(e, c_lo));
-}
-
-// (hi, lo) = a * b as an unevaluated sum, exact.
-__device__ __forceinline__ void two_prod(float a, float b, float &hi, float &lo) {
-    hi = __fmul_rn(a, b);
-    lo = __fmaf_rn(a, b, -hi);
 }
 
 __device__ __forceinline__ double ff_to_double(float hi, float lo) {
@@ -61,39 +36,6 @@ __device__ __forceinline__ float fast_rcp(float x) {
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
-}
-
-// ----------------------------------------------------------------- FP32 Kepler
-// The same Markley starter in FP32, followed by one Halley step; the starter's
-// error (< 4e-4 rad) leaves a Halley residual far below FP32 resolution.
-// a1 = 1.6 pi / ((1 + e)(pi^2 - 6)) is a per-sample constant.  M in [-pi, pi].
-template <bool ACCURATE_SINCOS>
-__device__ __forceinline__ void kepler_sincos_f32(float M, float e, float ome, float a1,
-                                                  float &sinE, float &cosE) {
-    const float x = fabsf(M);
-    const float alpha = __fmaf_rn(a1, PI_F - x, (float)MK_A0_D);
-    const float d = __fmaf_rn(alpha, e, 3.0f * ome);
-    const float x2 = x * x;
-    const float ad = alpha * d;
-    const float q = __fmaf_rn(2.0f * ad, ome, -x2);
-    const float r = x * __fmaf_rn(3.0f * ad, d - ome, x2);
-    const float disc = __fmaf_rn(q * q, q, r * r);
-    const float sq = disc * rsqrtf(disc);
-    float w = exp2f(0.6666667f * __log2f(fabsf(r) + sq));
-    const float den3 = __fmaf_rn(w, w + q, q * q);
-    const float E1 = __fmaf_rn(x, den3, 2.0f * r * w) * fast_rcp(den3 * d);
-    float s1, c1;
-    if (ACCURATE_SINCOS) sincosf(E1, &s1, &c1);
-    else __sincosf(E1, &s1, &c1);
-    const float es = e * s1;
-    const float f0 = (E1 - x) - es;
-    const float f1 = __fmaf_rn(-e, c1, 1.0f);
-    // Halley: delta = -f0 f1 / (f1^2 - f0 f2 / 2)
-    const float delta = -f0 * f1 * fast_rcp(__fmaf_rn(f1, f1, -0.5f * f0 * es));
-    const float hd2 = 0.5f * delta * delta;
-    const float sE = __fmaf_rn(delta, c1, __fmaf_rn(-hd2, s1, s1));
-    cosE = __fmaf_rn(-delta, s1, __fmaf_rn(-hd2, c1, c1));
-    sinE = (M < 0.0f) ? -sE : sE;
 }
 
 // ----------------------------------------------------------------- FP64 Kepler

@@ -167,7 +167,10 @@ template <class T> __device__ __forceinline__ void vff_mul(T xh, T xl, T yh, T y
     pe = vfma(xh, yl, vfma(xl, yh, pe));
 }
 
-// Markley's starter and one Halley step (as kepler_sincos_f32), on T.
+// FP32 Kepler on T: Markley's starter (markley_starter_f32's cubic, with the
+// approximate special functions) and one Halley step; the starter's error
+// (< 4e-4 rad) leaves a Halley residual far below FP32 resolution.  M in
+// [-pi, pi]; a1 = 1.6 pi / ((1 + e)(pi^2 - 6)) is a per-sample constant.
 template <bool ACCURATE, class T>
 __device__ __forceinline__ void vkepler(T M, T e, T ne, T ome, T ome3, T a1, T &sinE, T &cosE) {
     const T x = vmap([](float v) { return fabsf(v); }, M);
