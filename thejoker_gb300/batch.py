@@ -142,4 +142,7 @@ class BatchRejection:
 
     @property
     def n_refined_last(self):
+        """Samples the last run() re-evaluated in FP64 (mixed precisions: the
+        candidates for each star's maximum, the undecided samples and the kept
+        samples whose bound exceeds JOKER_MIXED_LNL_TOL)."""
         return int(self._refined.item())
