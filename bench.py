@@ -84,12 +84,19 @@ def fill_cache_host(out, seed, threads=16):
     return out
 
 
-# Algorithmic work per unit, fixed for the roofline:
-# FP32 operations of the mixed kernel per (sample, epoch) with the jitter
+# Algorithmic work per unit, fixed for the roofline (roofline.frac): per
+# (sample, epoch) F_epoch = 4 (phase: sub, mul, floor, fma) + 6 I_K (Newton
+# steps, sincos counted as 2, I_K = 4 nominal) + 12 (true anomaly and RV
+# column) + 2 (L(L+1)/2 + L + 1) (moment FMAs) = 62 at L = 2; per sample
+# F_sample = L^3/3 + 2 L^2 + 10 (Cholesky, solve, log-det, K variance,
+# accept) = 21 at L = 2.
+FLOPS_PER_EPOCH = 62
+FLOPS_PER_SAMPLE = 21
+# FP32 operations the mixed kernel issues per (sample, epoch) with the jitter
 # applied at L = 2, counted from its source (FMA = 2 flops, special-function
-# ops = 1), and per sample for the setup and the FP64 tail.
-FLOPS_PER_EPOCH = 196
-FLOPS_PER_SAMPLE = 60
+# ops = 1), and per sample for the setup and the tail (roofline.issued_frac).
+ISSUED_FLOPS_PER_EPOCH = 196
+ISSUED_FLOPS_PER_SAMPLE = 60
 # Algorithmic HBM bytes per sample of the cache-form mixed kernel (36 B prepared
 # sample read, 8 B ln L + 4 B bound written) and the DRAM bytes ncu measured per
 # sample (read + write of one 2^24-sample launch / 2^24), scaled to a launch.
@@ -98,13 +105,13 @@ DRAM_BYTES_PER_SAMPLE = 46.79
 
 
 def _hbm_peak():
-    """Measured copy bandwidth of the GB300 (MEASURED_PEAKS.json), else the
-    6800 GB/s fallback."""
+    """(GB/s, source): the measured copy bandwidth of the GB300
+    (MEASURED_PEAKS.json), else the 6800 GB/s fallback."""
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
-            return float(json.load(f)["hbm_gbs"])
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured)"
     except Exception:
-        return 6800.0
+        return 6800.0, "fallback 6800 GB/s (MEASURED_PEAKS.json absent)"
 
 
 # ------------------------------------------------------------------- clocks
@@ -311,6 +318,11 @@ def run_ours(args, rank, world, dist):
     barrier()
     fp64_ms = (time.perf_counter() - f0) * 1e3 / 2
 
+    # ---- parity of the mixed path on the same slice (after the timed region)
+    parity = _parity_slice(table, cache, b64, S64) if world == 1 else None
+    del b64, cache
+    torch.cuda.empty_cache()
+
     # ---- max over ranks
     def gmax(x):
         if dist is None or world == 1:
@@ -326,7 +338,9 @@ def run_ours(args, rank, world, dist):
     total = S * world
     flops = S * (N_EPOCHS * FLOPS_PER_EPOCH + FLOPS_PER_SAMPLE)
     achieved = flops / (kern_ms * 1e-3) / 1e12
+    issued = S * (N_EPOCHS * ISSUED_FLOPS_PER_EPOCH + ISSUED_FLOPS_PER_SAMPLE)
     peak = args.fp32_peak
+    hbm_peak, hbm_src = _hbm_peak()
     line = {
         "metric": "prior samples/s (lnL+accept)",
         "value": total / (ms * 1e-3),
@@ -356,13 +370,20 @@ def run_ours(args, rank, world, dist):
         "gpu_launches": int(launches),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak,
+                     "work": f"algorithmic: {FLOPS_PER_EPOCH} flops per (sample, epoch) + "
+                             f"{FLOPS_PER_SAMPLE} per sample (L = 2)",
+                     "issued_tflops": issued / (kern_ms * 1e-3) / 1e12,
+                     "issued_frac": issued / (kern_ms * 1e-3) / 1e12 / peak,
+                     "issued_work": f"FP32 operations issued, counted from the kernel source: "
+                                    f"{ISSUED_FLOPS_PER_EPOCH} per (sample, epoch) + "
+                                    f"{ISSUED_FLOPS_PER_SAMPLE} per sample",
                      "traffic": args.traffic if args.traffic else DRAM_BYTES_PER_SAMPLE * S,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
                                        "2^24-sample launch, scaled by samples",
                      "hbm": {"achieved_gbs": BYTES_PER_SAMPLE * S / (kern_ms * 1e-3) / 1e9,
-                             "peak_gbs": _hbm_peak(),
-                             "frac": BYTES_PER_SAMPLE * S / (kern_ms * 1e-3) / 1e9 / _hbm_peak(),
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+                             "peak_gbs": hbm_peak,
+                             "frac": BYTES_PER_SAMPLE * S / (kern_ms * 1e-3) / 1e9 / hbm_peak,
+                             "peak_source": hbm_src},
                      "kernel": "lnl_mixed2_kernel<L=2, jitter, VAR 0, cache form> (two samples "
                                "per thread, paired FP32)",
                      "kernel_ms": kern_ms,
@@ -370,56 +391,115 @@ def run_ours(args, rank, world, dist):
                                     "chains, 74.9 TFLOP/s paired (73.1 scalar)",
                      "flops_per_launch": flops},
         "clocks": clk.summary(),
+        "parity": parity,
     }
     if not args.no_cpu:
         v, kind, cores, secs = cpu_baseline(star, args.cpu_samples)
         line["cpu_baseline"] = {"value": v, "unit": "samples/s", "cores": cores, "kind": kind,
                                 "sample": f"{args.cpu_samples} prior samples of the same star "
                                           f"({secs:.1f} s wall); the reference ignores jitter"}
+    if world == 1 and not args.headline_only:
+        # the 4096-star configuration and the serving stream, one pass each
+        del host
+        torch.cuda.empty_cache()
+        line["batched"] = batched_measure(4096, 1 << 24, warmup=1, steps=1, subset_stars=64,
+                                          subset_samples=1 << 22)
+        torch.cuda.empty_cache()
+        line["serving"] = serving_measure(1 << 28, rates=[500.0], window=4.0, n_all=2000,
+                                          slots=1024, round_budget=1 << 26, fp64_requests=64)
     return line
 
 
-def run_batched(args, rank, world):
-    """The 4096-star configuration: every star against one shared 2^24-sample
-    prior cache, ln L + acceptance (mixed, refined to FP64 decisions); the
-    plain FP64 path timed on a 64-star x 2^22-sample subset beside it."""
+def _parity_slice(table, cache, b64, S):
+    """The mixed path against the plain FP64 path on the first S rows of the
+    workload: |d ln L| before and after the band refinement (samples within
+    JOKER_MIXED_LNL_BAND of the maximum), the raw error against its bound
+    everywhere, and the accepted indices of both paths (same uniforms)."""
     import torch
-    from thejoker_gb300 import build as tb
+    from thejoker_gb300 import device as dev
+    from thejoker_gb300 import _native as nat
+    from thejoker_gb300.batch import BatchRejection
+    l64 = torch.empty((1, S), dtype=torch.float64, device="cuda")
+    dev.lnl(table, cache, l64, precision="fp64", count=S)
+    lm = torch.empty((1, S), dtype=torch.float64, device="cuda")
+    err = torch.empty((1, S), dtype=torch.float32, device="cuda")
+    bk = dev.MaxKeys(2)
+    dev.lnl(table, cache, lm, precision="mixed", count=S, err=err, bound_keys=bk)
+    raw = lm.clone()
+    seg = [dict(lnl_off=0, n=S, out_off=0, max_out=0, max_slot=0, star=0, row0=0)]
+    exact, n1 = dev.refine_max(table, cache, lm.view(-1), err.view(-1), bk, seg)
+    n2 = dev.refine_band(table, cache, lm.view(-1), err.view(-1), exact, seg)
+    a64, ar, ab = (x.view(-1).cpu().numpy() for x in (l64, raw, lm))
+    band_nats = nat.JOKER_MIXED_LNL_BAND
+    mx = a64.max()
+    band = a64 >= mx - band_nats
+    bm = BatchRejection(table, cache, precision="mixed", max_out=S, seeds=[1000])
+    bm.run(count=S)
+    c64, i64, l64k = b64.results()
+    cm, im, lmk = bm.results()
+    same = bool(c64[0] == cm[0] and np.array_equal(i64[0], im[0]))
+    ev = err.view(-1).cpu().numpy()
+    # the raw bound: refine_band set the bound of re-evaluated samples to 0,
+    # so compare against the bound of the samples it left alone
+    kept_bound = ev > 0
+    over = np.abs(ar - a64)[kept_bound] / ev[kept_bound]
+    return {"rows": int(S), "band_nats": band_nats, "tol": nat.JOKER_MIXED_LNL_TOL,
+            "samples_in_band": int(band.sum()),
+            "max_abs_dlnl_in_band": float(np.abs(ab - a64)[band].max()),
+            "max_abs_dlnl_in_band_raw": float(np.abs(ar - a64)[band].max()),
+            "max_abs_dlnl_all_raw": float(np.nanmax(np.abs(ar - a64))),
+            "max_dlnl_over_bound": float(np.nanmax(over)) if over.size else 0.0,
+            "fp64_refined": int((n1 + n2).item()),
+            "max_abs_dmax": float(abs(exact.values()[0] - mx)),
+            "accepted": int(c64[0]), "accept_identical": same,
+            "max_abs_dlnl_kept": float(np.max(np.abs(lmk[0] - l64k[0]))) if same and
+            len(lmk[0]) else 0.0}
+
+
+def batched_measure(n_stars, S, warmup=1, steps=1, subset_stars=64, subset_samples=1 << 22,
+                    group=None, rank=0, world=1):
+    """The 4096-star configuration: every star against one shared 2^24-sample
+    prior cache, ln L + acceptance (mixed, refined to FP64 decisions), timed
+    over ``steps`` passes after ``warmup``; the mixed and the plain FP64 paths
+    timed on a subset of stars x samples beside it, with their accepted counts
+    compared."""
+    import torch
+    from thejoker_gb300 import _native as nat
+    from thejoker_gb300 import autotune
     from thejoker_gb300 import device as dev
     from thejoker_gb300.batch import BatchRejection
     from thejoker_gb300.synthetic import fill_prior_cache, survey_stars
-    tb.build()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-    n_stars = args.stars
-    S = args.samples
     stars = survey_stars(n_stars * world, seed=3)[rank * n_stars:(rank + 1) * n_stars]
     host = torch.empty((S, 5), dtype=torch.float64).pin_memory()
     fill_prior_cache(host.numpy(), SEED_CACHE)
     cache = dev.PriorCache(S).load(host.cuda())
     table = dev.StarTable(stars)
-    from thejoker_gb300 import autotune
     sub_t = dev.StarTable(stars[:256])
     sub_t.n_epochs = table.n_epochs            # tune for the survey's epoch counts
     tuned, tune_ms = autotune.tune(sub_t, cache, precision="mixed", count=min(S, 1 << 22),
                                    reps=1)
+    del sub_t
     br = BatchRejection(table, cache, precision="mixed", max_out=256,
-                        seeds=np.arange(n_stars) + rank * n_stars, group=args.group)
-    for _ in range(args.warmup):
+                        seeds=np.arange(n_stars) + rank * n_stars, group=group)
+    for _ in range(warmup):
         br.run()
     torch.cuda.synchronize()
-    from thejoker_gb300 import _native as nat
     with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
         launches0 = nat.lib().joker_launch_count()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             br.run()
         torch.cuda.synchronize()
-        ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        ms = (time.perf_counter() - t0) * 1e3 / steps
         launches = nat.lib().joker_launch_count() - launches0
     counts, _, _ = br.results()
+    n_refined = br.n_refined_last
+    group_used = br.group
+    del br
+    torch.cuda.empty_cache()
     # mixed vs FP64 on the same subset
-    sub = args.subset_stars
-    Ssub = min(S, args.fp64_samples)
+    sub = subset_stars
+    Ssub = min(S, subset_samples)
     table_sub = dev.StarTable(stars[:sub])
     res = {}
     for prec in ("mixed", "fp64"):
@@ -429,28 +509,57 @@ def run_batched(args, rank, world):
         t0 = time.perf_counter()
         b.run(count=Ssub)
         torch.cuda.synchronize()
-        res[prec] = (time.perf_counter() - t0, b.results()[0])
-    same = bool(np.array_equal(res["mixed"][1], res["fp64"][1]))
+        res[prec] = (time.perf_counter() - t0, b.results())
+        del b
+    c_m, i_m, _ = res["mixed"][1]
+    c_64, i_64, _ = res["fp64"][1]
+    same_counts = bool(np.array_equal(c_m, c_64))
+    same_idx = same_counts and all(np.array_equal(a, b) for a, b in zip(i_m, i_64))
     n_ep = np.array([len(s["t"]) for s in stars])
     return {
-        "metric": "prior samples/s (lnL+accept)",
         "value": n_stars * world * S / (ms * 1e-3), "unit": "samples/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded survey, numpy prior cache)",
-        "config": {"workload": f"{n_stars} stars x 2^{int(math.log2(S))} shared prior samples, "
-                               f"epochs log-uniform [3,256] (mean {n_ep.mean():.1f}), 30% "
-                               "companions; acceptance refined to FP64 decisions",
-                   "stars_per_gpu": n_stars, "prior_samples": S, "group": br.group,
-                   "autotune": {"chunk": tuned, "ms_256_stars_2^22_samples": tune_ms}},
+        "ms_per_step": ms, "steps": steps, "warmup": warmup,
+        "workload": f"{n_stars} stars x 2^{int(math.log2(S))} shared prior samples, epochs "
+                    f"log-uniform [3,256] (mean {n_ep.mean():.1f}), 30% companions; acceptance "
+                    "refined to FP64 decisions",
+        "stars_per_gpu": n_stars, "prior_samples": S, "group": group_used,
+        "autotune": {"chunk": tuned, "ms_256_stars_2^22_samples": tune_ms},
+        "fp64_refined_per_step": n_refined,
         "subset": {"stars": sub, "samples": Ssub,
                    "mixed_samples_per_s": sub * Ssub / res["mixed"][0],
                    "fp64_samples_per_s": sub * Ssub / res["fp64"][0],
                    "speedup_mixed_vs_fp64": res["fp64"][0] / res["mixed"][0],
-                   "accept_counts_identical": same},
+                   "accept_counts_identical": same_counts,
+                   "accepted_indices_identical": same_idx},
         "accepted_total": int(counts.sum()),
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
+    }
+
+
+def run_batched(args, rank, world):
+    """The 4096-star configuration as its own bench line (batched_measure)."""
+    import torch
+    from thejoker_gb300 import build as tb
+    tb.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    m = batched_measure(args.stars, args.samples, warmup=args.warmup, steps=args.steps,
+                        subset_stars=args.subset_stars,
+                        subset_samples=min(args.samples, args.fp64_samples), group=args.group,
+                        rank=rank, world=world)
+    return {
+        "metric": "prior samples/s (lnL+accept)",
+        "value": m["value"], "unit": "samples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": m["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded survey, numpy prior cache)",
+        "config": {"workload": m["workload"], "stars_per_gpu": m["stars_per_gpu"],
+                   "prior_samples": m["prior_samples"], "group": m["group"],
+                   "autotune": m["autotune"]},
+        "subset": m["subset"], "accepted_total": m["accepted_total"],
+        "fp64_refined_per_step": m["fp64_refined_per_step"],
+        "gpu_launches": m["gpu_launches"], "clocks": m["clocks"],
     }
 
 
@@ -578,7 +687,8 @@ def _lindley(arrivals, service):
     return out
 
 
-def run_serving(args, rank, world):
+def serving_measure(S, rates, window=4.0, n_all=20000, slots=1024, round_budget=1 << 26,
+                    fp64_requests=128, rank=0):
     """Serving: a Poisson stream of star requests (epochs log-uniform [3,200],
     prior budget log-uniform 2^20-2^27 samples of a device-resident 2^28
     cache, n_requested in {1, 128, 512}), admitted by free device memory into
@@ -587,12 +697,8 @@ def run_serving(args, rank, world):
     measured on a prefix of the stream, its latency at each rate from its
     measured service times (FIFO queue)."""
     import torch
-    from thejoker_gb300 import build as tb
     from thejoker_gb300 import device as dev
     from thejoker_gb300.serve import Request, ServingEngine
-    tb.build()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-    S = args.samples
     # the resident cache is drawn on the device (P log-uniform [2, 1024] d,
     # e ~ Beta(0.867, 3.03), uniform angles, s = 0)
     cache = dev.PriorCache(S)
@@ -601,26 +707,24 @@ def run_serving(args, rank, world):
                             s_value=0.0), S, seed=SEED_CACHE + 2)
     torch.cuda.synchronize()
     cache_s = time.perf_counter() - t0
-    n_all = args.requests
     stars, budgets, n_reqs = _serving_requests(n_all, 11 + rank)
 
     def make(k):
         return Request(stars[k], budget=int(budgets[k]), n_requested=int(n_reqs[k]),
                        seed=100000 + k)
 
-    eng = ServingEngine(cache, n_slots=args.slots, max_epochs=200, n_linear=2,
-                        max_requested=512, precision="mixed", round_budget=args.round_budget,
+    eng = ServingEngine(cache, n_slots=slots, max_epochs=200, n_linear=2,
+                        max_requested=512, precision="mixed", round_budget=round_budget,
                         pool_fraction=0.6)
     # warm-up: the first rounds load the kernels and capture the round graph
     for k in range(min(n_all, 64)):
         eng.submit(make(k))
     eng.drain()
-    rates = [float(r) for r in args.rates.split(",")]
     rng = np.random.default_rng(77)
     sweep = []
     with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
         for rate in rates:
-            n = int(min(n_all, max(200, rate * args.window)))
+            n = int(min(n_all, max(200, rate * window)))
             arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
             reqs = [make(k) for k in range(n)]
             lat, span, evals = _serve_stream(eng, reqs, arrivals)
@@ -632,7 +736,7 @@ def run_serving(args, rank, world):
     rounds = eng.rounds
     eng.close()
     # plain FP64 per-star path: one star at a time, same requests
-    n64 = min(args.fp64_requests, n_all)
+    n64 = min(fp64_requests, n_all)
     one = ServingEngine(cache, n_slots=1, max_epochs=200, n_linear=2, max_requested=512,
                         precision="fp64", pool_samples=1 << 27)
     one.submit(make(0))
@@ -649,12 +753,33 @@ def run_serving(args, rank, world):
     fp64 = {"requests_timed": n64, "mean_service_ms": float(service.mean() * 1e3),
             "capacity_req_per_s": float(1.0 / service.mean()), "per_rate": []}
     for rate in rates:
-        n = int(min(n_all, max(200, rate * args.window)))
+        n = int(min(n_all, max(200, rate * window)))
         arrivals = np.cumsum(np.random.default_rng(5).exponential(1.0 / rate, n))
         lat = _lindley(arrivals, np.resize(service, n))
         fp64["per_rate"].append({"rate_per_s": rate, "p50_ms": float(np.percentile(lat, 50) * 1e3),
                                  "p99_ms": float(np.percentile(lat, 99) * 1e3)})
-    top = sweep[-1]
+    del cache
+    torch.cuda.empty_cache()
+    return {"workload": "Poisson stream of star requests, epochs log-uniform [3,200], "
+                        "budget log-uniform 2^20-2^27 of a resident "
+                        f"2^{int(math.log2(S))} cache, n_requested in {{1,128,512}}",
+            "slots": slots, "round_budget": round_budget, "window_s": window,
+            "sweep": sweep, "rounds": rounds, "cache_sample_s": cache_s,
+            "fp64_per_star": fp64, "clocks": clk.summary()}
+
+
+def run_serving(args, rank, world):
+    """The serving stream as its own bench line (serving_measure), swept over
+    arrival rates."""
+    import torch
+    from thejoker_gb300 import build as tb
+    tb.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    rates = [float(r) for r in args.rates.split(",")]
+    m = serving_measure(args.samples, rates, window=args.window, n_all=args.requests,
+                        slots=args.slots, round_budget=args.round_budget,
+                        fp64_requests=args.fp64_requests, rank=rank)
+    top = m["sweep"][-1]
     return {
         "metric": "p50/p99 per-star latency and request throughput, serving",
         "value": top["throughput_req_per_s"], "unit": "requests/s",
@@ -662,14 +787,11 @@ def run_serving(args, rank, world):
         "ms_per_step": top["span_s"] * 1e3 / max(top["requests"], 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded survey stream, numpy prior cache)",
-        "config": {"workload": "Poisson stream of star requests, epochs log-uniform [3,200], "
-                               "budget log-uniform 2^20-2^27 of a resident "
-                               f"2^{int(math.log2(S))} cache, n_requested in {{1,128,512}}",
-                   "slots": args.slots, "round_budget": args.round_budget,
-                   "requests_max": n_all, "window_s": args.window},
-        "sweep": sweep, "rounds": rounds, "cache_sample_s": cache_s,
-        "fp64_per_star": fp64,
-        "clocks": clk.summary(),
+        "config": {"workload": m["workload"], "slots": args.slots,
+                   "round_budget": args.round_budget, "requests_max": args.requests,
+                   "window_s": args.window},
+        "sweep": m["sweep"], "rounds": m["rounds"], "cache_sample_s": m["cache_sample_s"],
+        "fp64_per_star": m["fp64_per_star"], "clocks": m["clocks"],
     }
 
 
@@ -915,6 +1037,8 @@ def main():
     p.add_argument("--fp32-peak", type=float, default=74.9)
     p.add_argument("--traffic", type=float, default=None)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--headline-only", action="store_true",
+                   help="default mode: skip the batched and serving sub-objects")
     p.add_argument("--config", default="single",
                    choices=["single", "small", "batched", "iterative", "serving",
                             "posterior"])

@@ -237,6 +237,26 @@ int joker_refine_max(const joker_stars *stars, const joker_cache *cache,
                      const float *d_err, const uint64_t *d_bound_key, uint64_t *d_exact_key,
                      uint64_t *d_n_refined, void *d_work, int64_t work_bytes, void *stream);
 
+/* The band refinement of mixed-precision ln L values (no counterpart in the
+ * reference, whose values are all FP64): every sample of the segments whose
+ * interval [lnL - err, lnL + err] reaches within `band` of its slot's FP64
+ * maximum d_exact_key[seg.max_slot] (from joker_refine_max or
+ * joker_accept_refined), and whose bound err exceeds `tol`, is re-evaluated
+ * in FP64; its FP64 ln L is written to d_lnl and its bound set to 0.  Samples
+ * without a finite value or bound are re-evaluated too.  Afterwards every
+ * ln L of the segments within `band` of the maximum is within `tol` of the
+ * FP64 path's value; below the band each value keeps its mixed bound.  The
+ * host mirror uses band = JOKER_MIXED_LNL_BAND and tol = JOKER_MIXED_LNL_TOL
+ * for the ln L values it returns (marginal_ln_likelihood,
+ * thejoker/thejoker.py:93-138; return_all_logprobs, :140-257).  Same
+ * workspace as joker_accept. */
+#define JOKER_MIXED_LNL_BAND 40.0  /* nats: exp(-40) < 2^-53, below any nonzero
+                                      uniform of the acceptance test */
+int joker_refine_band(const joker_stars *stars, const joker_cache *cache,
+                      const joker_accept_seg *segs, int n_segs, double *d_lnl, float *d_err,
+                      const uint64_t *d_exact_key, double band, double tol,
+                      uint64_t *d_n_refined, void *d_work, int64_t work_bytes, void *stream);
+
 /* ---- iterative rejection, one device-resident round at a time --------------
  * Replaces the loop of iterative_rejection_inmem
  * (thejoker/likelihood_helpers.py:130-229) for every star of a joker_stars
@@ -380,14 +400,23 @@ int joker_rejection_sample(const joker_stars *stars, const joker_cache *cache, i
  * unbounded latency), or a plugin inside a host framework whose caching
  * allocator already holds the device's free memory.  It needs no workspace.
  * Its scratch space is one fixed array of 2,220,288 bytes inside the
- * library, held on every GPU that loads the library until the process exits.
- * Limits: at most JOKER_NOALLOC_MAX_SEGS segments and
+ * library.  Limits: at most JOKER_NOALLOC_MAX_SEGS segments and
  * JOKER_NOALLOC_MAX_BLOCKS blocks of 8192 samples (each segment rounded up;
  * about 2^24 samples in all); larger calls return JOKER_ERANGE.  All calls
  * share the array: calls that overlap on the GPU (another stream, another
- * host thread) race and must not be issued.  The first call on a device looks
- * up the array's address with that device current; make it before any stream
- * capture.  It allocates nothing: no cudaMalloc, cudaFree or heap use. */
+ * host thread) race and must not be issued.
+ * Set-up: the first call on a device, with that device current, looks up the
+ * array's address and loads the pass's kernels; under lazy module loading
+ * (the CUDA default) that is also when the device's copy of the array is
+ * allocated.  Make that first call at start-up, before any stream capture: a
+ * call with n_segs = 0 does the set-up and nothing else.  After it the device
+ * holds the array until the process exits, and no call allocates: no
+ * cudaMalloc, cudaFree or heap use.  The address is kept for the life of the
+ * process, so the entry point must not be used on a device after
+ * cudaDeviceReset of that device.
+ * segs is copied to the device on `stream`: from pageable memory before the
+ * call returns; from pinned memory later, so pinned segs must stay unchanged
+ * until the stream has passed the call. */
 #define JOKER_NOALLOC_MAX_SEGS 1024
 #define JOKER_NOALLOC_MAX_BLOCKS 2048
 int joker_accept_noalloc(const joker_accept_seg *segs, int n_segs, const double *d_lnl,

@@ -18,7 +18,8 @@ import sysconfig
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = "/root/reference"
+# the reference checkout: JOKER_REFERENCE_ROOT, else where this container mounts it
+REFERENCE_ROOT = os.environ.get("JOKER_REFERENCE_ROOT", "/root/reference")
 REF_PYX = os.path.join(REFERENCE_ROOT, "thejoker", "src", "fast_likelihood.pyx")
 ORACLE_SO = os.path.join(BUILD, "liboracle.so")
 

@@ -22,7 +22,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-DATA_ECSV = "/root/reference/docs/examples/data.ecsv"
+# the reference checkout: JOKER_REFERENCE_ROOT, else where this container mounts it
+REFERENCE_ROOT = os.environ.get("JOKER_REFERENCE_ROOT", "/root/reference")
+DATA_ECSV = os.path.join(REFERENCE_ROOT, "docs", "examples", "data.ecsv")
 
 
 def kepler_known_answer():

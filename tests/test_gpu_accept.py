@@ -101,13 +101,17 @@ def test_thejoker_rejection_sample_matches_reference_pipeline(cuda, precision):
     st = synth_star(rng, 12, K=5.0)
     prior = JokerPrior.default(P_min=2, P_max=1024, sigma_K0=30.0, sigma_v=100.0)
     data = RVData(st["t"], st["rv"], 1 / np.sqrt(st["ivar"]))
-    samples = prior.sample(20000, rng=np.random.default_rng(3))
+    samples = prior.sample(20000, rng=np.random.default_rng(3), return_logprobs=True)
     chunk = samples.pack()[0]
     joker = TheJoker(prior, rng=np.random.default_rng(42), precision=precision)
-    out = joker.rejection_sample(data, samples, max_posterior_samples=300, return_logprobs=True)
+    out = joker.rejection_sample(data, samples, max_posterior_samples=300, return_logprobs=True,
+                                 in_memory=True)
     good, raw, lls = _reference_rejection(st, chunk, np.random.default_rng(42), 300, 1, prior)
     assert len(out) == len(good) > 0
     np.testing.assert_array_equal(out["P"], chunk[good, 0])
+    np.testing.assert_array_equal(out["ln_prior"], samples["ln_prior"][good])
+    np.testing.assert_allclose(out["ln_likelihood"], lls[good], rtol=0,
+                               atol=1e-4 if precision == "mixed" else 1e-8)
     np.testing.assert_allclose(out["K"], raw[:, 5], rtol=1e-6, atol=1e-6)
     np.testing.assert_allclose(out["v0"], raw[:, 6], rtol=1e-6, atol=1e-6)
     # the generator ends in the same state as the reference's
@@ -125,7 +129,7 @@ def test_thejoker_iterative_matches_reference_loop(cuda):
     chunk = prior.sample(200000, rng=np.random.default_rng(4)).pack()[0]
     joker = TheJoker(prior, rng=np.random.default_rng(7), precision="fp64")
     out = joker.iterative_rejection_sample(data, chunk, n_requested_samples=8,
-                                           init_batch_size=2000)
+                                           init_batch_size=2000, in_memory=True)
     # likelihood_helpers.iterative_rejection_inmem restated
     r = np.random.default_rng(7)
     lls_all = oracle_lnl(st, chunk[:200000])

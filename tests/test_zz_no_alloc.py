@@ -5,9 +5,11 @@ Some callers of this library cannot call cudaMalloc: a serving loop with
 per-request deadlines (cudaMalloc may synchronise the device) or a plugin
 inside a framework whose allocator already holds the free device memory.
 For them the pass keeps its scratch space in a fixed array inside the library.
-This test calls that entry point through the C ABI twice in a row, with
-different inputs, and checks each result against the ordinary entry point,
-which uses a caller-supplied workspace.  Indices and counts are integers and
+This test makes the start-up call (no segments), then calls that entry point
+through the C ABI twice in a row, with different inputs, and checks each
+result against the ordinary entry point, which uses a caller-supplied
+workspace, and that the device's free memory is the same after each call as
+before it.  Indices and counts are integers and
 must match exactly; the gathered ln L values are copies and must match
 bit for bit.  The file is named so that pytest collects it last.
 """
@@ -48,6 +50,16 @@ def _segments(rng, sizes, pcg):
     return arr, off, out_off
 
 
+def _warm_up():
+    """The start-up call with no segments: looks up the fixed array on this
+    device and loads the pass's kernels, so no later call loads anything."""
+    from thejoker_gb300 import _native as nat
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    nat.check(nat.lib().joker_accept_noalloc(None, 0, None, None, 1, None, None, None, None,
+                                             stream), "joker_accept_noalloc warm-up")
+    torch.cuda.synchronize()
+
+
 def _run(fn_name, arr, n_segs, lnl, keys, u_source, u, n_out):
     from thejoker_gb300 import _native as nat
     lib = nat.lib()
@@ -55,6 +67,8 @@ def _run(fn_name, arr, n_segs, lnl, keys, u_source, u, n_out):
     olnl = torch.full((n_out,), float("nan"), dtype=torch.float64, device="cuda")
     cnt = torch.full((n_segs,), -1, dtype=torch.int64, device="cuda")
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
     uptr = ctypes.c_void_p(u.data_ptr()) if u is not None else None
     if fn_name == "joker_accept":
         ws = lib.joker_accept_workspace(arr, n_segs)
@@ -72,6 +86,10 @@ def _run(fn_name, arr, n_segs, lnl, keys, u_source, u, n_out):
                                       ctypes.c_void_p(cnt.data_ptr()), stream)
     nat.check(st, fn_name)
     torch.cuda.synchronize()
+    if fn_name == "joker_accept_noalloc":
+        # after the warm-up the call takes no device memory: free memory is
+        # unchanged across it (its outputs were allocated before)
+        assert torch.cuda.mem_get_info()[0] == free0
     return idx.cpu().numpy(), olnl.cpu().numpy(), cnt.cpu().numpy()
 
 
@@ -81,6 +99,7 @@ def test_noalloc_matches_workspace_version_twice(u_source):
         pytest.skip("no CUDA device")
     from thejoker_gb300 import build
     build.build()
+    _warm_up()
     rng = np.random.default_rng(2024 + u_source)
     gen = np.random.default_rng(77)
     pcg = (int(gen.bit_generator.state["state"]["state"]),

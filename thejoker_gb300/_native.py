@@ -20,6 +20,8 @@ JOKER_U_PCG64 = 1
 JOKER_S_FIXED = 0
 JOKER_S_LOGNORMAL = 1
 JOKER_MAX_LINEAR = 6
+JOKER_MIXED_LNL_TOL = 1e-4
+JOKER_MIXED_LNL_BAND = 40.0
 
 # every extern "C" symbol of include/joker_gb300.h
 EXPORTED = (
@@ -33,7 +35,7 @@ EXPORTED = (
     "joker_iter_outputs", "joker_iter_read", "joker_iter_create_pool", "joker_iter_admit",
     "joker_iter_set_round_budget", "joker_accept_noalloc", "joker_linear_posterior",
     "joker_unmarginalized_lnl", "joker_prior_sample", "joker_rv_from_elements",
-    "joker_rejection_workspace", "joker_rejection_sample",
+    "joker_rejection_workspace", "joker_rejection_sample", "joker_refine_band",
 )
 
 
@@ -97,6 +99,9 @@ _SIGS = {
                                             _vp]),
     "joker_refine_max": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp,
                                         _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
+    "joker_refine_band": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp,
+                                         _vp, _vp, ctypes.c_double, ctypes.c_double, _vp, _vp,
+                                         _i64, _vp]),
     "joker_iter_create": (ctypes.c_int, [ctypes.POINTER(_vp), _vp, _vp, ctypes.c_int, _i64, _i64,
                                          ctypes.c_int, _i64, ctypes.c_double, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]),

@@ -10,6 +10,9 @@
 #include <vector>
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include "joker_internal.cuh"
 
 namespace joker {
@@ -21,6 +24,8 @@ cudaError_t launch_prepare(const double *chunk, int64_t n, int64_t row0, double 
 cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st,
                           bool max_given = false);
 cudaError_t launch_refine_max(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st);
+cudaError_t launch_refine_band(const AcceptArgs &a, int64_t total_blocks, double band, float tol,
+                               cudaStream_t st);
 int64_t accept_blocks(const joker_accept_seg *segs, int n_segs, int64_t *blk_base_host);
 }  // namespace joker
 
@@ -73,6 +78,38 @@ void set_last_error(const char *msg) { g_err = msg; }
 
 static std::atomic<unsigned long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// Grid size of a persistent launch on the current device: SM count x resident
+// CTAs of `kern` at `block` threads.  Both are looked up once per (device,
+// kernel, block) and kept, so a process that drives several devices sizes each
+// grid for its own device and no launch pays for an occupancy query.
+static std::mutex g_occ_mutex;
+static std::map<std::tuple<int, const void *, int>, int> g_occ_grid;
+
+cudaError_t persistent_grid(const void *kern, int block, int *grid) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const auto key = std::make_tuple(dev, kern, block);
+    {
+        std::lock_guard<std::mutex> lock(g_occ_mutex);
+        auto it = g_occ_grid.find(key);
+        if (it != g_occ_grid.end()) {
+            *grid = it->second;
+            return cudaSuccess;
+        }
+    }
+    int sms = 0, occ = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, 0);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+    *grid = sms * occ;
+    std::lock_guard<std::mutex> lock(g_occ_mutex);
+    g_occ_grid[key] = *grid;
+    return cudaSuccess;
+}
 }  // namespace joker
 
 extern "C" uint64_t joker_launch_count(void) { return (uint64_t)joker::g_launches.load(); }
@@ -859,6 +896,29 @@ extern "C" int joker_refine_max(const joker_stars *s, const joker_cache *c,
                                  "joker_refine_max");
     if (rc != JOKER_OK) return rc;
     CUDA_TRY(launch_refine_max(a, nb, st));
+    return JOKER_OK;
+}
+
+extern "C" int joker_refine_band(const joker_stars *s, const joker_cache *c,
+                                 const joker_accept_seg *segs, int n_segs, double *d_lnl,
+                                 float *d_err, const uint64_t *d_exact_key, double band,
+                                 double tol, uint64_t *d_n_refined, void *d_work,
+                                 int64_t work_bytes, void *stream) {
+    if (n_segs <= 0) return JOKER_OK;
+    if (!(band >= 0.0) || !(tol >= 0.0))
+        return fail(JOKER_EINVAL, "joker_refine_band: band and tol must be >= 0");
+    int n_slots = 0;
+    if (segs)
+        for (int i = 0; i < n_segs; ++i) n_slots = std::max(n_slots, segs[i].max_slot + 1);
+    AcceptArgs a;
+    int64_t nb = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    // the bound maxima are not read here; the FP64 maxima stand in for them
+    const int rc = refined_setup(s, c, segs, n_segs, d_lnl, d_err, d_exact_key,
+                                 const_cast<uint64_t *>(d_exact_key), n_slots, d_n_refined,
+                                 d_work, work_bytes, st, a, nb, "joker_refine_band");
+    if (rc != JOKER_OK) return rc;
+    CUDA_TRY(launch_refine_band(a, nb, band, (float)tol, st));
     return JOKER_OK;
 }
 

@@ -179,11 +179,12 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_candidates_kernel(AcceptAr
 
 // FP64 re-evaluation of the listed samples, one warp per sample (lanes over
 // epochs).  MODE 0 raises the FP64 maximum; MODE 1 decides the undecided
-// samples against it and their own uniforms.
+// samples against it and their own uniforms; MODE 2 (the band refinement)
+// only writes the FP64 value back.
 template <int MODE>
 __global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
     const int lane = threadIdx.x & 31;
-    const int64_t n = min((int64_t)a.flag_count[MODE], a.flag_cap);
+    const int64_t n = min((int64_t)a.flag_count[MODE == 1 ? 1 : 0], a.flag_cap);   // MODE 2 uses list 0
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t e = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); e < n;
          e += nw) {
@@ -198,6 +199,9 @@ __global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
         if (a.n_refined) atomicAdd(a.n_refined, 1ull);
         if (MODE == 0) {
             atomicMax(a.exact_key + sg.max_slot, double_to_key(v));
+        } else if (MODE == 2) {
+            const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
+            const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
         } else {
             const double mx = key_to_double(a.exact_key[sg.max_slot]);
             double u;
@@ -223,7 +227,8 @@ __global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
 // FP64 work on the samples flagged in amb_words.  One thread covers
 // WORDS_PER_THREAD consecutive words (all inside one 256-word CTA block);
 // almost all words are zero.  MODE 0 raises the FP64 maximum; MODE 1 decides
-// the undecided samples against it and their own uniforms.
+// the undecided samples against it and their own uniforms; MODE 2 writes the
+// FP64 value back.
 constexpr int WORDS_PER_THREAD = 16;
 
 template <int MODE>
@@ -264,6 +269,9 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
             if (a.n_refined) atomicAdd(a.n_refined, 1ull);
             if (MODE == 0) {
                 atomicMax(a.exact_key + sg.max_slot, double_to_key(v));
+            } else if (MODE == 2) {
+                const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
+                const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
             } else {
                 double u;
                 if (a.u_source == JOKER_U_PCG64) {
@@ -283,6 +291,49 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
             atomicAdd((unsigned long long *)(a.blk_count + gblk), (unsigned long long)__popc(add));
         }
     }
+    }
+}
+
+// The band refinement's scan: flags every sample whose mixed interval reaches
+// within `band` of its slot's FP64 maximum (lnL + err >= max - band) and whose
+// bound exceeds `tol`, and every sample without a usable bound or value.  The
+// float pre-test settles the samples far below the band without FP64 work.
+__global__ void __launch_bounds__(ACC_THREADS) band_flag_kernel(AcceptArgs a, double band,
+                                                                float tol) {
+    const int64_t nbk = n_blocks(a);
+    for (int64_t gblk = blockIdx.x; gblk < nbk; gblk += gridDim.x) {
+    const int si = find_seg(a, gblk);
+    const joker_accept_seg sg = a.segs[si];
+    const int64_t blk = gblk - seg_base(a, si);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t wbase = blk * ACC_BLOCK + (int64_t)warp * 1024;
+    const double thr = key_to_double(a.exact_key[sg.max_slot]) - band;
+    float thrf;
+    const bool fast = dbl_to_float_trunc(thr, thrf);
+    uint32_t my_word = 0;
+    for (int k = 0; k < 32; ++k) {
+        const int64_t i = wbase + (int64_t)k * 32 + lane;
+        bool flag = false;
+        if (i < sg.n) {
+            const double v = a.lnl[sg.lnl_off + i];
+            const float er = a.err[sg.lnl_off + i];
+            float vf;
+            if (!(er < 1e29f) || !(v == v)) {
+                flag = true;                         // no bound, or no value
+            } else if (er <= tol) {
+                flag = false;                        // already within the tolerance
+            } else if (fast && dbl_to_float_trunc(v, vf) &&
+                       vf + er + (1e-6f + 5e-7f * (fabsf(vf) + fabsf(thrf) + er)) < thrf) {
+                flag = false;                        // certainly below the band
+            } else {
+                flag = v + (double)er >= thr;
+            }
+        }
+        const bool fit = flag_append(a, 0, flag, si, i);
+        const uint32_t bal = __ballot_sync(0xffffffffu, !fit);
+        if (lane == k) my_word = bal;
+    }
+    a.amb_words[gblk * ACC_THREADS + threadIdx.x] = my_word;
     }
 }
 
@@ -454,13 +505,27 @@ int64_t accept_blocks(const joker_accept_seg *segs, int n_segs, int64_t *blk_bas
     return tot;
 }
 
+// Loads the module of the plain pass's kernels (mark, scan, emit) on the
+// current device without launching them.  Under lazy module loading (the
+// default since CUDA 12.2) a module is loaded, and its device memory taken, at
+// the first use of one of its functions; joker_accept_noalloc's warm-up call
+// uses this so that no later call loads anything.
+cudaError_t accept_preload() {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, accept_mark_kernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, accept_scan_kernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, accept_emit_kernel);
+    return e;
+}
+
 static cudaError_t launch_fp64_words(int mode, const AcceptArgs &a, int64_t total_blocks,
                                      cudaStream_t st) {
     // the compacted list first (one warp per sample), then the words of the
     // samples that did not fit in it (almost always none)
     const unsigned lgrid = 152 * 4;
     if (mode == 0) accept_fp64_list_kernel<0><<<lgrid, 256, 0, st>>>(a);
-    else accept_fp64_list_kernel<1><<<lgrid, 256, 0, st>>>(a);
+    else if (mode == 1) accept_fp64_list_kernel<1><<<lgrid, 256, 0, st>>>(a);
+    else accept_fp64_list_kernel<2><<<lgrid, 256, 0, st>>>(a);
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -468,9 +533,22 @@ static cudaError_t launch_fp64_words(int mode, const AcceptArgs &a, int64_t tota
     const int64_t threads = (n_words + WORDS_PER_THREAD - 1) / WORDS_PER_THREAD;
     const unsigned grid = (unsigned)((threads + 127) / 128);
     if (mode == 0) accept_fp64_words_kernel<0><<<grid, 128, 0, st>>>(a, n_words);
-    else accept_fp64_words_kernel<1><<<grid, 128, 0, st>>>(a, n_words);
+    else if (mode == 1) accept_fp64_words_kernel<1><<<grid, 128, 0, st>>>(a, n_words);
+    else accept_fp64_words_kernel<2><<<grid, 128, 0, st>>>(a, n_words);
     count_launch();
     return cudaGetLastError();
+}
+
+cudaError_t launch_refine_band(const AcceptArgs &a, int64_t total_blocks, double band, float tol,
+                               cudaStream_t st) {
+    if (total_blocks <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(a.flag_count, 0, 2 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    band_flag_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a, band, tol);
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_fp64_words(2, a, total_blocks, st);
 }
 
 cudaError_t launch_refine_max(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st) {

@@ -682,21 +682,14 @@ lnl_mixed2_kernel(LnlArgs a) {
 
 // Persistent launch: as many CTAs as can be resident on the device (never more
 // than there are work items); each CTA loops over the shared work counter.
+// persistent_grid (joker_abi.cu) caches the grid per device, kernel and block.
+cudaError_t persistent_grid(const void *kern, int block, int *grid);
+
 template <typename K>
 inline cudaError_t launch_persistent(K kern, const LnlArgs &a, int block, cudaStream_t st) {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e != cudaSuccess) return e;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return e;
-    }
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, 0);
+    int grid = 0;
+    cudaError_t e = persistent_grid(reinterpret_cast<const void *>(kern), block, &grid);
     if (e != cudaSuccess) return e;
-    if (occ < 1) occ = 1;
-    int grid = sms * occ;
     if (!a.n_items_dev && grid > a.n_items) grid = a.n_items;
     if (grid < 1) return cudaSuccess;
     kern<<<grid, block, 0, st>>>(a);

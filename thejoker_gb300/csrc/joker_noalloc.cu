@@ -12,8 +12,15 @@
 // accepted-sample bit masks and the copied segment table) in one file-scope
 // device array of fixed size, instead of a caller-supplied workspace.
 //
-// The array, ACC_SCRATCH_BYTES = 2,220,288 bytes, is part of the module image.
-// Every GPU on which the library is loaded holds it until the process exits.
+// The array, ACC_SCRATCH_BYTES = 2,220,288 bytes, is static device data of
+// this file's module.  Under lazy module loading (the CUDA default since 12.2)
+// that module, and with it the array's device memory, is loaded on a device at
+// the first lookup of the array there.  So each device needs one warm-up call
+// at start-up, with that device current and before any stream capture: a call
+// with n_segs = 0 does the lookup and loads the pass's kernels, and runs
+// nothing.  A first call that does real work does the same set-up itself, so
+// if it comes first it is the call that loads the module and takes the
+// memory.  From then on the device holds the array until the process exits.
 // Its limits are:
 // - at most JOKER_NOALLOC_MAX_SEGS segments;
 // - at most JOKER_NOALLOC_MAX_BLOCKS blocks of 8192 samples, counted per
@@ -27,9 +34,16 @@
 // whose work overlaps on the GPU race on the array: two streams must not run
 // this entry point at the same time on one device.
 //
-// The device address of the array is looked up once per device, with that
-// device current, by the first call made on it. That first call should
-// therefore come before any stream capture.
+// Each call copies the segment table (and its block offsets, from the
+// stack) into the array with cudaMemcpyAsync on the caller's stream.  From
+// pageable memory the copy is staged before the call returns; a segment table
+// in pinned memory is read by the copy engine later, so it must stay unchanged
+// until the stream has passed the call.
+//
+// The array's device address is looked up once per device and kept for the
+// life of the process.  After cudaDeviceReset the module may be reloaded at
+// another address, so this entry point must not be used on a device after a
+// reset of that device.
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -38,6 +52,7 @@
 namespace joker {
 cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st,
                           bool max_given = false);
+cudaError_t accept_preload();
 int64_t accept_blocks(const joker_accept_seg *segs, int n_segs, int64_t *blk_base_host);
 void set_last_error(const char *msg);
 }  // namespace joker
@@ -69,7 +84,9 @@ unsigned char *g_scratch_addr[MAX_DEVICES] = {};
 // on the host it only stands for the symbol, not a device address.
 static __device__ __align__(256) unsigned char g_accept_scratch[ACC_SCRATCH_BYTES];
 
-// Device address of g_accept_scratch on the current device, looked up once.
+// Device address of g_accept_scratch on the current device, looked up once
+// per device; the first lookup also loads the pass's kernels, so that later
+// calls load no module.
 static cudaError_t scratch_address(unsigned char **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -79,6 +96,8 @@ static cudaError_t scratch_address(unsigned char **out) {
     if (g_scratch_addr[dev] == nullptr) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_accept_scratch);
+        if (e != cudaSuccess) return e;
+        e = accept_preload();
         if (e != cudaSuccess) return e;
         g_scratch_addr[dev] = static_cast<unsigned char *>(p);
     }
@@ -102,6 +121,10 @@ extern "C" int joker_accept_noalloc(const joker_accept_seg *segs, int n_segs,
                                     const double *d_lnl, const uint64_t *d_max_key,
                                     int u_source, const double *d_u, int64_t *d_out_idx,
                                     double *d_out_lnl, int64_t *d_count, void *stream) {
+    // set-up first, so that a call with no segments is the warm-up call
+    unsigned char *scratch = nullptr;
+    cudaError_t e = scratch_address(&scratch);
+    if (e != cudaSuccess) return noalloc_cuda_fail("cudaGetSymbolAddress", e);
     if (n_segs <= 0) return JOKER_OK;
     if (!segs || !d_lnl || !d_max_key || !d_out_idx || !d_count)
         return noalloc_fail(JOKER_EINVAL, "joker_accept_noalloc: NULL argument");
@@ -121,9 +144,6 @@ extern "C" int joker_accept_noalloc(const joker_accept_seg *segs, int n_segs,
         return noalloc_fail(JOKER_ERANGE,
                             "joker_accept_noalloc: more 8192-sample blocks than "
                             "JOKER_NOALLOC_MAX_BLOCKS (about 2^24 samples)");
-    unsigned char *scratch = nullptr;
-    cudaError_t e = scratch_address(&scratch);
-    if (e != cudaSuccess) return noalloc_cuda_fail("cudaGetSymbolAddress", e);
     cudaStream_t st = (cudaStream_t)stream;
     joker_accept_seg *d_segs = reinterpret_cast<joker_accept_seg *>(scratch + OFF_SEGS);
     int64_t *d_base = reinterpret_cast<int64_t *>(scratch + OFF_BASE);

@@ -85,11 +85,19 @@ def get_trend_design_matrix(data, ids, poly_trend):
     return np.hstack((const, trend))
 
 
-def validate_prepare_data(data, poly_trend, n_offsets):
+def validate_prepare_data(data, poly_trend, n_offsets, ref_ids_order=True):
     """Concatenate one or several data sources (data_helpers.py:56-133).
 
     Returns (all_data, ids, trend_M).  Several sources share the reference time
     of the concatenated data, as in the reference.
+
+    ``RVData`` sorts the concatenated epochs by time (data.py:97-104), but the
+    reference builds the offset columns from the source ids in concatenation
+    order (data_helpers.py:115-133).  With ``ref_ids_order`` (the default,
+    for parity) the same happens here: when the sources' times interleave,
+    an epoch's offset column is that of the epoch at its position before the
+    sort.  ``ref_ids_order=False`` sorts the ids with the epochs, so that each
+    epoch gets its own source's column.
     """
     if isinstance(data, RVData):
         if n_offsets != 0:
@@ -122,7 +130,7 @@ def validate_prepare_data(data, poly_trend, n_offsets):
     if len(np.unique(ids)) - 1 != n_offsets:
         raise ValueError("Number of data IDs + 1 must equal the number of priors on constant "
                          "offsets specified (i.e. v0_offsets)")
-    order = np.argsort(t, kind="stable")
     all_data = RVData(t, rv, err)
-    ids = ids[order]
+    if not ref_ids_order:
+        ids = ids[np.argsort(t, kind="stable")]
     return all_data, ids, get_trend_design_matrix(all_data, ids, poly_trend)

@@ -360,6 +360,30 @@ def refine_max(stars, cache, lnl_buf, err, bound_keys, segments, exact=None, str
     return exact, n_ref
 
 
+def refine_band(stars, cache, lnl_buf, err, exact, segments, band=None, tol=None, stream=None):
+    """Band refinement of mixed ln L values (joker_refine_band): every sample
+    whose interval reaches within ``band`` of its slot's FP64 maximum
+    (``exact``, a MaxKeys from refine_max or accept_refined) and whose bound
+    exceeds ``tol`` is re-evaluated in FP64 in place (its bound set to 0).
+    Defaults: JOKER_MIXED_LNL_BAND and JOKER_MIXED_LNL_TOL.  Returns the
+    number of re-evaluated samples as a one-element CUDA tensor."""
+    band = nat.JOKER_MIXED_LNL_BAND if band is None else float(band)
+    tol = nat.JOKER_MIXED_LNL_TOL if tol is None else float(tol)
+    ns = len(segments)
+    arr, _ = _segments(segments, "array")
+    n_ref = torch.zeros(1, dtype=torch.int64, device=lnl_buf.device)
+    wbytes = nat.lib().joker_accept_workspace(arr, ns)
+    work = torch.empty(max(int(wbytes), 1), dtype=torch.uint8, device=lnl_buf.device)
+    nat.check(nat.lib().joker_refine_band(
+        stars.handle, cache.handle, arr, ns, ctypes.c_void_p(lnl_buf.data_ptr()),
+        ctypes.c_void_p(err.data_ptr()), exact.ptr(), band, tol,
+        ctypes.c_void_p(n_ref.data_ptr()), ctypes.c_void_p(work.data_ptr()), int(wbytes),
+        stream_handle(stream)), "joker_refine_band")
+    if stream is not None:
+        work.record_stream(stream)
+    return n_ref
+
+
 def accept_refined(stars, cache, lnl_buf, err, bound_keys, segments, u_source="pcg64", u=None,
                    out_idx=None, out_lnl=None, counts=None, exact=None, stream=None):
     """Acceptance over mixed-precision ln L with its error bounds, exact with

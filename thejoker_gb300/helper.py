@@ -14,7 +14,26 @@ from . import device as dev
 from .linear import multivariate_normal_draws
 from .samples import PACKED_ORDER
 
-__all__ = ["GPUJokerHelper"]
+__all__ = ["GPUJokerHelper", "band_refined_lnl"]
+
+
+def band_refined_lnl(stars, cache, out, precision, star=0, stream=None):
+    """Mixed-precision ln L of one star over every cache row into ``out`` (a
+    float64 CUDA tensor of cache.size values), with the band refinement: the
+    samples whose interval reaches within JOKER_MIXED_LNL_BAND of the star's
+    FP64 maximum and whose bound exceeds JOKER_MIXED_LNL_TOL are re-evaluated
+    in FP64, so every returned value within the band of the maximum is within
+    the tolerance of the FP64 path's.  Returns (per-sample bounds, FP64
+    maximum keys, number of re-evaluated samples)."""
+    S = cache.size
+    err = torch.empty((1, S), dtype=torch.float32, device=out.device)
+    bkeys = dev.MaxKeys(2)
+    dev.lnl(stars, cache, out.view(1, S), precision=precision, star0=star, n_sel=1,
+            err=err, bound_keys=bkeys, stream=stream)
+    seg = [dict(lnl_off=0, n=S, out_off=0, max_out=0, max_slot=0, star=star, row0=0)]
+    exact, n1 = dev.refine_max(stars, cache, out, err.view(-1), bkeys, seg, stream=stream)
+    n2 = dev.refine_band(stars, cache, out, err.view(-1), exact, seg, stream=stream)
+    return err.view(-1), exact, n1 + n2
 
 
 class GPUJokerHelper:
@@ -82,7 +101,12 @@ class GPUJokerHelper:
                 "joker_batch_marginal_ln_likelihood")
         else:
             cache = dev.PriorCache.from_samples(chunk, stream=stream)
-            dev.lnl(self._stars, cache, out.view(1, S), precision=self.precision, stream=stream)
+            if self.precision == "mixed_fp64_tail":
+                # this variant states no per-sample bound, so nothing is refined
+                dev.lnl(self._stars, cache, out.view(1, S), precision=self.precision,
+                        stream=stream)
+            else:
+                band_refined_lnl(self._stars, cache, out, self.precision, stream=stream)
         return out
 
     def batch_marginal_ln_likelihood(self, chunk):
