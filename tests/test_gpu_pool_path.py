@@ -122,7 +122,7 @@ class _Pool:
 def test_pool_rejection_matches_reference_helper(cuda, precision, randomize, n_batches,
                                                  pool_size):
     from thejoker_gb300 import TheJoker
-    st, prior, data, samples = _setup(41, 12, 6.0, 30000)
+    st, prior, data, samples = _setup(41, 4, 2.0, 30000)
     chunk = samples.pack()[0]
     pool = _Pool(pool_size) if pool_size is not None else None
     joker = TheJoker(prior, pool=pool, rng=np.random.default_rng(42), precision=precision)
@@ -183,7 +183,7 @@ def test_pool_iterative_safety_factor_differs_from_in_memory(cuda):
     1), so with the same generator they need not evaluate the same prefix;
     each matches its own restatement."""
     from thejoker_gb300 import TheJoker
-    st, prior, data, samples = _setup(63, 8, 15.0, 100000)
+    st, prior, data, samples = _setup(63, 4, 3.0, 100000)
     chunk = samples.pack()[0]
     j1 = TheJoker(prior, rng=np.random.default_rng(9))
     j2 = TheJoker(prior, rng=np.random.default_rng(9))

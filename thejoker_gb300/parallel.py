@@ -22,7 +22,7 @@ import numpy as np
 import torch
 
 __all__ = ["shard_rows", "shard_stars", "key_of", "value_of", "allreduce_max_keys",
-           "ShardedRejection", "gather_indices"]
+           "ShardedRejection", "StarShardedRejection", "gather_indices"]
 
 _TOP = -(1 << 63)
 
@@ -62,12 +62,25 @@ def value_of(k):
     return b.astype(np.uint64).view(np.float64)
 
 
+def _all_reduce(t, op, group=None):
+    """In-place all-reduce; a CUDA tensor goes through host memory when the
+    group's backend is gloo (its collectives are host-side)."""
+    import torch.distributed as dist
+    if t.is_cuda and dist.get_backend(group) == "gloo":
+        h = t.cpu()
+        dist.all_reduce(h, op=op, group=group)
+        t.copy_(h)
+    else:
+        dist.all_reduce(t, op=op, group=group)
+    return t
+
+
 def allreduce_max_keys(keys, group=None):
     """In-place MAX all-reduce of an int64 tensor holding uint64 keys."""
     import torch.distributed as dist
     flip = torch.tensor(_TOP, dtype=torch.int64, device=keys.device)
     m = torch.bitwise_xor(keys, flip)
-    dist.all_reduce(m, op=dist.ReduceOp.MAX, group=group)
+    _all_reduce(m, dist.ReduceOp.MAX, group)
     keys.copy_(torch.bitwise_xor(m, flip))
     return keys
 
@@ -136,5 +149,72 @@ class ShardedRejection:
                                                    exact=exact)
         c = int(cnt[0])
         total = torch.tensor([c], dtype=torch.int64, device="cuda")
-        dist.all_reduce(total, group=self.group)
+        _all_reduce(total, dist.ReduceOp.SUM, self.group)
         return idx[:min(c, self.max_out)].cpu().numpy(), int(total)
+
+
+class StarShardedRejection:
+    """Rejection sampling of many stars sharded across ranks by star, with no
+    exchange: every rank holds the whole prior cache and runs a BatchRejection
+    over its share of the stars (``shard_stars``, balanced by epoch count).
+    Star k uses the PCG64 stream of ``seeds[k]`` whichever rank owns it, so
+    the results do not depend on the number of ranks.
+
+    ``stars``: the full list of star dicts (as StarTable takes); ``world`` and
+    ``rank`` default to the process group's.  ``results`` returns this rank's
+    (global star indices, counts, indices, ln L); ``gather`` collects every
+    star's results in star order on every rank (host objects, so any backend).
+    """
+
+    def __init__(self, stars, cache, precision="mixed", jitter="reference", max_out=256,
+                 seeds=None, world=None, rank=None, group=None, chunk=None):
+        import torch.distributed as dist
+        from .batch import BatchRejection
+        if world is None:
+            world = dist.get_world_size(group) if dist.is_initialized() else 1
+        if rank is None:
+            rank = dist.get_rank(group) if dist.is_initialized() else 0
+        self.world, self.rank, self.group = int(world), int(rank), group
+        self.n_stars = len(stars)
+        n_ep = np.array([len(s["t"]) for s in stars])
+        self.mine = shard_stars(n_ep, self.world)[self.rank]
+        if seeds is None:
+            seeds = np.arange(self.n_stars)
+        seeds = np.asarray(seeds)
+        self.batch = None
+        if self.mine:
+            self.batch = BatchRejection([stars[k] for k in self.mine], cache, precision=precision,
+                                        jitter=jitter, max_out=max_out, seeds=seeds[self.mine],
+                                        chunk=chunk)
+
+    def run(self, row0=0, count=None, stream=None):
+        if self.batch is not None:
+            self.batch.run(row0=row0, count=count, stream=stream)
+        return self
+
+    def results(self):
+        """(global star indices, counts, [indices], [ln L]) of this rank's stars."""
+        if self.batch is None:
+            return [], np.zeros(0, dtype=np.int64), [], []
+        counts, idx, ll = self.batch.results()
+        return list(self.mine), counts, idx, ll
+
+    def gather(self):
+        """(counts, [indices per star], [ln L per star]) of all stars, in star
+        order, on every rank."""
+        import torch.distributed as dist
+        local = self.results()
+        if self.world == 1 or not dist.is_initialized():
+            parts = [local]
+        else:
+            parts = [None] * self.world
+            dist.all_gather_object(parts, local, group=self.group)
+        counts = np.zeros(self.n_stars, dtype=np.int64)
+        idx = [None] * self.n_stars
+        ll = [None] * self.n_stars
+        for ks, c, i, l in parts:
+            for j, k in enumerate(ks):
+                counts[k] = c[j]
+                idx[k] = i[j]
+                ll[k] = l[j]
+        return counts, idx, ll
