@@ -39,6 +39,10 @@ sys.path.insert(0, HERE)
 
 N_EPOCHS = 40
 SPAN_D = 3000.0
+# precision of the mixed path timed in every mode ("mixed_fast": FP32 epoch
+# sums, the first pass of the refined acceptance; "mixed": float-float sums);
+# set from --precision
+MIXED = "mixed_fast"
 SEED_STAR = 2
 SEED_CACHE = 0
 
@@ -92,11 +96,16 @@ def fill_cache_host(out, seed, threads=16):
 # accept) = 21 at L = 2.
 FLOPS_PER_EPOCH = 62
 FLOPS_PER_SAMPLE = 21
-# FP32 operations the mixed kernel issues per (sample, epoch) with the jitter
+# FP32 operations each mixed kernel issues per (sample, epoch) with the jitter
 # applied at L = 2, counted from its source (FMA = 2 flops, special-function
-# ops = 1), and per sample for the setup and the tail (roofline.issued_frac).
-ISSUED_FLOPS_PER_EPOCH = 196
-ISSUED_FLOPS_PER_SAMPLE = 60
+# ops = 1), and per sample for the setup and the tail (roofline.issued_frac):
+# float-float sums (mixed) and FP32 sums (mixed_fast, whose float-float tail
+# and error bound cost more per sample).
+ISSUED_FLOPS = {"mixed": (196, 60), "mixed_fast": (126, 420)}
+KERNEL_NAME = {"mixed": "lnl_mixed2_kernel<L=2, jitter, VAR 0, cache form> (two samples per "
+                        "thread, paired FP32, float-float sums)",
+               "mixed_fast": "lnl_fast2_kernel<L=2, jitter, cache form> (two samples per "
+                             "thread, paired FP32, FP32 sums re-centred on the trend fit)"}
 # Algorithmic HBM bytes per sample of the cache-form mixed kernel (36 B prepared
 # sample read, 8 B ln L + 4 B bound written) and the DRAM bytes ncu measured per
 # sample (read + write of one 2^24-sample launch / 2^24), scaled to a launch.
@@ -226,12 +235,12 @@ def run_ours(args, rank, world, dist):
     torch.cuda.empty_cache()
     # work-item size from the autotuner, measured here on this workload
     from thejoker_gb300 import autotune
-    tuned, tune_ms = autotune.tune(table, cache, precision="mixed", count=min(S, 1 << 26),
+    tuned, tune_ms = autotune.tune(table, cache, precision=MIXED, count=min(S, 1 << 26),
                                    reps=2)
     if world > 1:
-        runner = ShardedRejection(table, cache, row0=rank * S, precision="mixed", max_out=S)
+        runner = ShardedRejection(table, cache, row0=rank * S, precision=MIXED, max_out=S)
     else:
-        runner = BatchRejection(table, cache, precision="mixed", max_out=S, seeds=[1000],
+        runner = BatchRejection(table, cache, precision=MIXED, max_out=S, seeds=[1000],
                                 timing=True)
     lnl_ms = []
 
@@ -275,7 +284,7 @@ def run_ours(args, rank, world, dist):
     if world == 1:
         del runner, cache
         torch.cuda.empty_cache()
-        hr = HostRejection(table, S, precision="mixed", slice_rows=args.h2d_chunk, max_out=S)
+        hr = HostRejection(table, S, precision=MIXED, slice_rows=args.h2d_chunk, max_out=S)
 
         def e2e_step():
             hr.run(host, [(pcg_state, pcg_inc)])
@@ -338,7 +347,8 @@ def run_ours(args, rank, world, dist):
     total = S * world
     flops = S * (N_EPOCHS * FLOPS_PER_EPOCH + FLOPS_PER_SAMPLE)
     achieved = flops / (kern_ms * 1e-3) / 1e12
-    issued = S * (N_EPOCHS * ISSUED_FLOPS_PER_EPOCH + ISSUED_FLOPS_PER_SAMPLE)
+    ipe, ips = ISSUED_FLOPS[MIXED]
+    issued = S * (N_EPOCHS * ipe + ips)
     peak = args.fp32_peak
     hbm_peak, hbm_src = _hbm_peak()
     line = {
@@ -358,7 +368,7 @@ def run_ours(args, rank, world, dist):
                                f"applied, prior cache 2^{int(math.log2(S))} samples per GPU",
                    "prior_samples_per_gpu": S, "n_epochs": N_EPOCHS, "n_linear": 2,
                    "l2": "inputs larger than L2 (cache 76 B/sample resident, 2^28 samples)",
-                   "precision": "mixed", "u_source": "numpy PCG64 stream regenerated on device",
+                   "precision": MIXED, "u_source": "numpy PCG64 stream regenerated on device",
                    "accept": "refined to the FP64 decisions",
                    "autotune": {"chunk": tuned, "ms_per_2^26_samples": tune_ms}},
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "samples/s",
@@ -375,8 +385,7 @@ def run_ours(args, rank, world, dist):
                      "issued_tflops": issued / (kern_ms * 1e-3) / 1e12,
                      "issued_frac": issued / (kern_ms * 1e-3) / 1e12 / peak,
                      "issued_work": f"FP32 operations issued, counted from the kernel source: "
-                                    f"{ISSUED_FLOPS_PER_EPOCH} per (sample, epoch) + "
-                                    f"{ISSUED_FLOPS_PER_SAMPLE} per sample",
+                                    f"{ipe} per (sample, epoch) + {ips} per sample",
                      "traffic": args.traffic if args.traffic else DRAM_BYTES_PER_SAMPLE * S,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
                                        "2^24-sample launch, scaled by samples",
@@ -384,8 +393,7 @@ def run_ours(args, rank, world, dist):
                              "peak_gbs": hbm_peak,
                              "frac": BYTES_PER_SAMPLE * S / (kern_ms * 1e-3) / 1e9 / hbm_peak,
                              "peak_source": hbm_src},
-                     "kernel": "lnl_mixed2_kernel<L=2, jitter, VAR 0, cache form> (two samples "
-                               "per thread, paired FP32)",
+                     "kernel": KERNEL_NAME[MIXED],
                      "kernel_ms": kern_ms,
                      "peak_source": "FP32 FMA throughput measured on a GB300: independent FMA "
                                     "chains, 74.9 TFLOP/s paired (73.1 scalar)",
@@ -424,7 +432,7 @@ def _parity_slice(table, cache, b64, S):
     lm = torch.empty((1, S), dtype=torch.float64, device="cuda")
     err = torch.empty((1, S), dtype=torch.float32, device="cuda")
     bk = dev.MaxKeys(2)
-    dev.lnl(table, cache, lm, precision="mixed", count=S, err=err, bound_keys=bk)
+    dev.lnl(table, cache, lm, precision=MIXED, count=S, err=err, bound_keys=bk)
     raw = lm.clone()
     seg = [dict(lnl_off=0, n=S, out_off=0, max_out=0, max_slot=0, star=0, row0=0)]
     exact, n1 = dev.refine_max(table, cache, lm.view(-1), err.view(-1), bk, seg)
@@ -433,7 +441,7 @@ def _parity_slice(table, cache, b64, S):
     band_nats = nat.JOKER_MIXED_LNL_BAND
     mx = a64.max()
     band = a64 >= mx - band_nats
-    bm = BatchRejection(table, cache, precision="mixed", max_out=S, seeds=[1000])
+    bm = BatchRejection(table, cache, precision=MIXED, max_out=S, seeds=[1000])
     bm.run(count=S)
     c64, i64, l64k = b64.results()
     cm, im, lmk = bm.results()
@@ -476,10 +484,10 @@ def batched_measure(n_stars, S, warmup=1, steps=1, subset_stars=64, subset_sampl
     table = dev.StarTable(stars)
     sub_t = dev.StarTable(stars[:256])
     sub_t.n_epochs = table.n_epochs            # tune for the survey's epoch counts
-    tuned, tune_ms = autotune.tune(sub_t, cache, precision="mixed", count=min(S, 1 << 22),
+    tuned, tune_ms = autotune.tune(sub_t, cache, precision=MIXED, count=min(S, 1 << 22),
                                    reps=1)
     del sub_t
-    br = BatchRejection(table, cache, precision="mixed", max_out=256,
+    br = BatchRejection(table, cache, precision=MIXED, max_out=256,
                         seeds=np.arange(n_stars) + rank * n_stars, group=group)
     for _ in range(warmup):
         br.run()
@@ -502,14 +510,14 @@ def batched_measure(n_stars, S, warmup=1, steps=1, subset_stars=64, subset_sampl
     Ssub = min(S, subset_samples)
     table_sub = dev.StarTable(stars[:sub])
     res = {}
-    for prec in ("mixed", "fp64"):
+    for key, prec in (("mixed", MIXED), ("fp64", "fp64")):
         b = BatchRejection(table_sub, cache, precision=prec, max_out=256, seeds=np.arange(sub))
         b.run(count=Ssub)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         b.run(count=Ssub)
         torch.cuda.synchronize()
-        res[prec] = (time.perf_counter() - t0, b.results())
+        res[key] = (time.perf_counter() - t0, b.results())
         del b
     c_m, i_m, _ = res["mixed"][1]
     c_64, i_64, _ = res["fp64"][1]
@@ -584,7 +592,7 @@ def run_iterative(args, rank, world):
     cache = dev.PriorCache.from_samples(host)
     table = dev.StarTable(stars)
     seeds = lambda k: np.arange(n_stars) + 7919 * k + rank * n_stars
-    it = IterativeBatch(table, cache, n_req, precision="mixed", seeds=seeds(0))
+    it = IterativeBatch(table, cache, n_req, precision=MIXED, seeds=seeds(0))
     it.run()
     for w in range(args.warmup):
         it.reset(seeds(w + 1)).run()
@@ -602,7 +610,7 @@ def run_iterative(args, rank, world):
     sub = min(args.subset_stars, n_stars)
     table_sub = dev.StarTable(stars[:sub])
     res = {}
-    for prec in ("mixed", "fp64"):
+    for key, prec in (("mixed", MIXED), ("fp64", "fp64")):
         b = IterativeBatch(table_sub, cache, n_req, precision=prec, seeds=np.arange(sub))
         b.run()
         torch.cuda.synchronize()
@@ -611,11 +619,11 @@ def run_iterative(args, rank, world):
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         stt, idx, _ = b.results()
-        res[prec] = (dt, stt, idx)
+        res[key] = (dt, stt, idx)
         b.close()
     same = bool(np.array_equal(res["mixed"][1], res["fp64"][1]) and
                 all(np.array_equal(a, b) for a, b in zip(res["mixed"][2], res["fp64"][2])))
-    eager = IterativeBatch(table, cache, n_req, precision="mixed", seeds=seeds(100))
+    eager = IterativeBatch(table, cache, n_req, precision=MIXED, seeds=seeds(100))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     eager.run(use_graph=False)
@@ -714,7 +722,7 @@ def serving_measure(S, rates, window=4.0, n_all=20000, slots=1024, round_budget=
                        seed=100000 + k)
 
     eng = ServingEngine(cache, n_slots=slots, max_epochs=200, n_linear=2,
-                        max_requested=512, precision="mixed", round_budget=round_budget,
+                        max_requested=512, precision=MIXED, round_budget=round_budget,
                         pool_fraction=0.6)
     # warm-up: the first rounds load the kernels and capture the round graph
     for k in range(min(n_all, 64)):
@@ -827,7 +835,7 @@ def run_small(args, rank, world):
     table = dev.StarTable([star])
     from thejoker_gb300 import _native as nat
     res = {}
-    for prec in ("fp64", "mixed"):
+    for key, prec in (("fp64", "fp64"), ("mixed", MIXED)):
         br = BatchRejection(table, cache, precision=prec, max_out=S, seeds=[1])
         for _ in range(args.warmup):
             br.run()
@@ -840,7 +848,7 @@ def run_small(args, rank, world):
         ms = (time.perf_counter() - t0) * 1e3 / args.steps
         launches = nat.lib().joker_launch_count() - launches0
         counts, idx, ll = br.results()
-        res[prec] = (ms, idx[0], br.lnl[0, :S].cpu().numpy(), ll[0])
+        res[key] = (ms, idx[0], br.lnl[0, :S].cpu().numpy(), ll[0])
     d = np.abs(res["mixed"][2] - res["fp64"][2])
     kept_d = np.abs(res["mixed"][3] - res["fp64"][2][res["mixed"][1]]) \
         if np.array_equal(res["fp64"][1], res["mixed"][1]) else np.array([np.inf])
@@ -1039,6 +1047,8 @@ def main():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--headline-only", action="store_true",
                    help="default mode: skip the batched and serving sub-objects")
+    p.add_argument("--precision", default="mixed_fast", choices=["mixed_fast", "mixed"],
+                   help="the mixed path: FP32 epoch sums (mixed_fast) or float-float sums")
     p.add_argument("--config", default="single",
                    choices=["single", "small", "batched", "iterative", "serving",
                             "posterior"])
@@ -1053,6 +1063,8 @@ def main():
     p.add_argument("--group", type=int, default=None)
     p.add_argument("--subset-stars", type=int, default=64)
     args = p.parse_args()
+    global MIXED
+    MIXED = args.precision
     if args.samples is None:
         args.samples = {"single": 1 << 28, "small": 1 << 20, "batched": 1 << 24,
                         "iterative": 1 << 22, "serving": 1 << 28,

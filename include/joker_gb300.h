@@ -56,6 +56,12 @@ extern "C" {
 #define JOKER_MIXED_ACCURATE 2  /* as JOKER_MIXED with correctly rounded sincosf */
 #define JOKER_MIXED_FP64_TAIL 3 /* as JOKER_MIXED with the per-sample solve in FP64
                                    instead of float-float (no error bound) */
+#define JOKER_MIXED_FAST 4      /* the first pass of the refined acceptance: FP32
+                                   epoch sums re-centred on each star's trend-only
+                                   fit, float-float solve, and a rigorous
+                                   per-sample bound (looser than JOKER_MIXED's);
+                                   more than three linear parameters with the
+                                   jitter applied run as JOKER_MIXED */
 
 /* jitter handling (the reference Cython computes the jittered inverse variance
    but never reads it, fast_likelihood.pyx:458; its NumPy test oracle applies
@@ -216,9 +222,10 @@ int joker_accept(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
  * max_slot) receives the FP64 maxima -- or, with max_given != 0, already holds
  * them (from joker_refine_max, e.g. combined over ranks that each own a range
  * of the same star's samples).  d_n_refined (optional) counts the re-evaluated
- * samples.  Every kept sample whose bound exceeds JOKER_MIXED_LNL_TOL is
- * re-evaluated as well, so every kept ln L (d_out_lnl) is within that of the
- * FP64 value.  Each re-evaluated sample's FP64 ln L is written back to d_lnl
+ * samples.  When d_out_lnl is given, every kept sample written out (the first
+ * max_out of a segment) whose bound exceeds JOKER_MIXED_LNL_TOL is
+ * re-evaluated as well, so every ln L in d_out_lnl is within that of the FP64
+ * value.  Each re-evaluated sample's FP64 ln L is written back to d_lnl
  * and its bound in d_err set to 0.  Same workspace as joker_accept. */
 int joker_accept_refined(const joker_stars *stars, const joker_cache *cache,
                          const joker_accept_seg *segs, int n_segs, double *d_lnl,

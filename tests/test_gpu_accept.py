@@ -146,9 +146,10 @@ def test_thejoker_iterative_matches_reference_loop(cuda):
     np.testing.assert_array_equal(out["P"], chunk[good[:8], 0])
 
 
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fast"])
 @pytest.mark.parametrize("n_ep,K,jitter", [(3, 1.0, "reference"), (12, 5.0, "reference"),
                                            (40, 30.0, "applied"), (8, 0.5, "applied")])
-def test_refined_accept_equals_fp64_accept(cuda, n_ep, K, jitter):
+def test_refined_accept_equals_fp64_accept(cuda, n_ep, K, jitter, precision):
     """Acceptance over mixed ln L with refinement keeps exactly what the FP64
     path keeps (same uniforms), while re-evaluating few samples in FP64."""
     from thejoker_gb300 import device as dev
@@ -164,7 +165,7 @@ def test_refined_accept_equals_fp64_accept(cuda, n_ep, K, jitter):
     lnlm = torch.empty((1, S), dtype=torch.float64, device="cuda")
     err = torch.empty((1, S), dtype=torch.float32, device="cuda")
     km, bk = dev.MaxKeys(1), dev.MaxKeys(2)
-    dev.lnl(table, cache, lnlm, precision="mixed", max_keys=km, err=err, bound_keys=bk)
+    dev.lnl(table, cache, lnlm, precision=precision, max_keys=km, err=err, bound_keys=bk)
     gen = np.random.default_rng(5)
     pcg = dev.pcg64_state(gen)
     seg = dict(lnl_off=0, n=S, out_off=0, max_out=S, max_slot=0, star=0, row0=0,
@@ -173,7 +174,7 @@ def test_refined_accept_equals_fp64_accept(cuda, n_ep, K, jitter):
     im, _, cm, exact, nref = dev.accept_refined(table, cache, lnlm.view(-1), err.view(-1), bk,
                                                 [seg])
     n64, nm = int(c64[0]), int(cm[0])
-    print(n_ep, K, jitter, "accepted", n64, "refined in FP64", int(nref[0]))
+    print(n_ep, K, jitter, precision, "accepted", n64, "refined in FP64", int(nref[0]))
     assert n64 == nm
     np.testing.assert_array_equal(i64[:n64].cpu().numpy(), im[:nm].cpu().numpy())
     # the refinement re-evaluates in FP64 through a separately compiled call
@@ -182,8 +183,9 @@ def test_refined_accept_equals_fp64_accept(cuda, n_ep, K, jitter):
     assert int(nref[0]) < S // 50
 
 
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fast"])
 @pytest.mark.parametrize("K,sig", [(198.0, (0.1, 1.0)), (0.0, (2.0, 5.0))])
-def test_refined_kept_lnl_within_tolerance(cuda, K, sig):
+def test_refined_kept_lnl_within_tolerance(cuda, K, sig, precision):
     """Every kept sample's ln L (out_lnl) is within JOKER_MIXED_LNL_TOL of the FP64
     value: kept samples whose bound is looser are re-evaluated in FP64.  The
     first star is so well constrained that the best prior sample still has
@@ -202,7 +204,7 @@ def test_refined_kept_lnl_within_tolerance(cuda, K, sig):
     mix = torch.empty((1, S), dtype=torch.float64, device="cuda")
     err = torch.empty((1, S), dtype=torch.float32, device="cuda")
     bk = dev.MaxKeys(2)
-    dev.lnl(table, cache, mix, precision="mixed", err=err, bound_keys=bk)
+    dev.lnl(table, cache, mix, precision=precision, err=err, bound_keys=bk)
     st_, inc = dev.pcg64_state(np.random.default_rng(5))
     seg = dict(lnl_off=0, n=S, idx_base=0, out_off=0, max_out=S, max_slot=0, star=0, row0=0,
                pcg=(st_, inc, 0))

@@ -35,14 +35,14 @@ def _hard_chunk(rng, S, jitter):
     return c
 
 
-def _both(table, cache, S):
+def _both(table, cache, S, precision="mixed"):
     from thejoker_gb300 import device as dev
     l64 = torch.empty((1, S), dtype=torch.float64, device="cuda")
     dev.lnl(table, cache, l64, precision="fp64")
     lm = torch.empty((1, S), dtype=torch.float64, device="cuda")
     err = torch.empty((1, S), dtype=torch.float32, device="cuda")
     bk = dev.MaxKeys(2)
-    dev.lnl(table, cache, lm, precision="mixed", err=err, bound_keys=bk)
+    dev.lnl(table, cache, lm, precision=precision, err=err, bound_keys=bk)
     return l64, lm, err, bk
 
 
@@ -51,7 +51,8 @@ def _both(table, cache, S):
                                                 (200, 2, "reference", 3000.0),
                                                 (64, 3, "reference", 4000.0),
                                                 (5, 1, "applied", 300.0)])
-def test_bound_holds_and_band_meets_tolerance(cuda, N, poly, jitter, base):
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fast"])
+def test_bound_holds_and_band_meets_tolerance(cuda, N, poly, jitter, base, precision):
     from thejoker_gb300 import device as dev
     rng = np.random.default_rng(1000 + N + poly)
     st = synth_star(rng, N, base=base, sig=(0.05, 0.5), K=25.0, poly=poly)
@@ -59,7 +60,7 @@ def test_bound_holds_and_band_meets_tolerance(cuda, N, poly, jitter, base):
     chunk = _hard_chunk(rng, S, jitter == "applied")
     table = dev.StarTable([st], jitter=jitter)
     cache = dev.PriorCache.from_samples(chunk)
-    l64, lm, err, bk = _both(table, cache, S)
+    l64, lm, err, bk = _both(table, cache, S, precision)
     a64 = l64[0].cpu().numpy()
     am = lm[0].cpu().numpy()
     ev = err[0].cpu().numpy()
@@ -108,7 +109,8 @@ def test_helper_mixed_marginal_ln_likelihood_within_tolerance(cuda):
     assert np.max(np.abs(a - b)[band]) <= TOL
 
 
-def test_refined_accept_equals_fp64_on_the_4096_star_survey(cuda):
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fast"])
+def test_refined_accept_equals_fp64_on_the_4096_star_survey(cuda, precision):
     """The batched configuration (4096 stars, epochs log-uniform [3, 256], 30%
     with companions) over a 2^17-sample prior cache: for every star the
     refined mixed acceptance keeps exactly the FP64 path's indices, and every
@@ -121,12 +123,12 @@ def test_refined_accept_equals_fp64_on_the_4096_star_survey(cuda):
     cache = dev.PriorCache.from_samples(fill_prior_cache(np.empty((S, 5)), 0))
     table = dev.StarTable(stars)
     res = {}
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", precision):
         b = BatchRejection(table, cache, precision=prec, max_out=512, seeds=np.arange(4096))
         b.run()
         res[prec] = b.results()
     c64, i64, l64 = res["fp64"]
-    cm, im, lm = res["mixed"]
+    cm, im, lm = res[precision]
     np.testing.assert_array_equal(c64, cm)
     for k in range(4096):
         np.testing.assert_array_equal(i64[k], im[k])

@@ -13,6 +13,7 @@ JOKER_FP64 = 0
 JOKER_MIXED = 1
 JOKER_MIXED_ACCURATE = 2
 JOKER_MIXED_FP64_TAIL = 3
+JOKER_MIXED_FAST = 4
 JOKER_JITTER_REFERENCE = 0
 JOKER_JITTER_APPLIED = 1
 JOKER_U_ARRAY = 0

@@ -272,6 +272,32 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
     r.logdet_const = (double)(n * LOG2PI - slog_ivar + slog_lam + logdetC);
     r.log_norm_rest = (double)(n * LOG2PI + slog_lam);
     r.sum_log_ivar = (double)slog_ivar;
+    // FP32-sum path: the residual of the trend-only fit r_c = y' - T^T beta0
+    // (beta0 = C^-1 c, as stored in cC) and the magnitudes its bound needs
+    long double Cn = 0.0L, ivmax = 0.0L, Wjj[MAXL] = {0.0L}, kappa = 0.0L;
+    for (int j = 1; j < L; ++j) kappa += (long double)r.cC[j] * r.cC[j] / (long double)lamk[j];
+    for (int i = 0; i < n; ++i) {
+        long double yp = rv[i];
+        for (int j = 1; j < L; ++j) yp -= (long double)muk[j] * trend_M[(size_t)i * T + (j - 1)];
+        long double rc = yp;
+        for (int j = 1; j < L; ++j) rc -= (long double)r.cC[j] * trend_M[(size_t)i * T + (j - 1)];
+        const long double w = ivar[i];
+        Cn += w * rc * rc;
+        ivmax = std::max(ivmax, w);
+        for (int j = 1; j < L; ++j) {
+            const long double Tj = trend_M[(size_t)i * T + (j - 1)];
+            Wjj[j] += w * Tj * Tj;
+        }
+        float *r32 = rec32 + (size_t)i * REC32;
+        r32[18] = (float)rc;
+        r32[19] = (float)(w * rc);
+    }
+    split_ff((double)kappa, r.kappa_hi, r.kappa_lo);
+    split_ff(r.logdet_const, r.ldc_hi, r.ldc_lo);
+    split_ff((double)(n * LOG2PI + slog_lam - slog_ivar), r.lnr_hi, r.lnr_lo);
+    r.Cn = (float)(Cn * (1.0L + 1e-6L));
+    r.ivar_max = (float)(ivmax * (1.0L + 1e-6L));
+    for (int j = 1; j < L; ++j) r.Wjj[j] = (float)(Wjj[j] * (1.0L + 1e-6L));
     return JOKER_OK;
 }
 
@@ -626,7 +652,6 @@ static int run_lnl(const joker_stars *s, int precision, LnlArgs a, int block,
     CUDA_TRY(launch_lnl(precision, s->L, s->jitter == JOKER_JITTER_APPLIED, a, block, st));
     return JOKER_OK;
 }
-
 extern "C" int joker_batch_marginal_ln_likelihood(const joker_stars *s, int star,
                                                   const double *d_chunk, int64_t n_samples,
                                                   double *d_lnl, void *stream) {
@@ -700,7 +725,7 @@ extern "C" int joker_lnl(const joker_stars *s, const joker_cache *c, int star0, 
                          int64_t chunk, void *stream) {
     if (!s || !c) return fail(JOKER_EINVAL, "joker_lnl: NULL handle");
     if (precision != JOKER_FP64 && precision != JOKER_MIXED && precision != JOKER_MIXED_ACCURATE &&
-        precision != JOKER_MIXED_FP64_TAIL)
+        precision != JOKER_MIXED_FP64_TAIL && precision != JOKER_MIXED_FAST)
         return fail(JOKER_EINVAL, "joker_lnl: unknown precision %d", precision);
     if (star0 < 0 || n_sel < 0 || star0 + n_sel > s->n_stars)
         return fail(JOKER_EINVAL, "joker_lnl: stars [%d, %d) outside [0, %d)", star0,
@@ -860,6 +885,8 @@ static int refined_setup(const joker_stars *s, const joker_cache *c, const joker
     a.exact_key = (unsigned long long *)d_exact_key;
     a.stars = s->d_stars;
     a.ep64 = s->d_ep64;
+    a.ep32 = s->d_ep32;
+    a.err_c0 = err_c0();
     a.P = c->P; a.E = c->E; a.OM = c->OM; a.M0 = c->M0; a.S = c->S;
     a.stride = c->stride;
     a.L = s->L;

@@ -177,6 +177,17 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_candidates_kernel(AcceptAr
     }
 }
 
+// The maximum's refinement: a candidate whose interval -- tightened by the
+// float-float tier, or as scanned -- no longer reaches the star's largest
+// lower bound (raised by that tier) cannot be the maximum.
+__device__ __forceinline__ bool below_lower_bound(const AcceptArgs &a, const joker_accept_seg &sg,
+                                                  int64_t i) {
+    const double v = a.lnl[sg.lnl_off + i];
+    const float er = a.err[sg.lnl_off + i];
+    if (!(er < 1e29f) || !(v == v)) return false;
+    return v + (double)er < key_to_double(a.bound_key[2 * sg.max_slot + 1]);
+}
+
 // FP64 re-evaluation of the listed samples, one warp per sample (lanes over
 // epochs).  MODE 0 raises the FP64 maximum; MODE 1 decides the undecided
 // samples against it and their own uniforms; MODE 2 (the band refinement)
@@ -192,6 +203,7 @@ __global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
         const int si = (int)(ent >> 40);
         const int64_t i = ent & (((int64_t)1 << 40) - 1);
         const joker_accept_seg sg = a.segs[si];
+        if (MODE == 0 && below_lower_bound(a, sg, i)) continue;     // uniform in the warp
         const int64_t r = (sg.row0 + i) * a.stride;
         const double v = fp64_lnl_warp(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
                                        a.OM[r], a.M0[r], a.S[r]);
@@ -263,6 +275,7 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
             bits &= bits - 1;
             const int64_t i = first + b;
             if (i >= sg.n) continue;
+            if (MODE == 0 && below_lower_bound(a, sg, i)) continue;
             const int64_t r = (sg.row0 + i) * a.stride;
             const double v = fp64_lnl_sample(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
                                              a.OM[r], a.M0[r], a.S[r]);
@@ -404,9 +417,6 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
                     dec = interval_test(v, er, mx, u);
                 }
             }
-            // an accepted sample whose bound exceeds JOKER_MIXED_LNL_TOL is
-            // re-evaluated in FP64 too, so that every kept ln L is that close
-            if (refine && dec == 1 && !(er <= (float)JOKER_MIXED_LNL_TOL)) dec = -1;
             keep = dec == 1;
             amb = dec < 0;
         }
@@ -461,6 +471,12 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_scan_kernel(AcceptArgs a) 
     if (threadIdx.x == 0) a.count[si] = carry;
 }
 
+// Emit: each accepted sample's rank in its segment; the first max_out of them
+// are written out.  FLAG (refined pass with ln L outputs, before the writing
+// pass): every output sample whose bound exceeds JOKER_MIXED_LNL_TOL is put
+// on flag list 0 for re-evaluation in FP64 (or, past the list's capacity,
+// re-evaluated here), so that every ln L written out is within that of FP64.
+template <bool FLAG>
 __global__ void __launch_bounds__(ACC_THREADS) accept_emit_kernel(AcceptArgs a) {
     __shared__ int s_scan[ACC_THREADS];
     const int64_t nbk = n_blocks(a);
@@ -487,8 +503,24 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_emit_kernel(AcceptArgs a) 
         const int b = __ffs(wm) - 1;
         wm &= wm - 1;
         const int64_t i = first + b;
-        a.out_idx[sg.out_off + pos] = sg.idx_base + i;
-        if (a.out_lnl) a.out_lnl[sg.out_off + pos] = a.lnl[sg.lnl_off + i];
+        if (FLAG) {
+            if (!(a.err[sg.lnl_off + i] <= (float)JOKER_MIXED_LNL_TOL)) {
+                const unsigned long long q = atomicAdd(a.flag_count, 1ull);
+                if ((int64_t)q < a.flag_cap) {
+                    a.flag_list[q] = ((int64_t)si << 40) | i;
+                } else {
+                    const int64_t r = (sg.row0 + i) * a.stride;
+                    const double v = fp64_lnl_sample(a.L, a.jit, a.stars[sg.star], a.ep64,
+                                                     a.P[r], a.E[r], a.OM[r], a.M0[r], a.S[r]);
+                    if (a.n_refined) atomicAdd(a.n_refined, 1ull);
+                    const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
+                    const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
+                }
+            }
+        } else {
+            a.out_idx[sg.out_off + pos] = sg.idx_base + i;
+            if (a.out_lnl) a.out_lnl[sg.out_off + pos] = a.lnl[sg.lnl_off + i];
+        }
         ++pos;
     }
     __syncthreads();
@@ -514,7 +546,7 @@ cudaError_t accept_preload() {
     cudaFuncAttributes fa;
     cudaError_t e = cudaFuncGetAttributes(&fa, accept_mark_kernel);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, accept_scan_kernel);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, accept_emit_kernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, accept_emit_kernel<false>);
     return e;
 }
 
@@ -551,6 +583,8 @@ cudaError_t launch_refine_band(const AcceptArgs &a, int64_t total_blocks, double
     return launch_fp64_words(2, a, total_blocks, st);
 }
 
+cudaError_t launch_tier2(const AcceptArgs &a, cudaStream_t st);
+
 cudaError_t launch_refine_max(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st) {
     if (total_blocks <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(a.flag_count, 0, 2 * sizeof(unsigned long long), st);
@@ -558,6 +592,10 @@ cudaError_t launch_refine_max(const AcceptArgs &a, int64_t total_blocks, cudaStr
     accept_candidates_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
     count_launch();
     e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // the float-float tier tightens the listed candidates and raises the
+    // lower bounds; FP64 then takes only those still reaching them
+    e = launch_tier2(a, st);
     if (e != cudaSuccess) return e;
     return launch_fp64_words(0, a, total_blocks, st);
 }
@@ -586,7 +624,18 @@ cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || total_blocks == 0) return e;
-    accept_emit_kernel<<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
+    if (a.err != nullptr && a.out_lnl != nullptr) {
+        // the ln L written out: FP64 for every output sample with a loose bound
+        if ((e = cudaMemsetAsync(a.flag_count, 0, sizeof(unsigned long long), st)) != cudaSuccess)
+            return e;
+        accept_emit_kernel<true><<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        accept_fp64_list_kernel<2><<<152 * 4, 256, 0, st>>>(a);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    accept_emit_kernel<false><<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }

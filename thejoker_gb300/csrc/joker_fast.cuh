@@ -1,0 +1,406 @@
+// The FP32-sum ln L kernel (JOKER_MIXED_FAST): the first pass of the refined
+// acceptance.  Same phase, FP32 Kepler and RV column as the mixed kernel,
+// but every epoch sum is a plain FP32 accumulation, and each sample carries a
+// rigorous bound err on |lnL - lnL_FP64| built from the sums' magnitudes.
+//
+// Re-centred sums.  With beta0 = C^-1 c the star's trend-only fit (any fixed
+// shift would do) and r_c = y' - T^T beta0 its residual, for every sample
+//   chi2 = r^T W r - q^T G^-1 q = C + beta0^T Lambda_T^-1 beta0 - q'^T G^-1 q',
+//   C = r_c^T W r_c,  q' = M W r_c - Lambda^-1 (0, beta0),
+// exactly (substitute r = r_c + T^T beta0).  The large terms of a systemic
+// velocity never enter the FP32 sums: r_c is the scatter about the trend
+// fit.  Since T W0 r_c = Lambda_T^-1 beta0 for the nominal weights
+// W0 = diag(ivar),  q'_T = T (W - W0) r_c = -s^2 sum_i w_i ivar_i r_c,i T_i,
+// one more product per term and no cancellation.  A K prior mean mu0 enters
+// as r_c -> r_c - mu0 m, which the tail applies to the sums.  Without jitter
+// the trend block and C + kappa = chi2_0 are folded on the host.
+//
+// Error bound.  A sequential FP32 sum of N terms, each with k roundings, is
+// off by at most gamma sum |term|, gamma = (N + k) u / (1 - (N + k) u),
+// u = 2^-24; the FP32 weight and the r_c, ivar r_c and T_j stored as floats
+// are term-wise relative perturbations folded into k.  The magnitudes
+// sum |term| come from the non-negative diagonal sums by Cauchy-Schwarz
+// (sum |w m r_c| <= sqrt(F C), ...).  With theta = G^-1 q' (the best-fit
+// linear parameters) and dq', dG the sums' errors,
+//   d chi2 = dC - 2 theta.dq' + theta^T dG theta - (dq' - dG theta)^T
+//            (G + dG)^-1 (dq' - dG theta),
+// bounded term by term, the last by 2 tr(G^-1) |dq' - dG theta|^2 while
+// |dG|_F tr(G^-1) < 1/4 (else err = 1e30: no bound, always refined); and
+// |d log det G| <= |tr(G^-1 dG)| + 1.34 |G^-1 dG|_F^2.  The FP32 column's own
+// error (phase rounding, FP32 Kepler; the constant err_c0 is empirical)
+// enters as in the mixed kernel.  The tail runs in float-float; the only FP64
+// arithmetic per sample is the conversion of ln L to a double.
+#pragma once
+#include "joker_mixed.cuh"
+
+namespace joker {
+
+constexpr float U32 = 5.9604645e-8f;    // 2^-24
+
+template <int L, bool JIT, class T> struct AccF {
+    T F, D, C, LG;                   // sum w m^2, sum w m r_c; jitter: sum w r_c^2, sum lg2(1+s^2 iv)
+    T g[MAXL];                       // sum w m T_j (j >= 1)
+    T Q[MAXL];                       // jitter: sum w ivar r_c T_j
+    T G[MAXL][MAXL];                 // jitter: sum w T_j T_k (1 <= k <= j)
+    __device__ __forceinline__ void zero() {
+        const T z = vsplat<T>(0.0f);
+        F = D = C = LG = z;
+#pragma unroll
+        for (int i = 0; i < MAXL; ++i) {
+            g[i] = Q[i] = z;
+#pragma unroll
+            for (int k = 0; k < MAXL; ++k) G[i][k] = z;
+        }
+    }
+};
+
+// One epoch of the FP32-sum path.  Record words: 0,1 dt pair; 2 ivar;
+// no jitter: 6 + 2 (j - 1) ivar T_j; jitter: 8 + 2 (j - 1) T_j; 18 r_c;
+// 19 ivar r_c.
+template <int L, bool JIT, bool ACCURATE, class T>
+__device__ __forceinline__ void fast_epoch(const float *recf, const MixC<T> &c,
+                                           AccF<L, JIT, T> &A) {
+    const T m = unit_rv_column<ACCURATE>(vsplat<T>(recf[0]), vsplat<T>(recf[1]), c);
+    const T iv = vsplat<T>(recf[2]);
+    if constexpr (!JIT) {
+        const T ivm = vmul(iv, m);
+        A.F = vfma(ivm, m, A.F);
+        A.D = vfma(vsplat<T>(recf[19]), m, A.D);
+        if (L > 1) A.g[1] = vadd(A.g[1], ivm);
+#pragma unroll
+        for (int j = 2; j < L; ++j) A.g[j] = vfma(vsplat<T>(recf[6 + 2 * (j - 1)]), m, A.g[j]);
+    } else {
+        const T one = vsplat<T>(1.0f), two = vsplat<T>(2.0f);
+        const T onep = vfma(c.s2, iv, one);
+        const T ro0 = vmap([](float v) { return fast_rcp(v); }, onep);
+        const T ro = vmul(ro0, vfma(vneg(onep), ro0, two));
+        const T w = vmul(iv, ro);
+        A.LG = vadd(A.LG, vmap([](float v) { return lg2_approx(v); }, onep));
+        const T rc = vsplat<T>(recf[18]);
+        const T wm = vmul(w, m);
+        A.F = vfma(wm, m, A.F);
+        A.D = vfma(wm, rc, A.D);
+        const T wr = vmul(w, rc);
+        A.C = vfma(wr, rc, A.C);
+        const T wq = vmul(w, vsplat<T>(recf[19]));
+        if (L > 1) {
+            A.g[1] = vadd(A.g[1], wm);
+            A.G[1][1] = vadd(A.G[1][1], w);
+            A.Q[1] = vadd(A.Q[1], wq);
+        }
+#pragma unroll
+        for (int j = 2; j < L; ++j) {
+            const T Tj = vsplat<T>(recf[8 + 2 * (j - 1)]);
+            A.g[j] = vfma(wm, Tj, A.g[j]);
+            A.Q[j] = vfma(wq, Tj, A.Q[j]);
+            const T wt = vmul(w, Tj);
+            A.G[j][1] = vadd(A.G[j][1], wt);
+#pragma unroll
+            for (int k = 2; k <= j; ++k)
+                A.G[j][k] = vfma(wt, vsplat<T>(recf[8 + 2 * (k - 1)]), A.G[j][k]);
+        }
+    }
+}
+
+__device__ __forceinline__ ff ffv(float x) { return ff_make(x, 0.0f); }
+
+// The per-sample tail: ln L as a float pair (hi, lo) and its bound err.
+//
+// With H the trend block of G (Lambda_T^-1 + T W T^T: folded on the host
+// without jitter, from the sums with it), v = H^-1 g, s = 1/Lambda0 + F -
+// g^T v, q'_K = D - mu0 F, q'_T = -s^2 Q - mu0 g (no Q without jitter),
+// z = H^-1 q'_T and t = q'_K - g^T z:
+//   chi2 = C_eff - q'_T^T z - t^2 / s,  theta_K = t / s,  theta_T = z - v theta_K,
+//   C_eff = C + kappa - 2 mu0 D + mu0^2 F   (chi2_0 in place of C + kappa
+//                                            without jitter),
+//   log det G = log det H + log s.
+template <int L, bool JIT>
+__device__ __forceinline__ void fast_tail(const StarRec &st, const AccF<L, JIT, float> &A,
+                                          float e, float ome, float lgP, float s2, int N,
+                                          float err_c0, ff &lnl, float &err) {
+    constexpr int T = L - 1;
+    static_assert(!JIT || L <= 3, "the FP32-sum path takes at most three linear parameters "
+                                  "with the jitter applied");
+    float log_lam0f;
+    if (st.k_scaled) log_lam0f = fminf((float)st.log_maxK2, (float)st.log_kscale + lgP);
+    else log_lam0f = (float)log(st.lam0);
+    const float ilam0 = expf(-log_lam0f);
+    const float mu = st.mu0_f, amu = fabsf(mu);
+    // gamma: sequential FP32 sums of N terms; per term the FP32 weight (4
+    // roundings with jitter), the products, and r_c, ivar r_c, T_j as floats
+    const float gam = __fmul_ru((float)(N + (JIT ? 7 : 4)), U32) * 1.0001f;
+    const float F = A.F, D = A.D;
+    // ---- trend block inverse Hi and log det H
+    ff Hi[MAXL][MAXL];
+    ff ldH = ffv(0.0f);
+    if constexpr (!JIT) {
+#pragma unroll
+        for (int j = 0; j < T; ++j)
+#pragma unroll
+            for (int k = 0; k < T; ++k)
+                Hi[j][k] = ff_make(st.Cinv_hi[(j + 1) * MAXL + k + 1],
+                                   st.Cinv_lo[(j + 1) * MAXL + k + 1]);
+    } else if constexpr (T == 1) {
+        const ff H11 = ff_addf(ffv(A.G[1][1]), ff_make(st.ilam_hi[1], st.ilam_lo[1]));
+        Hi[0][0] = ff_divf(ffv(1.0f), H11);
+        ldH = ffv(ff_log(H11));
+    } else if constexpr (T == 2) {
+        const ff H11 = ff_addf(ffv(A.G[1][1]), ff_make(st.ilam_hi[1], st.ilam_lo[1]));
+        const ff H21 = ffv(A.G[2][1]);
+        const ff H22 = ff_addf(ffv(A.G[2][2]), ff_make(st.ilam_hi[2], st.ilam_lo[2]));
+        const ff det = ff_subf(ff_mulf(H11, H22), ff_mulf(H21, H21));
+        const ff idet = ff_divf(ffv(1.0f), det);
+        Hi[0][0] = ff_mulf(H22, idet);
+        Hi[1][1] = ff_mulf(H11, idet);
+        Hi[0][1] = Hi[1][0] = ff_neg(ff_mulf(H21, idet));
+        ldH = ffv(ff_log(det));
+    }
+    // ---- v = Hi g, q'_T, z = Hi q'_T
+    float qT[MAXL];
+#pragma unroll
+    for (int j = 0; j < T; ++j) qT[j] = (JIT ? -s2 * A.Q[j + 1] : 0.0f) - mu * A.g[j + 1];
+    ff v[MAXL], z[MAXL];
+    ff gv = ffv(0.0f), gz = ffv(0.0f), qz = ffv(0.0f);
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        v[j] = ffv(0.0f);
+        z[j] = ffv(0.0f);
+#pragma unroll
+        for (int k = 0; k < T; ++k) {
+            v[j] = ff_addf(v[j], ff_mul1(Hi[j][k], A.g[k + 1]));
+            z[j] = ff_addf(z[j], ff_mul1(Hi[j][k], qT[k]));
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        gv = ff_addf(gv, ff_mul1(v[j], A.g[j + 1]));
+        gz = ff_addf(gz, ff_mul1(z[j], A.g[j + 1]));
+        qz = ff_addf(qz, ff_mul1(z[j], qT[j]));
+    }
+    const ff amin = ff_subf(ffv(F), gv);                 // s - 1/Lambda0
+    const ff s = ff_addf(amin, ffv(ilam0));
+    const ff tK = ff_subf(ff_subf(ffv(D), ff_mul1(ffv(F), mu)), gz);
+    const ff K = ff_divf(tK, s);                         // theta_K
+    ff Ceff = JIT ? ff_addf(ffv(A.C), ff_make(st.kappa_hi, st.kappa_lo))
+                  : ff_make(st.chi2_0_hi, st.chi2_0_lo);
+    if (mu != 0.0f) Ceff = ff_addf(Ceff, ff_mul1(ff_subf(ff_mul1(ffv(F), mu), ffv(2.0f * D)), mu));
+    const ff chi2 = ff_subf(ff_subf(Ceff, qz), ff_mulf(K, tK));
+    const float chi2f = chi2.hi, sf = s.hi, Kh = fabsf(K.hi);
+    float th[MAXL];
+#pragma unroll
+    for (int j = 0; j < T; ++j) th[j] = fabsf(z[j].hi - v[j].hi * K.hi);
+    // ---- rounding of the sums: magnitudes by Cauchy-Schwarz from the
+    // non-negative sums (F, C, the diagonal trend sums)
+    const float Cmag = JIT ? A.C : st.Cn;
+    const float dF = gam * F;
+    const float dD = gam * sqrtf(F * Cmag);
+    float Gjj[MAXL], dg[MAXL], aT[MAXL];
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        Gjj[j] = JIT ? A.G[j + 1][j + 1] : st.Wjj[j + 1];
+        dg[j] = gam * sqrtf(F * Gjj[j]);
+        aT[j] = amu * dg[j];
+        if (JIT)
+            aT[j] += s2 * (gam * sqrtf(Gjj[j]) * sqrtf(A.C) * st.ivar_max +
+                           U32 * sqrtf(st.Cn * st.Wjj[j + 1])) + U32 * fabsf(qT[j]);
+    }
+    const float aK = dD + amu * dF;
+    const float dC = (JIT ? gam * A.C : 0.0f) + 2.0f * amu * dD + mu * mu * dF;
+    // first order: dC + 2 |theta|.|dq'| + |theta|^T |dG| |theta|
+    float d1 = dC + 2.0f * Kh * aK + Kh * Kh * dF;
+    float eK = aK + Kh * dF, dGf2 = dF * dF;
+    float eT[MAXL];
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        d1 += 2.0f * th[j] * (aT[j] + Kh * dg[j]);
+        eK += th[j] * dg[j];
+        eT[j] = aT[j] + Kh * dg[j];
+        dGf2 += 2.0f * dg[j] * dg[j];
+    }
+    if constexpr (JIT) {
+#pragma unroll
+        for (int j = 0; j < T; ++j)
+#pragma unroll
+            for (int k = 0; k < T; ++k) {
+                const float dG = gam * sqrtf(Gjj[j] * Gjj[k]);
+                d1 += th[j] * th[k] * dG;
+                eT[j] += dG * th[k];
+                dGf2 += dG * dG;
+            }
+    }
+    // second order: 2 tr(G^-1) |dq' - dG theta|^2, valid while |dG|_F tr(G^-1) < 1/4
+    const float iS = 1.0f / sf;
+    float trGi = iS;
+#pragma unroll
+    for (int j = 0; j < T; ++j) trGi += Hi[j][j].hi + v[j].hi * v[j].hi * iS;
+    float ee = eK * eK;
+#pragma unroll
+    for (int j = 0; j < T; ++j) ee += eT[j] * eT[j];
+    const float xf = sqrtf(dGf2) * trGi;
+    bool ok = xf < 0.25f;
+    d1 += 2.0f * trGi * ee;
+    // log det G: |tr(G^-1 dG)| + 1.34 |G^-1 dG|_F^2
+    float dl = iS * dF;
+#pragma unroll
+    for (int j = 0; j < T; ++j) dl += 2.0f * fabsf(v[j].hi) * iS * dg[j];
+    if constexpr (JIT) {
+#pragma unroll
+        for (int j = 0; j < T; ++j)
+#pragma unroll
+            for (int k = 0; k < T; ++k)
+                dl += fabsf(Hi[j][k].hi + v[j].hi * v[k].hi * iS) * gam * sqrtf(Gjj[j] * Gjj[k]);
+    }
+    float dlog = dl + 1.34f * xf * xf;
+    // ---- the FP32 column's own error (err_c0 empirical, as in the mixed
+    // kernel): chi2 is a minimum over the linear parameters, so it moves by
+    // -2 K sum w res dm; s moves directly
+    const float Dcol = err_c0 * (1.0f + e) / (ome * ome);
+    const float Wsum = st.sum_ivar;
+    const float c2 = fmaxf(chi2f, 0.0f);
+    const float dsc = 2.0f * Dcol * sqrtf(Wsum * fmaxf(amin.hi, 0.0f)) + Wsum * Dcol * Dcol;
+    ok = ok && dsc < 0.5f * sf;
+    float dchi = d1 + 2.0f * Kh * Dcol * sqrtf(Wsum * c2) + Kh * Kh * Dcol * Dcol * Wsum;
+    dlog += dsc / (sf - dsc);
+    if constexpr (JIT) {
+        // r_c stored as floats is a data perturbation; the FP32 log2 sum
+        dchi += 2.0f * U32 * sqrtf(c2 * st.Cn) + U32 * U32 * st.Cn;
+        dlog += gam * A.LG * 0.6931472f;
+    }
+    // ---- ln L
+    ff t;
+    if constexpr (!JIT) {
+        // -(chi2 + logdet_const + log Lambda0 + log s) / 2
+        t = ff_addf(chi2, ff_make(st.ldc_hi, st.ldc_lo));
+    } else {
+        // -(chi2 + log_norm_rest - sum log ivar + log Lambda0 + log det H + log s
+        //   + ln 2 sum lg2(1 + s^2 ivar)) / 2
+        t = ff_addf(chi2, ff_make(st.lnr_hi, st.lnr_lo));
+        t = ff_addf(t, ldH);
+        t = ff_addf(t, ff_mul1(ffv(A.LG), 0.6931472f));
+    }
+    t = ff_addf(t, ffv(log_lam0f));
+    t = ff_addf(t, ffv(ff_log(s)));
+    lnl = ff_make(-0.5f * t.hi, -0.5f * t.lo);
+    const float tailmag = fabsf(Ceff.hi) + fabsf(qz.hi) + Kh * fabsf(tK.hi);
+    // plus: log Lambda0 and the logs of the tail in FP32 (2e-6), the FP32 log2
+    // of each epoch's jitter term (2e-7 N), the float-float tail (its terms'
+    // magnitude times 2^-40), and 1 % for the FP32 evaluation of the bound
+    err = 1.01f * (0.5f * (dchi + dlog) + 2e-6f + 2e-7f * (float)N + 1e-12f * tailmag);
+    if (!ok || !(err == err) || !(lnl.hi == lnl.hi)) err = 1e30f;
+}
+
+template <int L, bool JIT>
+__device__ __forceinline__ AccF<L, JIT, float> accf_lane(const AccF<L, JIT, float2> &P, int lane) {
+    AccF<L, JIT, float> A;
+    auto g = [lane](float2 v) { return lane ? v.y : v.x; };
+    A.F = g(P.F); A.D = g(P.D); A.C = g(P.C); A.LG = g(P.LG);
+#pragma unroll
+    for (int i = 0; i < MAXL; ++i) {
+        A.g[i] = g(P.g[i]);
+        A.Q[i] = g(P.Q[i]);
+#pragma unroll
+        for (int k = 0; k < MAXL; ++k) A.G[i][k] = g(P.G[i][k]);
+    }
+    return A;
+}
+
+// Order-preserving key of the double equal to a float, from the float's bits
+// (integer operations only).
+__device__ __forceinline__ unsigned long long float_to_dkey(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned ex = (b >> 23) & 0xff;
+    const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+    unsigned long long d;
+    if (ex == 0xff) {
+        d = sign | 0x7ff0000000000000ull | ((unsigned long long)(b & 0x7fffffu) << 29);
+    } else if (ex == 0) {
+        d = sign;                       // zero or subnormal: +-0
+    } else {
+        d = sign | ((unsigned long long)(ex + 896) << 52) |
+            ((unsigned long long)(b & 0x7fffffu) << 29);
+    }
+    return key_of_bits((long long)d);
+}
+
+__device__ __forceinline__ void fast_store(const LnlArgs &a, int64_t out, bool active, ff lnl,
+                                           float err, unsigned long long *mk,
+                                           unsigned long long *bk) {
+    double d = 0.0;
+    if (active) {
+        d = (double)lnl.hi + (double)lnl.lo;
+        a.lnl[out] = d;
+        if (a.err) a.err[out] = err;
+    }
+    if (mk) warp_max_update(mk, active ? double_to_key(d) : 0ull);
+    if (bk) {
+        // lnL + err rounded up and lnL - err rounded down, as floats
+        const float up = __fadd_ru(lnl.hi, __fadd_ru(lnl.lo, err));
+        const float dn = __fadd_rd(lnl.hi, __fsub_rd(lnl.lo, err));
+        warp_max_update(bk, active ? float_to_dkey(up) : 0ull);
+        warp_max_update(bk + 1, active ? float_to_dkey(dn) : 0ull);
+    }
+}
+
+// Two samples per thread (paired FP32), any L without jitter, L <= 3 with.
+template <int L, bool JIT, bool PACKED>
+__global__ void __launch_bounds__(128, JOKER_PAIR_MINB)
+lnl_fast2_kernel(LnlArgs a) {
+    __shared__ __align__(16) float sm[TILE * REC32];
+    __shared__ double smr[PACKED ? PACK_ROWS * 5 : 1];
+    __shared__ int s_item;
+    int staged_star = -1;
+    const bool inter = PACKED && packed_interleaved(a);
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(a.queue, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= item_count(a)) break;
+        const WorkItem w = get_item(a, it);
+        const StarRec &st = a.stars[w.star];
+        const int N = st.n_epochs;
+        const bool single = N <= TILE;
+        if (single && w.star != staged_star) {
+            stage_epochs<float, REC32>(sm, a.ep32 + (size_t)st.epoch_off * REC32, N);
+            staged_star = w.star;
+            __syncthreads();
+        }
+        unsigned long long *mk = a.max_key ? a.max_key + w.max_slot : nullptr;
+        unsigned long long *bk = a.bound_key ? a.bound_key + 2 * w.max_slot : nullptr;
+        for (int base = 0; base < w.count; base += 2 * blockDim.x) {
+            const int j0 = base + threadIdx.x, j1 = j0 + blockDim.x;
+            const bool act0 = j0 < w.count, act1 = j1 < w.count;
+            float4 pa0, pb0, pa1, pb1;
+            float s20, s21;
+            load_pair<JIT, PACKED>(a, w, base, smr, inter, act0, act1, pa0, pb0, s20, pa1, pb1,
+                                   s21);
+            const MixC<float> c0 = mix_consts(pa0, pb0, s20), c1 = mix_consts(pa1, pb1, s21);
+            const MixC<float2> c = mix_pair(c0, c1);
+            AccF<L, JIT, float2> A;
+            A.zero();
+            for (int t0 = 0; t0 < N; t0 += TILE) {
+                const int nt = min(TILE, N - t0);
+                if (!single) {
+                    __syncthreads();
+                    stage_epochs<float, REC32>(sm, a.ep32 + ((size_t)st.epoch_off + t0) * REC32, nt);
+                    staged_star = -1;
+                    __syncthreads();
+                }
+                if (act0) {
+#pragma unroll 2
+                    for (int i = 0; i < nt; ++i) fast_epoch<L, JIT, false>(sm + i * REC32, c, A);
+                }
+            }
+            ff l0 = ffv(0.0f), l1 = ffv(0.0f);
+            float err0 = 0.0f, err1 = 0.0f;
+            if (act0)
+                fast_tail<L, JIT>(st, accf_lane(A, 0), c0.e, c0.ome, pb0.w, s20, N, a.err_c0, l0, err0);
+            if (act1)
+                fast_tail<L, JIT>(st, accf_lane(A, 1), c1.e, c1.ome, pb1.w, s21, N, a.err_c0, l1, err1);
+            fast_store(a, w.out_off + j0, act0, l0, err0, mk, bk);
+            fast_store(a, w.out_off + j1, act1, l1, err1, mk, bk);
+        }
+    }
+}
+
+}  // namespace joker

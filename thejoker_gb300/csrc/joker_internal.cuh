@@ -51,6 +51,15 @@ struct alignas(16) StarRec {
     float mu0_f;
     int32_t mu0_zero;                      // mu0 == 0 (the usual K prior mean)
     int32_t pad2;
+    // FP32-sum path (JOKER_MIXED_FAST).  With beta0 = C^-1 c the trend-only
+    // fit, r_c = y' - T^T beta0 is the residual of that fit; words 18 and 19
+    // of each REC32 epoch record hold r_c and ivar r_c as floats.
+    float kappa_hi, kappa_lo;          // beta0^T Lambda_T^-1 beta0
+    float ldc_hi, ldc_lo;              // logdet_const (jitter ignored)
+    float lnr_hi, lnr_lo;              // log_norm_rest - sum log ivar (jitter applied)
+    float Cn;                          // sum ivar r_c^2, rounded up
+    float ivar_max;                    // max ivar, rounded up
+    float Wjj[MAXL];                   // sum ivar T_j^2 (j >= 1), rounded up
 };
 
 // One unit of the persistent likelihood kernels: `count` samples of star
@@ -122,6 +131,8 @@ struct AcceptArgs {
     unsigned long long *exact_key;         // [slot]: exact FP64 maximum
     const StarRec *stars;
     const double *ep64;
+    const float *ep32;                      // mixed epoch records (the float-float tier)
+    float err_c0;                           // column-error constant of the mixed bound
     const double *P, *E, *OM, *M0, *S;
     int64_t stride;                         // doubles between consecutive samples (1 or 5)
     int L, jit;

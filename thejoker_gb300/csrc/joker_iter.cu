@@ -305,7 +305,8 @@ static int iter_alloc(joker_iter **out, const joker_stars *stars, const joker_ca
         snprintf(buf, sizeof buf, "%s: bad library, pool or schedule parameters", who);
         return iter_fail(JOKER_EINVAL, buf);
     }
-    if (precision != JOKER_FP64 && precision != JOKER_MIXED && precision != JOKER_MIXED_ACCURATE) {
+    if (precision != JOKER_FP64 && precision != JOKER_MIXED && precision != JOKER_MIXED_ACCURATE &&
+        precision != JOKER_MIXED_FAST) {
         snprintf(buf, sizeof buf, "%s: precision must be FP64 or a mixed precision with error "
                                   "bounds", who);
         return iter_fail(JOKER_EINVAL, buf);
@@ -542,6 +543,8 @@ extern "C" int joker_iter_round(joker_iter *it, void *stream) {
         c.exact_key = it->p.exact_key;
         c.stars = recs;
         c.ep64 = ep64;
+        c.ep32 = ep32;
+        c.err_c0 = mixed_err_c0();
         c.P = P; c.E = E; c.OM = OM; c.M0 = M0; c.S = S;
         c.stride = cstride;
         c.L = L;

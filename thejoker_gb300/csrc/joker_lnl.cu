@@ -138,8 +138,17 @@ static cudaError_t launch_mixed_L(bool jit, int var, const LnlArgs &a, int block
     return launch_mixed_LV<L, 0>(jit, a, block, st);
 }
 
+cudaError_t launch_lnl_fast(int L, bool jit, const LnlArgs &a, int block, cudaStream_t st);
+
 cudaError_t launch_lnl(int precision, int L, bool jit, const LnlArgs &a, int block,
                        cudaStream_t st) {
+    // The FP32-sum kernel covers any number of linear parameters without the
+    // jitter and at most three with it; larger jittered systems run the
+    // float-float kernel, whose outputs are of the same kind (tighter bound).
+    if (precision == JOKER_MIXED_FAST) {
+        if (!jit || L <= 3) return launch_lnl_fast(L, jit, a, block, st);
+        precision = JOKER_MIXED;
+    }
     if (precision == JOKER_FP64) {
         switch (L) {
             case 1: return launch_fp64_L<1>(jit, a, block, st);

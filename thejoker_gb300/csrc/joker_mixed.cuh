@@ -261,16 +261,12 @@ template <int L, bool JIT, class T> struct Acc32 {
     }
 };
 
-// One epoch.  recf: the epoch's REC32 float record (the same for every sample
-// of the thread; a field is splat into both lanes of a pair).
-template <int L, bool JIT, bool ACCURATE, class T>
-__device__ __forceinline__ void mixed_epoch(const float *recf, const MixC<T> &c, bool mu0z, T mu0,
-                                            T nmu0, Acc32<L, JIT, T> &A) {
-    T rec[REC32];
-#pragma unroll
-    for (int q = 0; q < 8 + 2 * (L - 1); ++q) rec[q] = vsplat<T>(recf[q]);
-    // ---- phase in cycles: dt * (1/P) - M0/(2 pi), mod 1
-    const T dth = rec[0], dtl = rec[1];
+// The unit-K RV column m = cos(omega + f) + e cos(omega) at one epoch: the
+// phase in cycles dt (1/P) - M0/(2 pi) mod 1 from float pairs (dth, dtl is
+// the epoch's dt pair), FP32 Kepler, and the true-anomaly form of the
+// velocity.  Shared by the float-float and the FP32-sum kernels.
+template <bool ACCURATE, class T>
+__device__ __forceinline__ T unit_rv_column(T dth, T dtl, const MixC<T> &c) {
     const T p = vmul(dth, c.iph);
     T pe = vfma(dth, c.iph, vnegprod(dth, c.niph, p));
     pe = vfma(dth, c.ipl, pe);
@@ -282,14 +278,25 @@ __device__ __forceinline__ void mixed_epoch(const float *recf, const MixC<T> &c,
     const T k = vmap([](float v) { return rintf(v); }, vadd(s1, lo));
     const T f = vadd(vsub(s1, k), lo);                                    // [-0.5, 0.5]
     const T M = vfma(f, vsplat<T>(TWO_PI_HI_F), vmul(f, vsplat<T>(TWO_PI_LO_F)));
-    // ---- Kepler + unit-K velocity
     T sE, cE;
     vkepler<ACCURATE>(M, c.e, c.ne, c.ome, c.ome3, c.a1, sE, cE);
     const T one = vsplat<T>(1.0f), two = vsplat<T>(2.0f);
     const T den = vfma(c.ne, cE, one);
     const T rd0 = vmap([](float v) { return fast_rcp(v); }, den);
     const T rd = vmul(rd0, vfma(vneg(den), rd0, two));
-    const T m = vfma(vfma(c.Ac, cE, vfma(c.Bc, sE, c.nDc)), rd, c.Dc);
+    return vfma(vfma(c.Ac, cE, vfma(c.Bc, sE, c.nDc)), rd, c.Dc);
+}
+
+// One epoch.  recf: the epoch's REC32 float record (the same for every sample
+// of the thread; a field is splat into both lanes of a pair).
+template <int L, bool JIT, bool ACCURATE, class T>
+__device__ __forceinline__ void mixed_epoch(const float *recf, const MixC<T> &c, bool mu0z, T mu0,
+                                            T nmu0, Acc32<L, JIT, T> &A) {
+    T rec[REC32];
+#pragma unroll
+    for (int q = 0; q < 8 + 2 * (L - 1); ++q) rec[q] = vsplat<T>(recf[q]);
+    const T one = vsplat<T>(1.0f), two = vsplat<T>(2.0f);
+    const T m = unit_rv_column<ACCURATE>(rec[0], rec[1], c);
     if constexpr (!JIT) {
         T th, tl;                                                         // w m, exact pair
         th = vmul(rec[2], m);
@@ -534,6 +541,50 @@ __device__ __forceinline__ void load_sample(const LnlArgs &a, int64_t row, float
     }
 }
 
+// PACKED over the reference's interleaved chunk (P, e, omega, M0, s adjacent,
+// stride 5): each pass stages its rows in shared memory with coalesced 8-byte
+// loads (consecutive threads, consecutive doubles), so that a chunk in host
+// memory read through a view crosses the link as whole lines, once.  Five
+// strided loads per sample would fetch each line several times.
+constexpr int PACK_ROWS = 256;          // rows per pass of the paired kernels
+
+__device__ __forceinline__ bool packed_interleaved(const LnlArgs &a) {
+    return a.stride == 5 && a.e == a.P + 1 && a.om == a.P + 2 && a.M0 == a.P + 3 &&
+           a.s == a.P + 4;
+}
+
+// Rows [row, row + n) into smr; the caller synchronises before and after.
+__device__ __forceinline__ void stage_rows(double *smr, const LnlArgs &a, int64_t row, int n) {
+    const double *src = a.P + row * 5;
+    for (int q = threadIdx.x; q < n * 5; q += blockDim.x) smr[q] = __ldg(src + q);
+}
+
+template <bool JIT>
+__device__ __forceinline__ void prepare_row(const double *r, float4 &pa, float4 &pb, float &s2) {
+    prepare_sample(r[0], r[1], r[2], r[3], JIT ? r[4] : 0.0, pa, pb, s2);
+}
+
+// The two samples of one pass of a paired kernel (thread t: samples base + t
+// and base + blockDim + t of the work item): from staged rows over an
+// interleaved chunk, else loaded directly.  Every thread of the CTA calls it.
+template <bool JIT, bool PACKED>
+__device__ __forceinline__ void load_pair(const LnlArgs &a, const WorkItem &w, int base,
+                                          double *smr, bool inter, bool act0, bool act1,
+                                          float4 &pa0, float4 &pb0, float &s20, float4 &pa1,
+                                          float4 &pb1, float &s21) {
+    const int j0 = base + threadIdx.x, j1 = j0 + blockDim.x;
+    if (PACKED && inter) {
+        __syncthreads();
+        stage_rows(smr, a, w.row0 + base, min(2 * (int)blockDim.x, w.count - base));
+        __syncthreads();
+        prepare_row<JIT>(smr + 5 * (act0 ? (int)threadIdx.x : 0), pa0, pb0, s20);
+        prepare_row<JIT>(smr + 5 * (act1 ? (int)(threadIdx.x + blockDim.x) : 0), pa1, pb1, s21);
+    } else {
+        load_sample<JIT, PACKED>(a, w.row0 + (act0 ? j0 : 0), pa0, pb0, s20);
+        load_sample<JIT, PACKED>(a, w.row0 + (act1 ? j1 : 0), pa1, pb1, s21);
+    }
+}
+
 __device__ __forceinline__ void store_sample(const LnlArgs &a, int64_t out, bool active, double lnl,
                                              float err, unsigned long long *mk,
                                              unsigned long long *bk) {
@@ -553,7 +604,7 @@ __device__ __forceinline__ void store_sample(const LnlArgs &a, int64_t out, bool
 // records smf holds (a single-tile star stays staged across items).
 template <int L, bool JIT, int VAR, bool PACKED>
 __device__ __forceinline__ void mixed_item_scalar(const LnlArgs &a, const WorkItem &w,
-                                                  float *smf, int *staged) {
+                                                  float *smf, double *smr, int *staged) {
     const StarRec &st = a.stars[w.star];
     const int N = st.n_epochs;
     const bool single = N <= TILE;
@@ -566,12 +617,20 @@ __device__ __forceinline__ void mixed_item_scalar(const LnlArgs &a, const WorkIt
     unsigned long long *bk = a.bound_key ? a.bound_key + 2 * w.max_slot : nullptr;
     const bool mu0z = st.mu0_zero != 0;
     const float mu0f = st.mu0_f;
+    const bool inter = PACKED && packed_interleaved(a);
     for (int base = 0; base < w.count; base += blockDim.x) {
         const int j = base + threadIdx.x;
         const bool active = j < w.count;
         float4 pa, pb;
         float s2;
-        load_sample<JIT, PACKED>(a, w.row0 + (active ? j : 0), pa, pb, s2);
+        if (inter) {
+            __syncthreads();
+            stage_rows(smr, a, w.row0 + base, min((int)blockDim.x, w.count - base));
+            __syncthreads();
+            prepare_row<JIT>(smr + 5 * (active ? threadIdx.x : 0), pa, pb, s2);
+        } else {
+            load_sample<JIT, PACKED>(a, w.row0 + (active ? j : 0), pa, pb, s2);
+        }
         const MixC<float> c = mix_consts(pa, pb, s2);
         Acc32<L, JIT, float> A;
         A.zero();
@@ -601,6 +660,7 @@ template <int L, bool JIT, int VAR, bool PACKED>
 __global__ void __launch_bounds__(128)
 lnl_mixed_kernel(LnlArgs a) {
     __shared__ __align__(16) float sm[TILE * REC32];
+    __shared__ double smr[PACKED ? 128 * 5 : 1];
     __shared__ int s_item;
     int staged = -1;
     for (;;) {
@@ -609,7 +669,7 @@ lnl_mixed_kernel(LnlArgs a) {
         __syncthreads();
         const int it = s_item;
         if (it >= item_count(a)) break;
-        mixed_item_scalar<L, JIT, VAR, PACKED>(a, get_item(a, it), sm, &staged);
+        mixed_item_scalar<L, JIT, VAR, PACKED>(a, get_item(a, it), sm, smr, &staged);
     }
 }
 
@@ -624,8 +684,10 @@ template <int L, bool JIT, int VAR, bool PACKED>
 __global__ void __launch_bounds__(128, JOKER_PAIR_MINB)
 lnl_mixed2_kernel(LnlArgs a) {
     __shared__ __align__(16) float sm[TILE * REC32];
+    __shared__ double smr[PACKED ? PACK_ROWS * 5 : 1];
     __shared__ int s_item;
     int staged_star = -1;
+    const bool inter = PACKED && packed_interleaved(a);
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_item = atomicAdd(a.queue, 1);
@@ -650,8 +712,8 @@ lnl_mixed2_kernel(LnlArgs a) {
             const bool act0 = j0 < w.count, act1 = j1 < w.count;
             float4 pa0, pb0, pa1, pb1;
             float s20, s21;
-            load_sample<JIT, PACKED>(a, w.row0 + (act0 ? j0 : 0), pa0, pb0, s20);
-            load_sample<JIT, PACKED>(a, w.row0 + (act1 ? j1 : 0), pa1, pb1, s21);
+            load_pair<JIT, PACKED>(a, w, base, smr, inter, act0, act1, pa0, pb0, s20, pa1, pb1,
+                                   s21);
             const MixC<float> c0 = mix_consts(pa0, pb0, s20), c1 = mix_consts(pa1, pb1, s21);
             const MixC<float2> c = mix_pair(c0, c1);
             Acc32<L, JIT, float2> A;

@@ -238,7 +238,7 @@ class PriorCache:
 
 PRECISIONS = {"fp64": nat.JOKER_FP64, "mixed": nat.JOKER_MIXED,
               "mixed_accurate": nat.JOKER_MIXED_ACCURATE,
-              "mixed_fp64_tail": nat.JOKER_MIXED_FP64_TAIL}
+              "mixed_fp64_tail": nat.JOKER_MIXED_FP64_TAIL, "mixed_fast": nat.JOKER_MIXED_FAST}
 
 
 class MaxKeys:
