@@ -289,6 +289,18 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
             Wjj[j] += w * Tj * Tj;
         }
         float *r32 = rec32 + (size_t)i * REC32;
+        // dt split for the FP32-sum kernel's phase: dth with 12 significant
+        // bits (exact in a float), dtl the rest.  Words 16 and 17 are free in
+        // every layout that kernel reads (with the jitter it takes L <= 3; at
+        // L = 6 they hold the float-float kernel's last trend column)
+        if (jitter_mode != JOKER_JITTER_APPLIED || L <= 5) {
+            const double dt = t[i] - t_ref;
+            int ex = 0;
+            const double mant = std::frexp(dt, &ex);
+            const double dth = std::ldexp(std::nearbyint(std::ldexp(mant, 12)), ex - 12);
+            r32[16] = (float)dth;
+            r32[17] = (float)(dt - dth);
+        }
         r32[18] = (float)rc;
         r32[19] = (float)(w * rc);
     }

@@ -54,13 +54,36 @@ template <int L, bool JIT, class T> struct AccF {
     }
 };
 
+// The unit-K RV column with a split phase: dt = dth + dtl with dth carrying
+// 12 significant bits and 1/P = ih + il with ih carrying 12, so dth ih is
+// exact in FP32 and so is its fractional part; |dth il| + |dtl / P| is below
+// 2^-10 dt/P cycles, and its FP32 rounding leaves about 2^-34 dt/P cycles
+// (1.2e-7 cycles at dt/P = 2000: a 4000-day baseline at P = 2 d; the
+// float-float phase of unit_rv_column gets 3e-8).  Both are inside the column
+// error that err_c0 bounds.  The reciprocal of the velocity's denominator is
+// the hardware one (within 2^-23 relative, no Newton step).
+template <class T>
+__device__ __forceinline__ T unit_rv_column_split(T dth, T dtl, const MixC<T> &c) {
+    const T p = vmul(dth, c.ih);                                          // exact
+    const T fr = vsub(p, vmap([](float v) { return rintf(v); }, p));      // exact
+    const T sm = vfma(dth, c.il, vmul(dtl, c.iph));
+    const T f0 = vadd(vsub(fr, c.mch), vsub(sm, c.mcl));
+    const T f = vsub(f0, vmap([](float v) { return rintf(v); }, f0));     // [-0.5, 0.5]
+    const T M = vfma(f, vsplat<T>(TWO_PI_HI_F), vmul(f, vsplat<T>(TWO_PI_LO_F)));
+    T sE, cE;
+    vkepler<false>(M, c.e, c.ne, c.ome, c.ome3, c.a1, sE, cE);
+    const T den = vfma(c.ne, cE, vsplat<T>(1.0f));
+    const T rd = vmap([](float v) { return fast_rcp(v); }, den);
+    return vfma(vfma(c.Ac, cE, vfma(c.Bc, sE, c.nDc)), rd, c.Dc);
+}
+
 // One epoch of the FP32-sum path.  Record words: 0,1 dt pair; 2 ivar;
-// no jitter: 6 + 2 (j - 1) ivar T_j; jitter: 8 + 2 (j - 1) T_j; 18 r_c;
-// 19 ivar r_c.
+// no jitter: 6 + 2 (j - 1) ivar T_j; jitter: 8 + 2 (j - 1) T_j; 16, 17 dt
+// split as dth (12 significant bits) + dtl; 18 r_c; 19 ivar r_c.
 template <int L, bool JIT, bool ACCURATE, class T>
 __device__ __forceinline__ void fast_epoch(const float *recf, const MixC<T> &c,
                                            AccF<L, JIT, T> &A) {
-    const T m = unit_rv_column<ACCURATE>(vsplat<T>(recf[0]), vsplat<T>(recf[1]), c);
+    const T m = unit_rv_column_split(vsplat<T>(recf[16]), vsplat<T>(recf[17]), c);
     const T iv = vsplat<T>(recf[2]);
     if constexpr (!JIT) {
         const T ivm = vmul(iv, m);
@@ -70,11 +93,10 @@ __device__ __forceinline__ void fast_epoch(const float *recf, const MixC<T> &c,
 #pragma unroll
         for (int j = 2; j < L; ++j) A.g[j] = vfma(vsplat<T>(recf[6 + 2 * (j - 1)]), m, A.g[j]);
     } else {
-        const T one = vsplat<T>(1.0f), two = vsplat<T>(2.0f);
-        const T onep = vfma(c.s2, iv, one);
-        const T ro0 = vmap([](float v) { return fast_rcp(v); }, onep);
-        const T ro = vmul(ro0, vfma(vneg(onep), ro0, two));
-        const T w = vmul(iv, ro);
+        // w = ivar / (1 + s^2 ivar): one rounding for 1 + s^2 ivar, the
+        // hardware reciprocal (within 2^-23 relative) and the product
+        const T onep = vfma(c.s2, iv, vsplat<T>(1.0f));
+        const T w = vmul(iv, vmap([](float v) { return fast_rcp(v); }, onep));
         A.LG = vadd(A.LG, vmap([](float v) { return lg2_approx(v); }, onep));
         const T rc = vsplat<T>(recf[18]);
         const T wm = vmul(w, m);
@@ -341,9 +363,15 @@ __device__ __forceinline__ void fast_store(const LnlArgs &a, int64_t out, bool a
     }
 }
 
+// Resident CTAs per SM the FP32-sum kernel is compiled for: 8 (64 registers,
+// 32 warps) measured 1-2 % faster than 7, 6 or 5 on GB300.
+#ifndef JOKER_FAST_MINB
+#define JOKER_FAST_MINB 8
+#endif
+
 // Two samples per thread (paired FP32), any L without jitter, L <= 3 with.
 template <int L, bool JIT, bool PACKED>
-__global__ void __launch_bounds__(128, JOKER_PAIR_MINB)
+__global__ void __launch_bounds__(128, JOKER_FAST_MINB)
 lnl_fast2_kernel(LnlArgs a) {
     __shared__ __align__(16) float sm[TILE * REC32];
     __shared__ double smr[PACKED ? PACK_ROWS * 5 : 1];

@@ -215,11 +215,14 @@ template <class T> struct MixC {
     T e, ne, ome, ome3, a1;       // e, -e, 1 - e, 3 (1 - e), Markley's a1
     T Ac, Bc, nDc, Dc;            // unit-K velocity: (Ac cE + Bc sE - Dc) / (1 - e cE) + Dc
     T s2, ns2;                    // s^2, -s^2
+    T ih, il;                     // 1/P as ih (12 significant bits) + il (the rest, a float)
 };
 
 __device__ __forceinline__ MixC<float> mix_consts(float4 pa, float4 pb, float s2) {
     MixC<float> c;
     c.iph = pa.x; c.ipl = pa.y; c.niph = -pa.x; c.mch = pa.z; c.mcl = pa.w;
+    c.ih = __int_as_float(__float_as_int(pa.x) & (int)0xFFFFF000);   // low 12 mantissa bits cleared
+    c.il = __fadd_rn(__fsub_rn(pa.x, c.ih), pa.y);                   // pa.x - ih is exact
     const float e = pb.x, ome = 1.0f - e;
     c.e = e; c.ne = -e; c.ome = ome; c.ome3 = 3.0f * ome;
     c.a1 = (float)MK_A1_D * fast_rcp(1.0f + e);
@@ -235,6 +238,7 @@ __device__ __forceinline__ MixC<float2> mix_pair(const MixC<float> &u, const Mix
     JOKER_PAIR(iph) JOKER_PAIR(ipl) JOKER_PAIR(niph) JOKER_PAIR(mch) JOKER_PAIR(mcl)
     JOKER_PAIR(e) JOKER_PAIR(ne) JOKER_PAIR(ome) JOKER_PAIR(ome3) JOKER_PAIR(a1)
     JOKER_PAIR(Ac) JOKER_PAIR(Bc) JOKER_PAIR(nDc) JOKER_PAIR(Dc) JOKER_PAIR(s2) JOKER_PAIR(ns2)
+    JOKER_PAIR(ih) JOKER_PAIR(il)
 #undef JOKER_PAIR
     return c;
 }
