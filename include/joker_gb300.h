@@ -313,6 +313,15 @@ int joker_iter_set_round_budget(joker_iter *it, int64_t samples);
 /* Synchronous copy of the same outputs to host arrays (any may be NULL). */
 int joker_iter_read(const joker_iter *it, int64_t *h_state, int64_t *h_idx, double *h_lnl,
                     int *h_done, uint64_t *h_n_refined);
+/* Asynchronous copies on `stream`: the state table (n_stars x 8, when h_state
+ * is not NULL) and the index rows (max_requested each) of the n_slots slots
+ * listed in `slots` (host array), row k to h_idx[k * max_requested ...].  Host
+ * buffers should be pinned for the copies to overlap device work; the caller
+ * synchronises with the stream before reading them.  A serving loop reads the
+ * small state table after every round and only the finished slots' rows.  No
+ * counterpart in the reference. */
+int joker_iter_read_async(const joker_iter *it, int64_t *h_state, const int *slots, int n_slots,
+                          int64_t *h_idx, void *stream);
 
 /* ---- prior samples on the device ------------------------------------------
  * The producer of the prior cache (JokerPrior.sample, thejoker/prior.py

@@ -37,6 +37,7 @@ EXPORTED = (
     "joker_iter_set_round_budget", "joker_accept_noalloc", "joker_linear_posterior",
     "joker_unmarginalized_lnl", "joker_prior_sample", "joker_rv_from_elements",
     "joker_rejection_workspace", "joker_rejection_sample", "joker_refine_band",
+    "joker_iter_read_async",
 )
 
 
@@ -112,6 +113,7 @@ _SIGS = {
                                           ctypes.POINTER(_vp), ctypes.POINTER(_vp),
                                           ctypes.POINTER(_vp)]),
     "joker_iter_read": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "joker_iter_read_async": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
     "joker_iter_create_pool": (ctypes.c_int, [ctypes.POINTER(_vp), _vp, _vp, ctypes.c_int, _i64,
                                               _i64, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                               ctypes.c_int]),

@@ -597,6 +597,26 @@ extern "C" int joker_iter_outputs(const joker_iter *it, int64_t **d_state, int64
 // Synchronous copy of the results to host arrays (any may be NULL): the state
 // rows (n_stars x 8), the accepted indices and their ln L (n_stars x
 // n_requested) and the finished-star count.
+extern "C" int joker_iter_read_async(const joker_iter *it, int64_t *h_state, const int *slots,
+                                     int n_slots, int64_t *h_idx, void *stream) {
+    if (!it) return iter_fail(JOKER_EINVAL, "joker_iter_read_async: NULL handle");
+    if (n_slots < 0 || (n_slots > 0 && (!slots || !h_idx)))
+        return iter_fail(JOKER_EINVAL, "joker_iter_read_async: bad slot list");
+    const size_t n = (size_t)it->p.n_stars, r = (size_t)it->p.max_req;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    if (h_state)
+        e = cudaMemcpyAsync(h_state, it->p.state, 8 * n * ST_FIELDS, cudaMemcpyDeviceToHost, st);
+    for (int k = 0; k < n_slots && e == cudaSuccess; ++k) {
+        if (slots[k] < 0 || (size_t)slots[k] >= n)
+            return iter_fail(JOKER_EINVAL, "joker_iter_read_async: slot outside the table");
+        e = cudaMemcpyAsync(h_idx + (size_t)k * r, it->out_idx + (size_t)slots[k] * r, 8 * r,
+                            cudaMemcpyDeviceToHost, st);
+    }
+    if (e != cudaSuccess) return iter_fail(JOKER_ECUDA, cudaGetErrorString(e));
+    return JOKER_OK;
+}
+
 extern "C" int joker_iter_read(const joker_iter *it, int64_t *h_state, int64_t *h_idx,
                                double *h_lnl, int *h_done, uint64_t *h_n_refined) {
     if (!it) return iter_fail(JOKER_EINVAL, "joker_iter_read: NULL handle");

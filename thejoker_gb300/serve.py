@@ -118,8 +118,16 @@ class ServingEngine:
         self.free_slots = list(range(self.n_slots))[::-1]
         self.active = {}
         self.done = []
-        self._state = np.zeros((self.n_slots, 8), dtype=np.int64)
         self.samples_evaluated = 0
+        # after every round its state table (n_slots x 8) comes back into one of
+        # two pinned buffers; the host retires round k - 1 while round k runs
+        self._state_h = [torch.empty((self.n_slots, 8), dtype=torch.int64).pin_memory()
+                         for _ in range(2)]
+        self._state_ev = [torch.cuda.Event() for _ in range(2)]
+        self._pending = None              # (buffer, round) of the last round's state copy
+        self._idx_h = torch.empty((self.n_slots, self.max_requested),
+                                  dtype=torch.int64).pin_memory()
+        self._side = torch.cuda.Stream()
 
     # ------------------------------------------------------------ requests
     def submit(self, req, t=None):
@@ -149,6 +157,7 @@ class ServingEngine:
                 pcg.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
                 dev.stream_handle(self.stream)), "joker_iter_admit")
             req.t_admitted = time.perf_counter()
+            req.admit_round = self.rounds       # the first round that includes it
             self.active[slot] = req
             n += 1
         return n
@@ -166,26 +175,42 @@ class ServingEngine:
             else:
                 nat.check(nat.lib().joker_iter_round(self._h, dev.stream_handle(self.stream)),
                           "joker_iter_round")
+            # the round's state table to the host, asynchronously
+            b = self.rounds % 2
+            nat.check(nat.lib().joker_iter_read_async(
+                self._h, ctypes.c_void_p(self._state_h[b].data_ptr()), None, 0, None,
+                dev.stream_handle(self.stream)), "joker_iter_read_async")
+            self._state_ev[b].record(self.stream)
+        pending = (self.rounds % 2, self.rounds)
         self.rounds += 1
+        return pending
 
-    def _retire(self):
-        self.stream.synchronize()
-        nat.check(nat.lib().joker_iter_read(self._h, self._state.ctypes.data_as(ctypes.c_void_p),
-                                            None, None, None, None), "joker_iter_read")
-        finished = [s for s in self.active if self._state[s, 4] != 0]
+    def _retire(self, pending):
+        """Retire the stars that round `pending` finished: its state copy is
+        complete by now (the following round was queued after it), the index
+        rows of only the finished slots are copied on a side stream (the
+        rounds running meanwhile do not write them)."""
+        b, k = pending
+        self._state_ev[b].synchronize()
+        state = self._state_h[b].numpy()
+        finished = [s for s, req in self.active.items()
+                    if req.admit_round <= k and state[s, 4] != 0]
         if not finished:
             return 0
-        idx = np.empty(self.n_slots * self.max_requested, dtype=np.int64)
-        nat.check(nat.lib().joker_iter_read(self._h, None, idx.ctypes.data_as(ctypes.c_void_p),
-                                            None, None, None), "joker_iter_read")
-        idx = idx.reshape(self.n_slots, self.max_requested)
+        slots = np.array(finished, dtype=np.int32)
+        nat.check(nat.lib().joker_iter_read_async(
+            self._h, None, slots.ctypes.data_as(ctypes.c_void_p), len(finished),
+            ctypes.c_void_p(self._idx_h.data_ptr()), dev.stream_handle(self._side)),
+            "joker_iter_read_async")
+        self._side.synchronize()
+        idx = self._idx_h.numpy()
         now = time.perf_counter()
-        for s in finished:
+        for j, s in enumerate(finished):
             req = self.active.pop(s)
-            row = self._state[s]
-            k = int(min(row[3], req.n_requested))
+            row = state[s]
+            n = int(min(row[3], req.n_requested))
             status = {1: "done", 2: "no samples accepted", 3: "hit maxiter"}.get(int(row[4]), "?")
-            req.result = (idx[s, :k].copy(), int(row[3]), int(row[2]), status)
+            req.result = (idx[j, :n].copy(), int(row[3]), int(row[2]), status)
             req.t_done = now
             self.samples_evaluated += int(row[2])
             self.pool.release(*req.pool)
@@ -194,16 +219,19 @@ class ServingEngine:
         return len(finished)
 
     def step(self):
-        """Admit what fits, run one round for every active star, retire the
-        finished ones.  Returns the number of active stars after the step."""
+        """Admit what fits, queue one round for every active star, and retire
+        the stars the previous round finished while this one runs.  Returns
+        the number of active stars after the step."""
         self._admit()
+        prev, self._pending = self._pending, None
         if self.active:
-            self._round()
-            self._retire()
+            self._pending = self._round()
+        if prev is not None:
+            self._retire(prev)
         return len(self.active)
 
     def drain(self):
-        while self.queue or self.active:
+        while self.queue or self.active or self._pending is not None:
             self.step()
         return self.done
 
