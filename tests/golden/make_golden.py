@@ -176,8 +176,45 @@ def ref_cases():
         print(name, lnl_ref.min(), lnl_ref.max())
 
 
+def degenerate_cases():
+    """ref_lnl_degenerate.npz: the reference's own output on degenerate
+    designs -- an infinite prior variance on an offset column that duplicates
+    the constant one, zero errors at most epochs, an infinite v0 variance --
+    where its LU-failure branches (fast_likelihood.pyx:283-291, 347-348,
+    381-382) would apply.  Each case stores its star and the reference's
+    ln L of 16 prior samples."""
+    from oracle import ref_cython
+    rng = np.random.default_rng(0)
+    N = 8
+    t = np.sort(rng.uniform(0, 500, N)) + 56000
+    err = rng.uniform(0.2, 0.5, N)
+    rv = rng.normal(0, 2, N)
+    chunk = _chunk(rng, 16, 2.0, 1024.0)
+    e0 = err.copy()
+    e0[:6] = 0.0
+    with np.errstate(divide="ignore"):
+        iv0 = 1 / e0 ** 2
+    cases = {
+        "dup_offset_inf_var": (1 / err ** 2, np.ones((N, 2)), 1, 1, [0, 0, 0], [0, 100.0, np.inf]),
+        "zero_errors": (iv0, np.ones((N, 1)), 1, 0, [0, 0], [0, 100.0]),
+        "inf_v0_var": (1 / err ** 2, np.ones((N, 1)), 1, 0, [0, 0], [0, np.inf]),
+    }
+    out = {"t": t, "rv": rv, "chunk": chunk}
+    for name, (ivar, trend, poly, noff, mu, std) in cases.items():
+        h = ref_cython.make_helper(t, rv, ivar, t.min(), trend, poly, noff, mu, std, True, 30.0,
+                                   365.25, 500.0)
+        out[f"{name}_ivar"] = ivar
+        out[f"{name}_trend_M"] = trend
+        out[f"{name}_mu"] = np.asarray(mu, dtype=float)
+        out[f"{name}_lam"] = np.asarray(std, dtype=float) ** 2
+        out[f"{name}_lnl_ref"] = np.array(h.batch_marginal_ln_likelihood(chunk))
+        print(name, out[f"{name}_lnl_ref"][:4])
+    np.savez(os.path.join(HERE, "ref_lnl_degenerate.npz"), **out)
+
+
 if __name__ == "__main__":
     from oracle import build
     build.build_all()
     kepler_known_answer()
     ref_cases()
+    degenerate_cases()

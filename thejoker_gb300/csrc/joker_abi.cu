@@ -180,9 +180,12 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
             if (trend_M[(size_t)i * T] != 1.0)
                 return fail(JOKER_EINVAL, "star %d: column 0 of trend_M must be 1 (the constant "
                                           "v0 term of the reference's design matrix)", k);
+    // finite and positive: an infinite variance makes the prior's normalisation
+    // (sum log lambda) infinite, where the reference's arithmetic gives NaN
     for (int j = 0; j < L; ++j)
-        if (!(lamk[j] > 0.0) && !(j == 0 && kp[0] != 0.0))
-            return fail(JOKER_EINVAL, "star %d: prior variance lambda[%d] must be > 0", k, j);
+        if (!(lamk[j] > 0.0 && std::isfinite(lamk[j])) && !(j == 0 && kp[0] != 0.0))
+            return fail(JOKER_EINVAL, "star %d: prior variance lambda[%d] must be positive and "
+                                      "finite", k, j);
     if (kp[0] != 0.0 && !(kp[1] > 0.0 && kp[2] > 0.0 && kp[3] > 0.0))
         return fail(JOKER_EINVAL, "star %d: scaled K prior needs sigma_K0, P0, max_K > 0", k);
     const int32_t keep_off = r.epoch_off;
