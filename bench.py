@@ -104,12 +104,14 @@ FLOPS_PER_SAMPLE = 21
 ISSUED_FLOPS = {"mixed": (196, 60), "mixed_fast": (126, 420)}
 KERNEL_NAME = {"mixed": "lnl_mixed2_kernel<L=2, jitter, VAR 0, cache form> (two samples per "
                         "thread, paired FP32, float-float sums)",
-               "mixed_fast": "lnl_fast2_kernel<L=2, jitter, cache form> (two samples per "
-                             "thread, paired FP32, FP32 sums re-centred on the trend fit)"}
+               "mixed_fast": "lnl_fast2_kernel<L=2, jitter, cache form, fused acceptance> (two "
+                             "samples per thread, paired FP32, FP32 sums re-centred on the "
+                             "trend fit; each sample's PCG64 uniform and candidate bit)"}
 # Algorithmic HBM bytes per sample of the cache-form mixed kernel (36 B prepared
-# sample read, 8 B ln L + 4 B bound written) and the DRAM bytes ncu measured per
-# sample (read + write of one 2^24-sample launch / 2^24), scaled to a launch.
-BYTES_PER_SAMPLE = 48
+# sample read, 8 B ln L + 4 B bound written, and for the fused pass 1 bit of
+# candidate mask) and the DRAM bytes ncu measured per sample (read + write of
+# one 2^24-sample launch / 2^24), scaled to a launch.
+BYTES_PER_SAMPLE = 48.125
 DRAM_BYTES_PER_SAMPLE = 46.79
 
 
@@ -369,7 +371,9 @@ def run_ours(args, rank, world, dist):
                    "prior_samples_per_gpu": S, "n_epochs": N_EPOCHS, "n_linear": 2,
                    "l2": "inputs larger than L2 (cache 76 B/sample resident, 2^28 samples)",
                    "precision": MIXED, "u_source": "numpy PCG64 stream regenerated on device",
-                   "accept": "refined to the FP64 decisions",
+                   "accept": "refined to the FP64 decisions; first pass fused into the ln L "
+                             "kernel" if MIXED == "mixed_fast" else
+                             "refined to the FP64 decisions",
                    "autotune": {"chunk": tuned, "ms_per_2^26_samples": tune_ms}},
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "samples/s",
                 "h2d_bytes_per_step": S * 40, "d2h_bytes_per_step": d2h,
@@ -433,7 +437,7 @@ def _parity_slice(table, cache, b64, S):
     err = torch.empty((1, S), dtype=torch.float32, device="cuda")
     bk = dev.MaxKeys(2)
     dev.lnl(table, cache, lm, precision=MIXED, count=S, err=err, bound_keys=bk)
-    raw = lm.clone()
+    raw, eraw = lm.clone(), err.clone()
     seg = [dict(lnl_off=0, n=S, out_off=0, max_out=0, max_slot=0, star=0, row0=0)]
     exact, n1 = dev.refine_max(table, cache, lm.view(-1), err.view(-1), bk, seg)
     n2 = dev.refine_band(table, cache, lm.view(-1), err.view(-1), exact, seg)
@@ -446,9 +450,9 @@ def _parity_slice(table, cache, b64, S):
     c64, i64, l64k = b64.results()
     cm, im, lmk = bm.results()
     same = bool(c64[0] == cm[0] and np.array_equal(i64[0], im[0]))
-    ev = err.view(-1).cpu().numpy()
-    # the raw bound: refine_band set the bound of re-evaluated samples to 0,
-    # so compare against the bound of the samples it left alone
+    # the raw values against their own bounds, as the ln L kernel wrote both
+    # (the refinements tighten or zero the bounds of the samples they touch)
+    ev = eraw.view(-1).cpu().numpy()
     kept_bound = ev > 0
     over = np.abs(ar - a64)[kept_bound] / ev[kept_bound]
     return {"rows": int(S), "band_nats": band_nats, "tol": nat.JOKER_MIXED_LNL_TOL,

@@ -185,7 +185,7 @@ int joker_batch_marginal_ln_likelihood(const joker_stars *stars, int star,
  * d_max_key[k] holds an order-preserving integer image of the running
  * maximum of star star0+k and is raised atomically (it must be zeroed, or hold
  * a previous maximum, before the call).  precision: JOKER_FP64, JOKER_MIXED,
- * JOKER_MIXED_ACCURATE or JOKER_MIXED_FP64_TAIL.
+ * JOKER_MIXED_ACCURATE, JOKER_MIXED_FP64_TAIL or JOKER_MIXED_FAST.
  * Mixed precisions only: d_err (optional, laid out like d_lnl) receives a
  * bound on |lnL - lnL_FP64| per sample, and d_bound_key (optional, 2 per star)
  * the running maxima of lnL + err and lnL - err.
@@ -263,6 +263,49 @@ int joker_refine_band(const joker_stars *stars, const joker_cache *cache,
                       const joker_accept_seg *segs, int n_segs, double *d_lnl, float *d_err,
                       const uint64_t *d_exact_key, double band, double tol,
                       uint64_t *d_n_refined, void *d_work, int64_t work_bytes, void *stream);
+
+/* ---- fused first acceptance pass (JOKER_MIXED_FAST) -------------------------
+ * joker_lnl_fused is joker_lnl at JOKER_MIXED_FAST with the first pass of the
+ * acceptance folded into the ln L kernel: each sample's uniform is drawn from
+ * its star's numpy PCG64 stream inside the kernel, and every sample that the
+ * running bounds cannot reject -- whatever the maximum turns out to be -- gets
+ * a candidate bit.  joker_accept_fused then finds the FP64 maxima among the
+ * candidates and decides them; a sample without the bit is rejected.  The
+ * two calls keep exactly the rows joker_lnl + joker_accept_refined keep
+ * (the FP64 decisions), without the two full scans over ln L and its bounds.
+ *
+ * joker_lnl_fused: d_pcg (device, n_sel x 4 {state_hi, state_lo, inc_hi,
+ * inc_lo}) holds each star's generator before its first uniform; row row0 + j
+ * is sample number first + j of the star's stream (its uniform the draw after
+ * first + j steps; first a multiple of 32, as for a slice of a larger run).
+ * Sample q of star star0 + k gets bit q % 32 of d_cand[k * cand_ld + q / 32]
+ * (cand_ld >= (first + count + 31) / 32 words); the other bits of the words
+ * it covers are written, words outside [first, first + count) are not.
+ * d_err and d_bound_key are required (zeroed, or holding smaller maxima,
+ * before the first call of a run); chunk a multiple of 128 and at most 8192
+ * (0 = 1024).  A jittered table with more than three linear parameters
+ * returns JOKER_EINVAL (use joker_lnl + joker_accept_refined).
+ *
+ * joker_accept_fused: joker_accept_refined's output contract for segments
+ * whose candidate bits segment s finds at d_cand + s * cand_ld (sample i at
+ * bit i % 32 of word i / 32; cand_ld a multiple of 4, d_cand 16-byte
+ * aligned), uniforms from the segments' PCG64 states (u_source
+ * JOKER_U_PCG64).  d_exact_key (n_slots) receives the FP64 maxima.
+ * Same workspace as joker_accept.
+ * Replace, as joker_lnl + joker_accept_refined do, the ln L loop and the
+ * acceptance of rejection_sample (thejoker/likelihood_helpers.py:40-66,
+ * 107-109). */
+int joker_lnl_fused(const joker_stars *stars, const joker_cache *cache, int star0, int n_sel,
+                    int64_t row0, int64_t count, const uint64_t *d_pcg, int64_t first,
+                    double *d_lnl, int64_t ld, uint64_t *d_max_key, float *d_err,
+                    uint64_t *d_bound_key, uint32_t *d_cand, int64_t cand_ld, int64_t chunk,
+                    void *stream);
+int joker_accept_fused(const joker_stars *stars, const joker_cache *cache,
+                       const joker_accept_seg *segs, int n_segs, double *d_lnl, float *d_err,
+                       const uint64_t *d_bound_key, uint64_t *d_exact_key, int n_slots,
+                       const uint32_t *d_cand, int64_t cand_ld, int64_t *d_out_idx,
+                       double *d_out_lnl, int64_t *d_count, uint64_t *d_n_refined,
+                       void *d_work, int64_t work_bytes, void *stream);
 
 /* ---- iterative rejection, one device-resident round at a time --------------
  * Replaces the loop of iterative_rejection_inmem
@@ -401,7 +444,9 @@ int joker_rv_from_elements(const double *d_t, int n_t, const double *d_elems, in
  * Replaces, for a batch of stars, marginal_ln_likelihood_inmem plus the
  * acceptance of rejection_sample (thejoker/likelihood_helpers.py:40-66,
  * 107-109; thejoker/multiproc_helpers.py:63-120, 256-258): the sequence
- * joker_lnl + joker_accept / joker_accept_refined in one call. */
+ * joker_lnl + joker_accept / joker_accept_refined in one call -- for
+ * JOKER_MIXED_FAST, joker_lnl_fused + joker_accept_fused (the workspace then
+ * also holds the generator states and the candidate bits). */
 int64_t joker_rejection_workspace(int n_sel, int64_t count, int64_t max_out, int precision);
 int joker_rejection_sample(const joker_stars *stars, const joker_cache *cache, int star0,
                            int n_sel, int64_t row0, int64_t count, int precision,

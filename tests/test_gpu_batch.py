@@ -106,7 +106,7 @@ def test_autotune_records_fastest_chunk(cuda, tmp_path):
         del os.environ["JOKER_AUTOTUNE"]
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fast", "fp64"])
 def test_one_call_rejection_equals_engine(cuda, precision):
     """joker_rejection_sample (ln L + maxima + acceptance in one C call) keeps
     the same rows, counts and ln L as the BatchRejection engine, including a
@@ -124,7 +124,7 @@ def test_one_call_rejection_equals_engine(cuda, precision):
     table = dev.StarTable(stars, jitter="applied")
     counts, idx, ll = BatchRejection(table, cache, precision=precision, max_out=max_out,
                                      seeds=seeds).run().results()
-    prec = nat.JOKER_MIXED if precision == "mixed" else nat.JOKER_FP64
+    prec = dev.PRECISIONS[precision]
     mask = (1 << 64) - 1
     words = []
     for sd in seeds:

@@ -37,7 +37,7 @@ EXPORTED = (
     "joker_iter_set_round_budget", "joker_accept_noalloc", "joker_linear_posterior",
     "joker_unmarginalized_lnl", "joker_prior_sample", "joker_rv_from_elements",
     "joker_rejection_workspace", "joker_rejection_sample", "joker_refine_band",
-    "joker_iter_read_async",
+    "joker_iter_read_async", "joker_lnl_fused", "joker_accept_fused",
 )
 
 
@@ -91,6 +91,11 @@ _SIGS = {
     "joker_batch_marginal_ln_likelihood": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64, _vp, _vp]),
     "joker_lnl": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _i64, _i64, ctypes.c_int,
                                  _vp, _i64, _vp, _vp, _vp, ctypes.c_int, _i64, _vp]),
+    "joker_lnl_fused": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _i64, _i64, _vp,
+                                       _i64, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i64, _vp]),
+    "joker_accept_fused": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(AcceptSeg), ctypes.c_int,
+                                          _vp, _vp, _vp, _vp, ctypes.c_int, _vp, _i64, _vp, _vp,
+                                          _vp, _vp, _vp, _i64, _vp]),
     "joker_key_to_double": (ctypes.c_double, [ctypes.c_uint64]),
     "joker_accept_workspace": (_i64, [ctypes.POINTER(AcceptSeg), ctypes.c_int]),
     "joker_accept": (ctypes.c_int, [ctypes.POINTER(AcceptSeg), ctypes.c_int, _vp, _vp,

@@ -85,9 +85,10 @@ def chunk_for(n_linear, jitter, precision, n_epochs, path=None):
 
 def tune(table, cache, precision="mixed", n_epochs=None, star0=0, n_sel=None, count=None,
          candidates=CANDIDATE_CHUNKS, reps=3, path=None, write=True):
-    """Time joker_lnl over stars [star0, star0 + n_sel) x cache rows
-    [0, count) for every candidate chunk; record and return the fastest
-    (chunk, {chunk: ms})."""
+    """Time joker_lnl (joker_lnl_fused where "mixed_fast" runs the fused
+    acceptance pass) over stars [star0, star0 + n_sel) x cache rows [0, count)
+    for every candidate chunk; record and return the fastest (chunk,
+    {chunk: ms})."""
     n_sel = table.n_stars - star0 if n_sel is None else int(n_sel)
     count = cache.size if count is None else int(count)
     out = torch.empty((n_sel, count), dtype=torch.float64, device="cuda")
@@ -95,10 +96,20 @@ def tune(table, cache, precision="mixed", n_epochs=None, star0=0, n_sel=None, co
     err = torch.empty((n_sel, count), dtype=torch.float32, device="cuda") if mixed else None
     keys = dev.MaxKeys(n_sel)
     bkeys = dev.MaxKeys(2 * n_sel) if mixed else None
+    fused = dev.fused_available(table, precision)
+    if fused:
+        pcg = dev.pcg_table([(int(s), 1 + 2 * int(s)) for s in range(n_sel)])
+        cand_ld, cand = dev.cand_words(n_sel, count)
     times = {}
     for ch in candidates:
-        run = lambda: dev.lnl(table, cache, out, precision=precision, star0=star0, n_sel=n_sel,
-                              count=count, max_keys=keys, err=err, bound_keys=bkeys, chunk=ch)
+        if fused:
+            run = lambda: dev.lnl_fused(table, cache, out, err, bkeys, pcg, cand, cand_ld,
+                                        star0=star0, n_sel=n_sel, count=count, max_keys=keys,
+                                        chunk=ch)
+        else:
+            run = lambda: dev.lnl(table, cache, out, precision=precision, star0=star0,
+                                  n_sel=n_sel, count=count, max_keys=keys, err=err,
+                                  bound_keys=bkeys, chunk=ch)
         run()
         torch.cuda.synchronize()
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -35,8 +35,9 @@ class BatchRejection:
     """Rejection sampling of ``stars`` (dicts as StarTable takes) against a
     PriorCache.
 
-    precision: "mixed" (default; acceptance refined to the FP64 decisions) or
-    "fp64".  group: stars per launch (bounded by device memory: 12 bytes per
+    precision: "mixed" (default; acceptance refined to the FP64 decisions),
+    "mixed_fast" (the same decisions, with the first acceptance pass fused
+    into the ln L kernel) or "fp64".  group: stars per launch (bounded by device memory: 12 bytes per
     star and sample for the mixed path).  seeds: one seed per star for its
     numpy PCG64 generator (its first ``n`` uniforms are the star's ``uu``).
     chunk: samples per ln L work item (None: the autotuned size, autotune.py).
@@ -73,6 +74,12 @@ class BatchRejection:
             if precision != "fp64" else None
         self.keys = dev.MaxKeys(G)
         self.bkeys = dev.MaxKeys(2 * G) if precision != "fp64" else None
+        # "mixed_fast": the first acceptance pass runs inside the ln L kernel
+        # (joker_lnl_fused), leaving one candidate bit per sample
+        self.fused = dev.fused_available(self.table, precision)
+        if self.fused:
+            self.pcg_dev = dev.pcg_table(self.pcg)
+            self.cand_ld, self.cand = dev.cand_words(G, S)
         self.out_idx = torch.empty(self.n_stars * self.max_out, dtype=torch.int64, device="cuda")
         self.out_lnl = torch.empty(self.n_stars * self.max_out, dtype=torch.float64,
                                    device="cuda")
@@ -99,10 +106,16 @@ class BatchRejection:
             if self.timing:
                 ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                 ev[0].record(stream)
-            dev.lnl(self.table, self.cache, out, precision=self.precision, star0=g0, n_sel=n,
-                    row0=row0, count=S, max_keys=self.keys,
-                    err=self.err[:n] if err is not None else None, bound_keys=self.bkeys,
-                    chunk=self.chunk, stream=stream)
+            if self.fused:
+                dev.lnl_fused(self.table, self.cache, out, self.err[:n], self.bkeys,
+                              self.pcg_dev[g0:g0 + n], self.cand, self.cand_ld, star0=g0,
+                              n_sel=n, row0=row0, count=S, max_keys=self.keys,
+                              chunk=min(self.chunk, 8192), stream=stream)
+            else:
+                dev.lnl(self.table, self.cache, out, precision=self.precision, star0=g0,
+                        n_sel=n, row0=row0, count=S, max_keys=self.keys,
+                        err=self.err[:n] if err is not None else None, bound_keys=self.bkeys,
+                        chunk=self.chunk, stream=stream)
             if self.timing:
                 ev[1].record(stream)
                 self.lnl_events.append(ev)
@@ -118,6 +131,12 @@ class BatchRejection:
                 dev.accept(self.lnl.view(-1), self.keys, segs, u_source="pcg64",
                            out_idx=self.out_idx, out_lnl=self.out_lnl, counts=cnt,
                            stream=stream)
+            elif self.fused:
+                _, _, _, _, nref = dev.accept_fused(
+                    self.table, self.cache, self.lnl.view(-1), self.err.view(-1), self.bkeys,
+                    self.cand, self.cand_ld, segs, out_idx=self.out_idx, out_lnl=self.out_lnl,
+                    counts=cnt, stream=stream)
+                refined += nref
             else:
                 _, _, _, _, nref = dev.accept_refined(
                     self.table, self.cache, self.lnl.view(-1), self.err.view(-1), self.bkeys,

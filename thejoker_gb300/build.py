@@ -15,7 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(OUT_DIR, "libjoker_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["joker_lnl.cu", "joker_lnl_packed.cu", "joker_lnl_fast.cu", "joker_accept.cu",
+SOURCES = ["joker_lnl.cu", "joker_lnl_packed.cu", "joker_lnl_fast.cu", "joker_lnl_fused.cu",
+           "joker_accept.cu",
            "joker_tier2.cu", "joker_abi.cu",
            "joker_noalloc.cu", "joker_iter.cu", "joker_posterior.cu", "joker_prior.cu"]
 HEADERS = ["joker_internal.cuh", "joker_math.cuh", "joker_fp64.cuh", "joker_mixed.cuh",

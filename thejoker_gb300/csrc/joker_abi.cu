@@ -734,6 +734,36 @@ static float err_c0() {
     return c0;
 }
 
+// Arguments of an implicit-item launch over stars [star0, star0 + n_sel) x
+// cache rows [row0, row0 + count) (validated by the caller); false when the
+// work items do not fit in an int.
+static bool lnl_args(const joker_stars *s, const joker_cache *c, int star0, int n_sel,
+                     int64_t row0, int64_t count, double *d_lnl, int64_t ld,
+                     uint64_t *d_max_key, int64_t chunk, LnlArgs &a) {
+    memset(&a, 0, sizeof a);
+    a.stars = s->d_stars;
+    a.ep64 = s->d_ep64;
+    a.ep32 = s->d_ep32;
+    a.P = c->P; a.e = c->E; a.om = c->OM; a.M0 = c->M0; a.s = c->S;
+    a.stride = c->stride;
+    a.mx_a = c->mx_a; a.mx_b = c->mx_b; a.mx_s2 = c->mx_s2;
+    a.queue = s->d_queue;
+    a.lnl = d_lnl;
+    a.max_key = (unsigned long long *)d_max_key;
+    a.star0 = star0;
+    a.n_sel = n_sel;
+    a.row0 = row0;
+    a.count = count;
+    a.ld = ld;
+    a.chunk = (int)chunk;
+    a.ips = (count + chunk - 1) / chunk;
+    a.order = (star0 == 0 && n_sel == s->n_stars) ? s->d_order : nullptr;
+    const int64_t items = a.ips * n_sel;
+    if (items > INT32_MAX) return false;
+    a.n_items = (int)items;
+    return true;
+}
+
 extern "C" int joker_lnl(const joker_stars *s, const joker_cache *c, int star0, int n_sel,
                          int64_t row0, int64_t count, int precision, double *d_lnl, int64_t ld,
                          uint64_t *d_max_key, float *d_err, uint64_t *d_bound_key, int block,
@@ -756,33 +786,63 @@ extern "C" int joker_lnl(const joker_stars *s, const joker_cache *c, int star0, 
     if (chunk <= 0) chunk = 1024;
     if (chunk % block) return fail(JOKER_EINVAL, "joker_lnl: chunk must be a multiple of block");
     LnlArgs a;
-    memset(&a, 0, sizeof a);
-    a.stars = s->d_stars;
-    a.ep64 = s->d_ep64;
-    a.ep32 = s->d_ep32;
-    a.P = c->P; a.e = c->E; a.om = c->OM; a.M0 = c->M0; a.s = c->S;
-    a.stride = c->stride;
-    a.mx_a = c->mx_a; a.mx_b = c->mx_b; a.mx_s2 = c->mx_s2;
-    a.queue = s->d_queue;
-    a.lnl = d_lnl;
-    a.max_key = (unsigned long long *)d_max_key;
+    if (!lnl_args(s, c, star0, n_sel, row0, count, d_lnl, ld, d_max_key, chunk, a))
+        return fail(JOKER_ERANGE, "joker_lnl: too many work items; use a larger chunk");
     if (precision != JOKER_FP64) {
         a.err = d_err;
         a.bound_key = (unsigned long long *)d_bound_key;
         a.err_c0 = err_c0();
     }
-    a.star0 = star0;
-    a.n_sel = n_sel;
-    a.row0 = row0;
-    a.count = count;
-    a.ld = ld;
-    a.chunk = (int)chunk;
-    a.ips = (count + chunk - 1) / chunk;
-    a.order = (star0 == 0 && n_sel == s->n_stars) ? s->d_order : nullptr;
-    const int64_t items = a.ips * n_sel;
-    if (items > INT32_MAX) return fail(JOKER_ERANGE, "joker_lnl: too many work items; use a larger chunk");
-    a.n_items = (int)items;
     return run_lnl(s, precision, a, block, (cudaStream_t)stream);
+}
+
+namespace joker {
+cudaError_t launch_lnl_fused(int L, bool jit, const LnlArgs &a, int block, cudaStream_t st);
+cudaError_t launch_accept_fused(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st);
+}
+
+extern "C" int joker_lnl_fused(const joker_stars *s, const joker_cache *c, int star0, int n_sel,
+                               int64_t row0, int64_t count, const uint64_t *d_pcg, int64_t first,
+                               double *d_lnl, int64_t ld, uint64_t *d_max_key, float *d_err,
+                               uint64_t *d_bound_key, uint32_t *d_cand, int64_t cand_ld,
+                               int64_t chunk, void *stream) {
+    if (!s || !c) return fail(JOKER_EINVAL, "joker_lnl_fused: NULL handle");
+    if (star0 < 0 || n_sel < 0 || star0 + n_sel > s->n_stars)
+        return fail(JOKER_EINVAL, "joker_lnl_fused: stars [%d, %d) outside [0, %d)", star0,
+                    star0 + n_sel, s->n_stars);
+    if (row0 < 0 || count < 0 || row0 + count > c->cap)
+        return fail(JOKER_ERANGE, "joker_lnl_fused: rows [%lld, %lld) outside the cache (%lld)",
+                    (long long)row0, (long long)(row0 + count), (long long)c->cap);
+    if (n_sel == 0 || count == 0) return JOKER_OK;
+    if (!d_lnl || !d_err || !d_bound_key || !d_pcg || !d_cand)
+        return fail(JOKER_EINVAL, "joker_lnl_fused: NULL device pointer");
+    if (s->jitter == JOKER_JITTER_APPLIED && s->L > 3)
+        return fail(JOKER_EINVAL, "joker_lnl_fused: at most 3 linear parameters with the jitter "
+                                  "applied (this table has %d)", s->L);
+    if (ld < count) return fail(JOKER_EINVAL, "joker_lnl_fused: ld < count");
+    if (first < 0 || first % 32)
+        return fail(JOKER_EINVAL, "joker_lnl_fused: first must be a non-negative multiple of 32");
+    if (cand_ld < (first + count + 31) / 32)
+        return fail(JOKER_EINVAL, "joker_lnl_fused: cand_ld %lld < %lld words",
+                    (long long)cand_ld, (long long)((first + count + 31) / 32));
+    if (chunk <= 0) chunk = 1024;
+    if (chunk % 128 || chunk > FUSED_MAX_CHUNK)
+        return fail(JOKER_EINVAL, "joker_lnl_fused: chunk must be a multiple of 128 and at most %d",
+                    FUSED_MAX_CHUNK);
+    LnlArgs a;
+    if (!lnl_args(s, c, star0, n_sel, row0, count, d_lnl, ld, d_max_key, chunk, a))
+        return fail(JOKER_ERANGE, "joker_lnl_fused: too many work items; use a larger chunk");
+    a.err = d_err;
+    a.bound_key = (unsigned long long *)d_bound_key;
+    a.err_c0 = err_c0();
+    a.fa_pcg = (const unsigned long long *)d_pcg;
+    a.fa_first = first;
+    a.cand_words = d_cand;
+    a.cand_ld = cand_ld;
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemsetAsync(s->d_queue, 0, sizeof(int), st));
+    CUDA_TRY(launch_lnl_fused(s->L, s->jitter == JOKER_JITTER_APPLIED, a, 128, st));
+    return JOKER_OK;
 }
 
 // ---------------------------------------------------------------- acceptance
@@ -985,12 +1045,51 @@ extern "C" int joker_accept_refined(const joker_stars *s, const joker_cache *c,
                                  "joker_accept_refined");
     if (rc != JOKER_OK) return rc;
     if (!max_given) CUDA_TRY(cudaMemsetAsync(d_exact_key, 0, sizeof(uint64_t) * n_slots, st));
+    a.write_max = 1;
     a.u_source = u_source;
     a.u = d_u;
     a.out_idx = d_out_idx;
     a.out_lnl = d_out_lnl;
     a.count = d_count;
     CUDA_TRY(launch_accept(a, nb, st, max_given != 0));
+    return JOKER_OK;
+}
+
+extern "C" int joker_accept_fused(const joker_stars *s, const joker_cache *c,
+                                  const joker_accept_seg *segs, int n_segs, double *d_lnl,
+                                  float *d_err, const uint64_t *d_bound_key,
+                                  uint64_t *d_exact_key, int n_slots, const uint32_t *d_cand,
+                                  int64_t cand_ld, int64_t *d_out_idx, double *d_out_lnl,
+                                  int64_t *d_count, uint64_t *d_n_refined, void *d_work,
+                                  int64_t work_bytes, void *stream) {
+    if (n_segs <= 0) return JOKER_OK;
+    if (!d_out_idx || !d_count || !d_cand)
+        return fail(JOKER_EINVAL, "joker_accept_fused: NULL argument");
+    if (cand_ld % 4 || ((uintptr_t)d_cand) % 16)
+        return fail(JOKER_EINVAL, "joker_accept_fused: cand_ld must be a multiple of 4 and "
+                                  "d_cand 16-byte aligned");
+    if (segs)
+        for (int i = 0; i < n_segs; ++i)
+            if (segs[i].n > 32 * cand_ld)
+                return fail(JOKER_EINVAL, "joker_accept_fused: segment %d has %lld samples, "
+                                          "cand_ld %lld words", i, (long long)segs[i].n,
+                            (long long)cand_ld);
+    AcceptArgs a;
+    int64_t nb = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int rc = refined_setup(s, c, segs, n_segs, d_lnl, d_err, d_bound_key, d_exact_key,
+                                 n_slots, d_n_refined, d_work, work_bytes, st, a, nb,
+                                 "joker_accept_fused");
+    if (rc != JOKER_OK) return rc;
+    CUDA_TRY(cudaMemsetAsync(d_exact_key, 0, sizeof(uint64_t) * n_slots, st));
+    a.write_max = 1;
+    a.u_source = JOKER_U_PCG64;
+    a.out_idx = d_out_idx;
+    a.out_lnl = d_out_lnl;
+    a.count = d_count;
+    a.cand_words = d_cand;
+    a.cand_ld = cand_ld;
+    CUDA_TRY(launch_accept_fused(a, nb, st));
     return JOKER_OK;
 }
 
@@ -1023,24 +1122,37 @@ static void rejection_segs(int star0, int n_sel, int64_t row0, int64_t count, in
 
 // Scratch layout: ln L (n_sel x count doubles), bounds (n_sel x count
 // floats, mixed only), 4 n_sel keys (running maxima, two bound maxima,
-// FP64 maxima), then the acceptance workspace.
-static int64_t rejection_bytes(int n_sel, int64_t count, int64_t max_out, int precision,
-                               int64_t *off_err, int64_t *off_keys, int64_t *off_acc) {
+// FP64 maxima); for JOKER_MIXED_FAST the generator states (4 words per star)
+// and the fused pass's candidate bits (cand_ld words per star); then the
+// acceptance workspace.
+struct RejLayout {
+    int64_t err, keys, pcg, cand, acc, total, cand_ld;
+};
+
+static RejLayout rejection_layout(int n_sel, int64_t count, int64_t max_out, int precision) {
     std::vector<joker_accept_seg> segs;
     rejection_segs(0, n_sel, 0, count, max_out, nullptr, segs);
+    RejLayout r;
     const int64_t lnl = align256(8 * (int64_t)n_sel * count);
     const int64_t err = precision == JOKER_FP64 ? 0 : align256(4 * (int64_t)n_sel * count);
     const int64_t keys = align256(8 * 4 * (int64_t)n_sel);
-    if (off_err) *off_err = lnl;
-    if (off_keys) *off_keys = lnl + err;
-    if (off_acc) *off_acc = lnl + err + keys;
-    return lnl + err + keys + joker_accept_workspace(segs.data(), n_sel);
+    const bool fused = precision == JOKER_MIXED_FAST;
+    r.cand_ld = ((count + 31) / 32 + 7) & ~(int64_t)7;
+    const int64_t pcg = fused ? align256(32 * (int64_t)n_sel) : 0;
+    const int64_t cand = fused ? align256(4 * r.cand_ld * (int64_t)n_sel) : 0;
+    r.err = lnl;
+    r.keys = lnl + err;
+    r.pcg = r.keys + keys;
+    r.cand = r.pcg + pcg;
+    r.acc = r.cand + cand;
+    r.total = r.acc + joker_accept_workspace(segs.data(), n_sel);
+    return r;
 }
 
 extern "C" int64_t joker_rejection_workspace(int n_sel, int64_t count, int64_t max_out,
                                              int precision) {
     if (n_sel <= 0 || count <= 0 || max_out < 0) return 0;
-    return rejection_bytes(n_sel, count, max_out, precision, nullptr, nullptr, nullptr);
+    return rejection_layout(n_sel, count, max_out, precision).total;
 }
 
 extern "C" int joker_rejection_sample(const joker_stars *s, const joker_cache *c, int star0,
@@ -1054,31 +1166,43 @@ extern "C" int joker_rejection_sample(const joker_stars *s, const joker_cache *c
     if (n_sel == 0 || count == 0) return JOKER_OK;
     if (!pcg || !d_out_idx || !d_count || !d_work)
         return fail(JOKER_EINVAL, "joker_rejection_sample: NULL argument");
-    int64_t off_err, off_keys, off_acc;
-    const int64_t need = rejection_bytes(n_sel, count, max_out, precision, &off_err, &off_keys,
-                                         &off_acc);
-    if (work_bytes < need)
+    const RejLayout lay = rejection_layout(n_sel, count, max_out, precision);
+    if (work_bytes < lay.total)
         return fail(JOKER_EINVAL, "joker_rejection_sample: workspace %lld bytes, needs %lld",
-                    (long long)work_bytes, (long long)need);
+                    (long long)work_bytes, (long long)lay.total);
     if (((uintptr_t)d_work) % 256)
         return fail(JOKER_EINVAL, "joker_rejection_sample: workspace not 256-byte aligned");
     char *w = (char *)d_work;
     double *lnl = (double *)w;
-    float *err = precision == JOKER_FP64 ? nullptr : (float *)(w + off_err);
-    uint64_t *keys = (uint64_t *)(w + off_keys);
+    float *err = precision == JOKER_FP64 ? nullptr : (float *)(w + lay.err);
+    uint64_t *keys = (uint64_t *)(w + lay.keys);
     uint64_t *max_key = keys, *bound_key = keys + n_sel, *exact_key = keys + 3 * n_sel;
     cudaStream_t st = (cudaStream_t)stream;
     CUDA_TRY(cudaMemsetAsync(keys, 0, 8 * 4 * (size_t)n_sel, st));
+    std::vector<joker_accept_seg> segs;
+    rejection_segs(star0, n_sel, row0, count, max_out, pcg, segs);
+    const int64_t acc_bytes = work_bytes - lay.acc;
+    // JOKER_MIXED_FAST: the first acceptance pass fused into the ln L kernel
+    // (a jittered table with more than three linear parameters runs the
+    // float-float kernel and the separate passes instead)
+    if (precision == JOKER_MIXED_FAST && !(s->jitter == JOKER_JITTER_APPLIED && s->L > 3)) {
+        uint64_t *d_pcg = (uint64_t *)(w + lay.pcg);
+        uint32_t *cand = (uint32_t *)(w + lay.cand);
+        CUDA_TRY(cudaMemcpyAsync(d_pcg, pcg, 32 * (size_t)n_sel, cudaMemcpyHostToDevice, st));
+        int rc = joker_lnl_fused(s, c, star0, n_sel, row0, count, d_pcg, 0, lnl, count, max_key,
+                                 err, bound_key, cand, lay.cand_ld, 0, stream);
+        if (rc != JOKER_OK) return rc;
+        return joker_accept_fused(s, c, segs.data(), n_sel, lnl, err, bound_key, exact_key,
+                                  n_sel, cand, lay.cand_ld, d_out_idx, d_out_lnl, d_count,
+                                  nullptr, w + lay.acc, acc_bytes, stream);
+    }
     int rc = joker_lnl(s, c, star0, n_sel, row0, count, precision, lnl, count, max_key, err,
                        bound_key, 0, 0, stream);
     if (rc != JOKER_OK) return rc;
-    std::vector<joker_accept_seg> segs;
-    rejection_segs(star0, n_sel, row0, count, max_out, pcg, segs);
-    const int64_t acc_bytes = work_bytes - off_acc;
     if (precision == JOKER_FP64)
         return joker_accept(segs.data(), n_sel, lnl, max_key, JOKER_U_PCG64, nullptr, d_out_idx,
-                            d_out_lnl, d_count, w + off_acc, acc_bytes, stream);
+                            d_out_lnl, d_count, w + lay.acc, acc_bytes, stream);
     return joker_accept_refined(s, c, segs.data(), n_sel, lnl, err, bound_key, exact_key, n_sel, 0,
                                 JOKER_U_PCG64, nullptr, d_out_idx, d_out_lnl, d_count, nullptr,
-                                w + off_acc, acc_bytes, stream);
+                                w + lay.acc, acc_bytes, stream);
 }

@@ -21,6 +21,8 @@
 // The uniforms come either from a device array or from numpy's PCG64 stream,
 // regenerated here from the generator state (joker_math.cuh), so the draws are
 // bit-identical to rng.uniform() on the host.
+#include <algorithm>
+
 #include "joker_fp64.cuh"
 
 namespace joker {
@@ -99,16 +101,6 @@ __device__ __forceinline__ bool dbl_to_float_trunc(double x, float &f) {
     const unsigned mant = (unsigned)(b >> 29) & 0x7fffffu;
     f = __int_as_float((hi & (int)0x80000000) | ((ex - 1023 + 127) << 23) | (int)mant);
     return true;
-}
-
-// u = m 2^-53 (m the 53-bit integer of numpy's uniform double) as a float
-// truncated to 24 significant bits; m must be nonzero.
-__device__ __forceinline__ float u53_to_float(uint64_t m) {
-    const int lz = __clzll(m);                       // 11..63
-    const uint64_t norm = m << lz;                   // leading one at bit 63
-    const unsigned mant = (unsigned)(norm >> 40) & 0x7fffffu;
-    const int e2 = 63 - lz - 53;                     // u in [2^e2, 2^(e2+1))
-    return __int_as_float(((e2 + 127) << 23) | (int)mant);
 }
 
 // Decision of exp(v + [-er, er] - mx) > u from float approximations:
@@ -211,6 +203,10 @@ __global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
         if (a.n_refined) atomicAdd(a.n_refined, 1ull);
         if (MODE == 0) {
             atomicMax(a.exact_key + sg.max_slot, double_to_key(v));
+            if (a.write_max) {
+                const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
+                const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
+            }
         } else if (MODE == 2) {
             const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
             const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
@@ -259,6 +255,12 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
         any |= (v.x | v.y | v.z | v.w) != 0u;
     }
     if (!any) continue;
+    if (MODE != 1) {
+        // consumed: cleared, so that a later pass can flag into zero words
+        uint4 *pw = reinterpret_cast<uint4 *>(a.amb_words + w0);
+#pragma unroll
+        for (int q = 0; q < WORDS_PER_THREAD / 4; ++q) pw[q] = make_uint4(0u, 0u, 0u, 0u);
+    }
     const int64_t gblk = w0 / ACC_THREADS;
     const int si = find_seg(a, gblk);
     const joker_accept_seg sg = a.segs[si];
@@ -282,6 +284,10 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
             if (a.n_refined) atomicAdd(a.n_refined, 1ull);
             if (MODE == 0) {
                 atomicMax(a.exact_key + sg.max_slot, double_to_key(v));
+                if (a.write_max) {
+                    const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
+                    const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
+                }
             } else if (MODE == 2) {
                 const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
                 const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
@@ -445,28 +451,203 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
     }
 }
 
-// One CTA per segment: exclusive scan of that segment's per-CTA counts.
-__global__ void __launch_bounds__(ACC_THREADS) accept_scan_kernel(AcceptArgs a) {
-    const int si = blockIdx.x;
-    const int64_t b0 = seg_base(a, si), nb = seg_base(a, si + 1) - b0;
-    __shared__ int64_t s_part[ACC_THREADS];
-    int64_t carry = 0;
-    for (int64_t base = 0; base < nb; base += ACC_THREADS) {
-        const int64_t b = base + threadIdx.x;
-        const int64_t v = (b < nb) ? a.blk_count[b0 + b] : 0;
-        s_part[threadIdx.x] = v;
-        __syncthreads();
-        // Hillis-Steele inclusive scan
-        for (int off = 1; off < ACC_THREADS; off <<= 1) {
-            const int64_t add = (threadIdx.x >= off) ? s_part[threadIdx.x - off] : 0;
-            __syncthreads();
-            s_part[threadIdx.x] += add;
-            __syncthreads();
+// ---- second stage of the fused pass -----------------------------------------
+// The ln L kernel has left one candidate bit per sample (cand_words); every
+// sample without it is rejected.  These scans read the bits (1/96 of the
+// bytes of ln L and its bound) and touch ln L only where a bit is set.
+
+__device__ __forceinline__ uint32_t cand_word(const AcceptArgs &a, int si, int64_t n,
+                                              int64_t first) {
+    if (first >= n) return 0u;
+    uint32_t w = a.cand_words[(int64_t)si * a.cand_ld + (first >> 5)];
+    if (n - first < 32) w &= (1u << (n - first)) - 1u;
+    return w;
+}
+
+// Both scans take one 8192-sample CTA block per warp (grid-stride): each lane
+// loads 8 of the block's 256 words of candidate bits (two 16-byte loads, all
+// independent), and only the nonzero words are visited, each by the whole
+// warp (lane b on the word's sample b).  The arrays they fill (amb_words,
+// words) and the per-CTA counts are zeroed before; a block without candidate
+// bits costs its loads.
+struct FusedBlock {
+    int si;
+    joker_accept_seg sg;
+    int64_t gblk, first;      // CTA block; its first sample in the segment
+    uint32_t wv[8];           // words 8 lane .. 8 lane + 7 of the block
+};
+
+__device__ __forceinline__ void fused_block(const AcceptArgs &a, int64_t gblk, FusedBlock &b) {
+    const int lane = threadIdx.x & 31;
+    b.gblk = gblk;
+    b.si = find_seg(a, gblk);
+    b.sg = a.segs[b.si];
+    b.first = (gblk - seg_base(a, b.si)) * ACC_BLOCK;
+    const int64_t nw = (b.sg.n + 31) >> 5;                  // words of the segment
+    const int64_t w0 = (b.first >> 5) + 8 * lane;
+    const uint32_t *row = a.cand_words + (int64_t)b.si * a.cand_ld;
+    if (w0 + 8 <= nw) {
+        const uint4 p = *reinterpret_cast<const uint4 *>(row + w0);
+        const uint4 q = *reinterpret_cast<const uint4 *>(row + w0 + 4);
+        b.wv[0] = p.x; b.wv[1] = p.y; b.wv[2] = p.z; b.wv[3] = p.w;
+        b.wv[4] = q.x; b.wv[5] = q.y; b.wv[6] = q.z; b.wv[7] = q.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) b.wv[j] = w0 + j < nw ? row[w0 + j] : 0u;
+    }
+    // the segment's last word: bits past its last sample
+    const int64_t tail = b.sg.n & 31;
+    if (tail) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (w0 + j == nw - 1) b.wv[j] &= (1u << tail) - 1u;
+    }
+}
+
+// Visit every nonzero word of the block: fn(word index in the block, bits),
+// called by all lanes (warp-uniform).
+template <class F>
+__device__ __forceinline__ void for_nonzero_words(const FusedBlock &b, F fn) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        unsigned owners = __ballot_sync(0xffffffffu, b.wv[j] != 0u);
+        while (owners) {
+            const int l = __ffs(owners) - 1;
+            owners &= owners - 1;
+            fn(8 * l + j, __shfl_sync(0xffffffffu, b.wv[j], l));
         }
-        if (b < nb) a.blk_count[b0 + b] = carry + s_part[threadIdx.x] - v;
-        const int64_t tot = s_part[ACC_THREADS - 1];
+    }
+}
+
+// Candidates for each segment's FP64 maximum: the candidate samples whose
+// upper bound reaches the largest lower bound, plus those without a usable
+// bound (as accept_candidates_kernel, over the bits only); flag list 0,
+// past its capacity bits in amb_words.
+__global__ void __launch_bounds__(ACC_THREADS) fused_max_cands_kernel(AcceptArgs a, int64_t nbk) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (ACC_THREADS / 32);
+    for (int64_t gblk = blockIdx.x * (int64_t)(ACC_THREADS / 32) + (threadIdx.x >> 5);
+         gblk < nbk; gblk += nwarps) {
+        FusedBlock b;
+        fused_block(a, gblk, b);
+        const double lb = key_to_double(a.bound_key[2 * b.sg.max_slot + 1]);
+        for_nonzero_words(b, [&](int w, uint32_t bits) {
+            const int64_t i = b.first + 32 * w + lane;
+            bool cand = false;
+            if ((bits >> lane) & 1u) {
+                const double v = a.lnl[b.sg.lnl_off + i];
+                const float er = a.err[b.sg.lnl_off + i];
+                cand = (v + (double)er >= lb) || !(er < 1e29f) || !(v == v);
+            }
+            const uint32_t over = __ballot_sync(0xffffffffu, !flag_append(a, 0, cand, b.si, i));
+            if (over && lane == 0) a.amb_words[gblk * ACC_THREADS + w] = over;
+        });
+    }
+}
+
+// The decisions: the mark pass over the candidate bits.  For each nonzero
+// word its 32 lanes regenerate their uniforms -- the block's state by one
+// jump, then a table step to the word and one to the lane -- and decide the
+// candidates against the FP64 maximum as the mark pass does; kept bits go
+// to words, undecided samples to flag list 1 (past its capacity to
+// amb_words), the kept count to the block's counter.
+__global__ void __launch_bounds__(ACC_THREADS) fused_decide_kernel(AcceptArgs a, int64_t nbk) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (ACC_THREADS / 32);
+    for (int64_t gblk = blockIdx.x * (int64_t)(ACC_THREADS / 32) + (threadIdx.x >> 5);
+         gblk < nbk; gblk += nwarps) {
+        FusedBlock b;
+        fused_block(a, gblk, b);
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) any |= b.wv[j] != 0u;
+        if (!__any_sync(0xffffffffu, any)) continue;
+        const double mx = key_to_double(a.exact_key[b.sg.max_slot]);
+        float mxf;
+        const bool fast = dbl_to_float_trunc(mx, mxf);
+        const u128 inc = ((u128)b.sg.pcg_inc_hi << 64) | (u128)b.sg.pcg_inc_lo;
+        const u128 sblk = pcg_jump(((u128)b.sg.pcg_state_hi << 64) | (u128)b.sg.pcg_state_lo, inc,
+                                   (uint64_t)b.first);
+        const unsigned long long *lt = g_pcg_thr.v[lane];
+        const u128 a_lane = ((u128)lt[1] << 64) | (u128)lt[0];
+        const u128 c_lane = (((u128)lt[3] << 64) | (u128)lt[2]) * inc;
+        int count = 0;
+        for_nonzero_words(b, [&](int w, uint32_t bits) {
+            const int64_t i = b.first + 32 * w + lane;
+            const unsigned long long *wt = g_pcg_w32.v[w];
+            const u128 sw = (((u128)wt[1] << 64) | (u128)wt[0]) * sblk +
+                            (((u128)wt[3] << 64) | (u128)wt[2]) * inc;
+            bool keep = false, amb = false;
+            if ((bits >> lane) & 1u) {
+                const uint64_t m = pcg_output(a_lane * sw + c_lane) >> 11;
+                const double v = a.lnl[b.sg.lnl_off + i];
+                const float er = a.err[b.sg.lnl_off + i];
+                float vf;
+                int dec = 2;
+                if (fast && m != 0 && er < 1e29f && dbl_to_float_trunc(v, vf))
+                    dec = fast_decide(vf, er, mxf, u53_to_float(m));
+                if (dec == 2) dec = interval_test(v, er, mx, (double)m * 0x1.0p-53);
+                keep = dec == 1;
+                amb = dec < 0;
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+            const uint32_t over = __ballot_sync(0xffffffffu, !flag_append(a, 1, amb, b.si, i));
+            if (lane == 0) {
+                if (bal) a.words[gblk * ACC_THREADS + w] = bal;
+                if (over) a.amb_words[gblk * ACC_THREADS + w] = over;
+            }
+            count += __popc(bal);
+        });
+        if (lane == 0 && count)
+            atomicAdd((unsigned long long *)(a.blk_count + gblk), (unsigned long long)count);
+    }
+}
+
+// One CTA per segment: exclusive scan of that segment's per-CTA counts,
+// SCAN_PER consecutive counts per thread (SCAN_THREADS x SCAN_PER per round),
+// warp shuffles for the block-wide part.
+constexpr int SCAN_THREADS = 1024, SCAN_PER = 8;
+
+__global__ void __launch_bounds__(SCAN_THREADS) accept_scan_kernel(AcceptArgs a) {
+    const int si = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t b0 = seg_base(a, si), nb = seg_base(a, si + 1) - b0;
+    __shared__ int64_t s_w[SCAN_THREADS / 32];
+    int64_t carry = 0;
+    for (int64_t base = 0; base < nb; base += (int64_t)SCAN_THREADS * SCAN_PER) {
+        const int64_t e0 = base + (int64_t)threadIdx.x * SCAN_PER;
+        int64_t v[SCAN_PER], sum = 0;
+#pragma unroll
+        for (int j = 0; j < SCAN_PER; ++j) {
+            v[j] = e0 + j < nb ? a.blk_count[b0 + e0 + j] : 0;
+            sum += v[j];
+        }
+        int64_t x = sum;                                   // inclusive scan in the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_w[warp] = x;
         __syncthreads();
-        carry += tot;
+        if (warp == 0) {
+            int64_t t = s_w[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int64_t y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            s_w[lane] = t;
+        }
+        __syncthreads();
+        int64_t run = carry + (warp ? s_w[warp - 1] : 0) + x - sum;
+#pragma unroll
+        for (int j = 0; j < SCAN_PER; ++j) {
+            if (e0 + j < nb) a.blk_count[b0 + e0 + j] = run;
+            run += v[j];
+        }
+        carry += s_w[SCAN_THREADS / 32 - 1];
+        __syncthreads();
     }
     if (threadIdx.x == 0) a.count[si] = carry;
 }
@@ -486,6 +667,10 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_emit_kernel(AcceptArgs a) 
     const int64_t blk = gblk - seg_base(a, si);
     const int64_t boff = a.blk_count[gblk];
     if (boff >= sg.max_out) continue;
+    // nothing kept in this block: the next block's offset (or the segment's
+    // count) equals this one's
+    const int64_t bnext = gblk + 1 < seg_base(a, si + 1) ? a.blk_count[gblk + 1] : a.count[si];
+    if (bnext == boff) continue;
     const uint32_t word = a.words[gblk * ACC_THREADS + threadIdx.x];
     const int c = __popc(word);
     s_scan[threadIdx.x] = c;
@@ -600,6 +785,8 @@ cudaError_t launch_refine_max(const AcceptArgs &a, int64_t total_blocks, cudaStr
     return launch_fp64_words(0, a, total_blocks, st);
 }
 
+static cudaError_t accept_finish(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st);
+
 cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st,
                           bool max_given) {
     if (a.err != nullptr && !max_given && total_blocks > 0) {
@@ -620,7 +807,39 @@ cudaError_t launch_accept(const AcceptArgs &a, int64_t total_blocks, cudaStream_
             if (e != cudaSuccess) return e;
         }
     }
-    accept_scan_kernel<<<a.n_segs, ACC_THREADS, 0, st>>>(a);
+    return accept_finish(a, total_blocks, st);
+}
+
+// The fused pass's second stage, after the ln L kernel has written the
+// candidate bits (a.cand_words) and the bound maxima; a.exact_key zeroed.
+// The flag words of list 0's overflow are cleared by the FP64 pass that
+// reads them, so list 1's overflow starts from zero words too.
+cudaError_t launch_accept_fused(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st) {
+    if (total_blocks > 0) {
+        const unsigned grid = (unsigned)std::min<int64_t>((total_blocks + 7) / 8, 152 * 8);
+        const size_t wbytes = (size_t)total_blocks * ACC_THREADS * sizeof(uint32_t);
+        cudaError_t e = cudaMemsetAsync(a.flag_count, 0, 2 * sizeof(unsigned long long), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(a.amb_words, 0, wbytes, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(a.words, 0, wbytes, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(a.blk_count, 0, 8 * (size_t)total_blocks, st);
+        if (e != cudaSuccess) return e;
+        fused_max_cands_kernel<<<grid, ACC_THREADS, 0, st>>>(a, total_blocks);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = launch_tier2(a, st)) != cudaSuccess) return e;
+        if ((e = launch_fp64_words(0, a, total_blocks, st)) != cudaSuccess) return e;
+        fused_decide_kernel<<<grid, ACC_THREADS, 0, st>>>(a, total_blocks);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = launch_fp64_words(1, a, total_blocks, st)) != cudaSuccess) return e;
+    }
+    return accept_finish(a, total_blocks, st);
+}
+
+// Counts, offsets and output of an acceptance pass whose words and per-CTA
+// counts are set.
+static cudaError_t accept_finish(const AcceptArgs &a, int64_t total_blocks, cudaStream_t st) {
+    accept_scan_kernel<<<a.n_segs, SCAN_THREADS, 0, st>>>(a);
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || total_blocks == 0) return e;

@@ -344,22 +344,151 @@ __device__ __forceinline__ unsigned long long float_to_dkey(float x) {
     return key_of_bits((long long)d);
 }
 
-__device__ __forceinline__ void fast_store(const LnlArgs &a, int64_t out, bool active, ff lnl,
-                                           float err, unsigned long long *mk,
-                                           unsigned long long *bk) {
-    double d = 0.0;
-    if (active) {
-        d = (double)lnl.hi + (double)lnl.lo;
-        a.lnl[out] = d;
-        if (a.err) a.err[out] = err;
+__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, k, o);
+        k = other > k ? other : k;
     }
-    if (mk) warp_max_update(mk, active ? double_to_key(d) : 0ull);
+    return k;
+}
+
+__device__ __forceinline__ void key_max_update(unsigned long long *key, unsigned long long k) {
+    if ((threadIdx.x & 31) == 0 && k != 0ull) {
+        if (k > *((volatile unsigned long long *)key)) atomicMax(key, k);
+    }
+}
+
+// Both samples of a pass: ln L (and its bound) written out, the running
+// maxima raised (one warp reduction each, over both samples).  Returns the
+// warp's largest lower bound lnL - err as a key (0: none).
+__device__ __forceinline__ unsigned long long fast_store2(const LnlArgs &a, int64_t out0,
+                                                          bool act0, ff l0, float e0,
+                                                          int64_t out1, bool act1, ff l1,
+                                                          float e1, unsigned long long *mk,
+                                                          unsigned long long *bk) {
+    double d0 = 0.0, d1 = 0.0;
+    if (act0) {
+        d0 = (double)l0.hi + (double)l0.lo;
+        a.lnl[out0] = d0;
+        if (a.err) a.err[out0] = e0;
+    }
+    if (act1) {
+        d1 = (double)l1.hi + (double)l1.lo;
+        a.lnl[out1] = d1;
+        if (a.err) a.err[out1] = e1;
+    }
+    auto kmax = [](unsigned long long x, unsigned long long y) { return x > y ? x : y; };
+    if (mk)
+        key_max_update(mk, warp_max_key(kmax(act0 ? double_to_key(d0) : 0ull,
+                                             act1 ? double_to_key(d1) : 0ull)));
+    unsigned long long kd = 0ull;
     if (bk) {
         // lnL + err rounded up and lnL - err rounded down, as floats
-        const float up = __fadd_ru(lnl.hi, __fadd_ru(lnl.lo, err));
-        const float dn = __fadd_rd(lnl.hi, __fsub_rd(lnl.lo, err));
-        warp_max_update(bk, active ? float_to_dkey(up) : 0ull);
-        warp_max_update(bk + 1, active ? float_to_dkey(dn) : 0ull);
+        const float up0 = __fadd_ru(l0.hi, __fadd_ru(l0.lo, e0));
+        const float dn0 = __fadd_rd(l0.hi, __fsub_rd(l0.lo, e0));
+        const float up1 = __fadd_ru(l1.hi, __fadd_ru(l1.lo, e1));
+        const float dn1 = __fadd_rd(l1.hi, __fsub_rd(l1.lo, e1));
+        key_max_update(bk, warp_max_key(kmax(act0 ? float_to_dkey(up0) : 0ull,
+                                             act1 ? float_to_dkey(up1) : 0ull)));
+        kd = warp_max_key(kmax(act0 ? float_to_dkey(dn0) : 0ull, act1 ? float_to_dkey(dn1) : 0ull));
+        key_max_update(bk + 1, kd);
+    }
+    return kd;
+}
+
+// ---- the fused first acceptance pass
+// Thread 0 of the block, at the start of a work item: the generator state
+// before the item's first uniform and every 256 samples after it (the block's
+// passes), the increment, and the 128-step constant S_128 inc.  Shared
+// layout: s[2p], s[2p + 1] pass p (lo, hi); then inc, then S_128 inc.
+constexpr int FUSED_PASSES = FUSED_MAX_CHUNK / 256;
+
+__device__ __forceinline__ void fused_item_states(const LnlArgs &a, const WorkItem &w,
+                                                  unsigned long long *s) {
+    const unsigned long long *g = a.fa_pcg + 4 * (int64_t)w.max_slot;
+    const u128 inc = ((u128)g[2] << 64) | (u128)g[3];
+    u128 x = pcg_jump(((u128)g[0] << 64) | (u128)g[1], inc,
+                      (uint64_t)(a.fa_first + (w.row0 - a.row0)));
+    const u128 A256 = u128_of(g_pcg.dbl_a[8]), C256 = u128_of(g_pcg.dbl_s[8]) * inc;
+    const int np = (w.count + 255) >> 8;
+    for (int p = 0; p < np; ++p) {
+        s[2 * p] = (unsigned long long)x;
+        s[2 * p + 1] = (unsigned long long)(x >> 64);
+        x = A256 * x + C256;
+    }
+    const u128 C128 = u128_of(g_pcg.dbl_s[7]) * inc;
+    s[2 * FUSED_PASSES] = (unsigned long long)inc;
+    s[2 * FUSED_PASSES + 1] = (unsigned long long)(inc >> 64);
+    s[2 * FUSED_PASSES + 2] = (unsigned long long)C128;
+    s[2 * FUSED_PASSES + 3] = (unsigned long long)(C128 >> 64);
+}
+
+// A sample can be accepted only if exp(lnL_64 - max) > u.  With lb the
+// running lower bound of the maximum (lb <= max) and lnL_64 <= lnl + err, a
+// sample with lnl + err - lb < log u is rejected whatever the maximum; every
+// other sample is a candidate, including each one that can be the maximum
+// (lnl + err >= max >= lb).  The float test keeps a margin for the FP32 log
+// of u and for the float forms of lnl and lb, as the acceptance scan does.
+//
+// Most samples need no uniform: x = lnl + err - lb (with the margin) >= 0
+// makes a candidate for any u < 1, and x < -746 rejects for every u,
+// u = 0 included (exp of anything below -745.2 is 0 in FP64).  Returns 0
+// (rejected), 1 (candidate) or 2 (test against u).
+__device__ __forceinline__ int fused_pretest(bool act, ff l, float err, bool lb_ok, float lbf,
+                                             float &x) {
+    x = 0.0f;
+    if (!act) return 0;
+    if (!(err < 1e29f) || !(l.hi == l.hi) || !lb_ok) return 1;
+    const float tol = 1e-4f + 5e-7f * (fabsf(l.hi) + fabsf(lbf) + err);
+    x = (l.hi - lbf) + err + tol;
+    if (x >= 0.0f) return 1;
+    if (x < -746.0f) return 0;
+    return 2;
+}
+
+// The test against u = m 2^-53 of a sample that fused_pretest left open.
+__device__ __forceinline__ int fused_utest(int c, float x, uint64_t m) {
+    if (c != 2) return c;
+    if (m == 0ull) return 1;                          // u = 0: decided in FP64 later
+    return x < __logf(u53_to_float(m)) ? 0 : 1;
+}
+
+template <bool FUSED>
+__device__ __forceinline__ void fused_pass(const LnlArgs &a, const WorkItem &w, int base,
+                                           const unsigned long long *s, unsigned long long kd,
+                                           const unsigned long long *bk, bool act0, ff l0,
+                                           float e0, bool act1, ff l1, float e1) {
+    if constexpr (FUSED) {
+        // the running lower bound: this warp's, or the slot's if larger
+        const unsigned long long gk = *((volatile const unsigned long long *)(bk + 1));
+        const unsigned long long lk = gk > kd ? gk : kd;
+        const bool lb_ok = lk != 0ull && lk != 0xFFFFFFFFFFFFFFFFull;   // a bound, not NaN
+        const float lbf = lb_ok ? __double2float_rd(key_to_double(lk)) : 0.0f;
+        float x0, x1;
+        int c0 = fused_pretest(act0, l0, e0, lb_ok, lbf, x0);
+        int c1 = fused_pretest(act1, l1, e1, lb_ok, lbf, x1);
+        if (__any_sync(0xffffffffu, c0 == 2 || c1 == 2)) {
+            // the uniforms of j0 and j1 = j0 + 128 from the pass's state
+            const int p = base >> 8;
+            const u128 sb = ((u128)s[2 * p + 1] << 64) | (u128)s[2 * p];
+            const u128 inc = ((u128)s[2 * FUSED_PASSES + 1] << 64) | (u128)s[2 * FUSED_PASSES];
+            const u128 C128 =
+                ((u128)s[2 * FUSED_PASSES + 3] << 64) | (u128)s[2 * FUSED_PASSES + 2];
+            const u128 st0 = pcg_thread_step(sb, inc, threadIdx.x);
+            const u128 st1 = u128_of(g_pcg.dbl_a[7]) * st0 + C128;
+            c0 = fused_utest(c0, x0, pcg_output(st0) >> 11);
+            c1 = fused_utest(c1, x1, pcg_output(st1) >> 11);
+        }
+        const unsigned b0 = __ballot_sync(0xffffffffu, c0 == 1);
+        const unsigned b1 = __ballot_sync(0xffffffffu, c1 == 1);
+        if ((threadIdx.x & 31) == 0) {
+            const int wo = base + (int)(threadIdx.x & ~31u);          // the warp's first j0
+            const int64_t q = a.fa_first + (w.row0 - a.row0) + wo;    // its stream position
+            uint32_t *cw = a.cand_words + (int64_t)w.max_slot * a.cand_ld + (q >> 5);
+            if (wo < w.count) cw[0] = b0;
+            if (wo + 128 < w.count) cw[4] = b1;
+        }
     }
 }
 
@@ -370,11 +499,15 @@ __device__ __forceinline__ void fast_store(const LnlArgs &a, int64_t out, bool a
 #endif
 
 // Two samples per thread (paired FP32), any L without jitter, L <= 3 with.
-template <int L, bool JIT, bool PACKED>
+// FUSED: also the first acceptance pass (implicit work items, chunks of at
+// most FUSED_MAX_CHUNK samples): each sample's uniform from its slot's PCG64
+// stream and its candidate bit.
+template <int L, bool JIT, bool PACKED, bool FUSED>
 __global__ void __launch_bounds__(128, JOKER_FAST_MINB)
 lnl_fast2_kernel(LnlArgs a) {
     __shared__ __align__(16) float sm[TILE * REC32];
     __shared__ double smr[PACKED ? PACK_ROWS * 5 : 1];
+    __shared__ unsigned long long s_pcg[FUSED ? 2 * FUSED_PASSES + 4 : 1];
     __shared__ int s_item;
     int staged_star = -1;
     const bool inter = PACKED && packed_interleaved(a);
@@ -388,9 +521,12 @@ lnl_fast2_kernel(LnlArgs a) {
         const StarRec &st = a.stars[w.star];
         const int N = st.n_epochs;
         const bool single = N <= TILE;
+        if (FUSED && threadIdx.x == 0) fused_item_states(a, w, s_pcg);
         if (single && w.star != staged_star) {
             stage_epochs<float, REC32>(sm, a.ep32 + (size_t)st.epoch_off * REC32, N);
             staged_star = w.star;
+            __syncthreads();
+        } else if (FUSED) {
             __syncthreads();
         }
         unsigned long long *mk = a.max_key ? a.max_key + w.max_slot : nullptr;
@@ -425,10 +561,43 @@ lnl_fast2_kernel(LnlArgs a) {
                 fast_tail<L, JIT>(st, accf_lane(A, 0), c0.e, c0.ome, pb0.w, s20, N, a.err_c0, l0, err0);
             if (act1)
                 fast_tail<L, JIT>(st, accf_lane(A, 1), c1.e, c1.ome, pb1.w, s21, N, a.err_c0, l1, err1);
-            fast_store(a, w.out_off + j0, act0, l0, err0, mk, bk);
-            fast_store(a, w.out_off + j1, act1, l1, err1, mk, bk);
+            const unsigned long long kd =
+                fast_store2(a, w.out_off + j0, act0, l0, err0, w.out_off + j1, act1, l1, err1, mk,
+                            bk);
+            fused_pass<FUSED>(a, w, base, s_pcg, kd, bk, act0, l0, err0, act1, l1, err1);
         }
     }
+}
+
+// Launch over the kernel's forms: the prepared cache, or packed FP64 rows
+// prepared in registers (cache views); L <= 6 without the jitter, L <= 3
+// with it.
+template <bool FUSED, int L, bool JIT>
+static cudaError_t launch_fast_LJ(const LnlArgs &a, int block, cudaStream_t st) {
+    if (a.mx_a == nullptr)
+        return launch_persistent(lnl_fast2_kernel<L, JIT, true, FUSED>, a, block, st);
+    return launch_persistent(lnl_fast2_kernel<L, JIT, false, FUSED>, a, block, st);
+}
+
+template <bool FUSED>
+cudaError_t launch_fast_any(int L, bool jit, const LnlArgs &a, int block, cudaStream_t st) {
+    if (jit) {
+        switch (L) {
+            case 1: return launch_fast_LJ<FUSED, 1, true>(a, block, st);
+            case 2: return launch_fast_LJ<FUSED, 2, true>(a, block, st);
+            case 3: return launch_fast_LJ<FUSED, 3, true>(a, block, st);
+        }
+        return cudaErrorInvalidValue;
+    }
+    switch (L) {
+        case 1: return launch_fast_LJ<FUSED, 1, false>(a, block, st);
+        case 2: return launch_fast_LJ<FUSED, 2, false>(a, block, st);
+        case 3: return launch_fast_LJ<FUSED, 3, false>(a, block, st);
+        case 4: return launch_fast_LJ<FUSED, 4, false>(a, block, st);
+        case 5: return launch_fast_LJ<FUSED, 5, false>(a, block, st);
+        case 6: return launch_fast_LJ<FUSED, 6, false>(a, block, st);
+    }
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace joker

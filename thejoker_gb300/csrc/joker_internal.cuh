@@ -101,7 +101,23 @@ struct LnlArgs {
     float *err;
     unsigned long long *bound_key;   // [slot][2]
     float err_c0;                    // column-error constant of the bound
+    // Fused first acceptance pass (FP32-sum kernel, implicit work items; NULL
+    // fa_pcg: none).  Per slot the numpy PCG64 state and increment {state hi,
+    // lo, inc hi, lo} before the slot's first uniform; the sample of row
+    // row0 + j is number fa_first + j of the slot's stream (its uniform the
+    // draw after fa_first + j steps).  Sample q of slot k is a candidate --
+    // bit q % 32 of cand_words[k * cand_ld + q / 32] set -- unless its upper
+    // bound lies below the running lower bound of the maximum by more than
+    // -log u, which rejects it whatever the maximum.
+    const unsigned long long *fa_pcg;
+    int64_t fa_first;
+    uint32_t *cand_words;
+    int64_t cand_ld;
 };
+
+// Largest work item (samples) of the fused pass: its per-pass generator
+// states (one per 256 samples) are kept in shared memory.
+constexpr int FUSED_MAX_CHUNK = 8192;
 
 __device__ __forceinline__ int item_count(const LnlArgs &a) {
     return a.n_items_dev ? *((volatile const int *)a.n_items_dev) : a.n_items;
@@ -137,6 +153,9 @@ struct AcceptArgs {
     int64_t stride;                         // doubles between consecutive samples (1 or 5)
     int L, jit;
     unsigned long long *n_refined;          // samples re-evaluated in FP64 (statistics)
+    int write_max;                          // the maximum's FP64 pass writes its values back
+                                            // to lnl (bound 0), sparing the decisions a
+                                            // second evaluation of those samples
     uint32_t *amb_words;                    // undecided samples, one bit each (refinement)
     // flagged samples (max candidates, then undecided ones) compacted into a
     // list, (segment << 40) | index; entries past flag_cap fall back to
@@ -144,6 +163,10 @@ struct AcceptArgs {
     int64_t *flag_list;
     unsigned long long *flag_count;
     int64_t flag_cap;
+    // candidate bits of the fused first pass: sample i of segment s at bit
+    // i % 32 of cand_words[s * cand_ld + i / 32]
+    const uint32_t *cand_words;
+    int64_t cand_ld;
     const joker_accept_seg *segs;
     const int64_t *blk_base;     // n_segs + 1 prefix of CTA counts
     int64_t fixed_blocks;        // > 0: segment s owns CTA blocks [s * fixed, (s+1) * fixed)

@@ -550,6 +550,7 @@ extern "C" int joker_iter_round(joker_iter *it, void *stream) {
         c.L = L;
         c.jit = jit;
         c.n_refined = it->n_refined;
+        c.write_max = 1;
         c.amb_words = it->amb;
         c.flag_list = it->flag_list;
         c.flag_count = it->flag_count;

@@ -258,6 +258,69 @@ __device__ __forceinline__ double pcg_uniform(uint64_t x) {
     return (double)(x >> 11) * (1.0 / 9007199254740992.0);
 }
 
+// (A^n, S_n) for n = 1..128 as {A lo, A hi, S lo, S hi}: entry t takes a
+// state at position p to the state of position p + t + 1, so that thread t
+// of a 128-thread block (or lane t of a warp) draws the uniform of sample
+// p + t.  In global memory: a warp reads its 32 entries as one coalesced
+// 1 KB line set, where the constant bank would serialise 32 addresses.
+struct PcgThreadTable {
+    unsigned long long v[128][4];
+};
+
+constexpr PcgThreadTable make_pcg_thread_table() {
+    PcgThreadTable t{};
+    const u128 A = ((u128)0x2360ED051FC65DA4ull << 64) | (u128)0x4385DF649FCCF645ull;
+    u128 an = A, sn = 1;                                  // n = 1
+    for (int k = 0; k < 128; ++k) {
+        t.v[k][0] = (unsigned long long)an; t.v[k][1] = (unsigned long long)(an >> 64);
+        t.v[k][2] = (unsigned long long)sn; t.v[k][3] = (unsigned long long)(sn >> 64);
+        sn = sn + an;
+        an = an * A;
+    }
+    return t;
+}
+
+__device__ PcgThreadTable g_pcg_thr = make_pcg_thread_table();
+
+// (A^n, S_n) for n = 32 w, w = 0..255: from the state of the first sample of
+// an 8192-sample block to that of word w (same layout).
+struct PcgWordTable {
+    unsigned long long v[256][4];
+};
+
+constexpr PcgWordTable make_pcg_word_table() {
+    PcgWordTable t{};
+    const u128 A = ((u128)0x2360ED051FC65DA4ull << 64) | (u128)0x4385DF649FCCF645ull;
+    u128 a32 = 1, s32 = 0;                                // (A^32, S_32)
+    for (int k = 0; k < 32; ++k) { s32 = s32 + a32; a32 = a32 * A; }
+    u128 an = 1, sn = 0;                                  // n = 0
+    for (int w = 0; w < 256; ++w) {
+        t.v[w][0] = (unsigned long long)an; t.v[w][1] = (unsigned long long)(an >> 64);
+        t.v[w][2] = (unsigned long long)sn; t.v[w][3] = (unsigned long long)(sn >> 64);
+        sn = sn * a32 + s32;                              // S_(n+32) = S_n A^32 + S_32
+        an = an * a32;
+    }
+    return t;
+}
+
+__device__ PcgWordTable g_pcg_w32 = make_pcg_word_table();
+
+// State of position p + t + 1 from the state x of position p.
+__device__ __forceinline__ u128 pcg_thread_step(u128 x, u128 inc, int t) {
+    const unsigned long long *e = g_pcg_thr.v[t];
+    return (((u128)e[1] << 64) | (u128)e[0]) * x + (((u128)e[3] << 64) | (u128)e[2]) * inc;
+}
+
+// u = m 2^-53 (m the 53-bit integer of numpy's uniform double) as a float
+// truncated to 24 significant bits; m must be nonzero.
+__device__ __forceinline__ float u53_to_float(uint64_t m) {
+    const int lz = __clzll(m);                       // 11..63
+    const uint64_t norm = m << lz;                   // leading one at bit 63
+    const unsigned mant = (unsigned)(norm >> 40) & 0x7fffffu;
+    const int e2 = 63 - lz - 53;                     // u in [2^e2, 2^(e2+1))
+    return __int_as_float(((e2 + 127) << 23) | (int)mant);
+}
+
 }  // namespace joker
 
 namespace joker {

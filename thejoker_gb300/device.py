@@ -422,6 +422,88 @@ def accept_refined(stars, cache, lnl_buf, err, bound_keys, segments, u_source="p
     return out_idx, out_lnl, counts, exact, n_ref
 
 
+def fused_available(stars, precision):
+    """Whether ``precision`` on ``stars`` runs the fused first acceptance pass
+    (joker_lnl_fused): "mixed_fast", with at most three linear parameters
+    when the jitter is applied."""
+    return precision == "mixed_fast" and not (stars.jitter == "applied" and stars.n_linear > 3)
+
+
+def pcg_table(states):
+    """Device table of generator states for joker_lnl_fused: one row
+    {state_hi, state_lo, inc_hi, inc_lo} per (state, inc) or (state, inc,
+    offset) entry of ``states``, as int64 words."""
+    rows = []
+    for s in states:
+        st, inc = s[0], s[1]
+        off = s[2] if len(s) > 2 else 0
+        rows.append([w - (1 << 64) if w >= (1 << 63) else w for w in pcg64_fields(st, inc, off)])
+    return torch.tensor(rows, dtype=torch.int64).view(-1, 4).cuda()
+
+
+def cand_words(n_sel, n_samples):
+    """(cand_ld, tensor) of candidate bits for joker_lnl_fused: n_sel rows of
+    cand_ld 32-bit words, enough for n_samples samples per star."""
+    ld = ((int(n_samples) + 31) // 32 + 7) // 8 * 8
+    return ld, torch.empty((max(int(n_sel), 1), ld), dtype=torch.int32, device="cuda")
+
+
+def lnl_fused(stars, cache, out, err, bound_keys, pcg, cand, cand_ld, star0=0, n_sel=None,
+              row0=0, count=None, first=0, max_keys=None, chunk=0, out_offset=0, stream=None):
+    """ln L at "mixed_fast" with the first acceptance pass fused in
+    (joker_lnl_fused): as ``lnl``, plus each sample's candidate bit in
+    ``cand`` (from cand_words).  ``pcg``: pcg_table of the n_sel stars' streams;
+    row row0 + j is number first + j of each stream."""
+    n_sel = stars.n_stars - star0 if n_sel is None else n_sel
+    count = cache.size - row0 if count is None else count
+    if out.dtype != torch.float64 or out.dim() != 2 or out.shape[0] < n_sel or \
+            out.shape[1] < out_offset + count or not out.is_contiguous():
+        raise ValueError("out must be contiguous float64 with shape (n_sel, >= out_offset + count)")
+    if err.shape != out.shape or not err.is_contiguous() or err.dtype != torch.float32:
+        raise ValueError("err must be contiguous float32 shaped like out")
+    nat.check(nat.lib().joker_lnl_fused(
+        stars.handle, cache.handle, int(star0), int(n_sel), int(row0), int(count),
+        ctypes.c_void_p(pcg.data_ptr()), int(first),
+        ctypes.c_void_p(out.data_ptr() + 8 * int(out_offset)), out.shape[1],
+        max_keys.ptr() if max_keys is not None else None,
+        ctypes.c_void_p(err.data_ptr() + 4 * int(out_offset)), bound_keys.ptr(),
+        ctypes.c_void_p(cand.data_ptr()), int(cand_ld), int(chunk), stream_handle(stream)),
+        "joker_lnl_fused")
+    return out
+
+
+def accept_fused(stars, cache, lnl_buf, err, bound_keys, cand, cand_ld, segments, out_idx=None,
+                 out_lnl=None, counts=None, exact=None, stream=None):
+    """Second stage of the fused pass (joker_accept_fused): the FP64 maxima
+    among the candidates and their decisions; segment s reads its bits from
+    row s of ``cand``.  Returns (out_idx, out_lnl, counts, exact_max_keys,
+    n_refined) as accept_refined does."""
+    ns = len(segments)
+    arr, total_out = _segments(segments, "pcg64")
+    n_slots = max(int(sg.get("max_slot", 0)) for sg in segments) + 1
+    dev = lnl_buf.device
+    if out_idx is None:
+        out_idx = torch.empty(max(total_out, 1), dtype=torch.int64, device=dev)
+    if counts is None:
+        counts = torch.empty(ns, dtype=torch.int64, device=dev)
+    if exact is None:
+        exact = MaxKeys(n_slots)
+    n_ref = torch.zeros(1, dtype=torch.int64, device=dev)
+    wbytes = nat.lib().joker_accept_workspace(arr, ns)
+    work = torch.empty(max(int(wbytes), 1), dtype=torch.uint8, device=dev)
+    nat.check(nat.lib().joker_accept_fused(
+        stars.handle, cache.handle, arr, ns, ctypes.c_void_p(lnl_buf.data_ptr()),
+        ctypes.c_void_p(err.data_ptr()), bound_keys.ptr(), exact.ptr(), n_slots,
+        ctypes.c_void_p(cand.data_ptr()), int(cand_ld), ctypes.c_void_p(out_idx.data_ptr()),
+        ctypes.c_void_p(out_lnl.data_ptr()) if out_lnl is not None else None,
+        ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(n_ref.data_ptr()),
+        ctypes.c_void_p(work.data_ptr()), int(wbytes), stream_handle(stream)),
+        "joker_accept_fused")
+    if stream is not None:
+        work.record_stream(stream)
+    return out_idx, out_lnl, counts, exact, n_ref
+
+
 def accept(lnl_buf, max_keys, segments, u_source="pcg64", u=None, out_idx=None, out_lnl=None,
            counts=None, stream=None):
     """Run the acceptance pass (joker_accept) over ``segments``.

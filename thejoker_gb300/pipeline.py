@@ -55,6 +55,12 @@ class HostRejection:
             if mixed else None
         self.keys = dev.MaxKeys(n)
         self.bkeys = dev.MaxKeys(2 * n) if mixed else None
+        # "mixed_fast": the first acceptance pass fused into the ln L kernel
+        # (slices must then start on multiples of 32 samples)
+        self.fused = dev.fused_available(table, precision) and self.slice_rows % 32 == 0
+        if self.fused:
+            self.cand_ld, self.cand = dev.cand_words(n, self.capacity)
+            self.chunk = min(self.chunk, 8192)
         self.out_idx = torch.empty(n * self.max_out, dtype=torch.int64, device="cuda")
         self.counts = torch.empty(n, dtype=torch.int64, device="cuda")
         self.copy_stream = torch.cuda.Stream()
@@ -65,7 +71,17 @@ class HostRejection:
         self.host_counts = torch.empty(n, dtype=torch.int64).pin_memory()
         self.d2h_bytes = 0
 
-    def _staged(self, host_chunk, S, ks):
+    def _lnl(self, cache, row0, count, pcg, ks):
+        if self.fused:
+            dev.lnl_fused(self.table, cache, self.lnl, self.err, self.bkeys, pcg, self.cand,
+                          self.cand_ld, row0=row0, count=count, first=row0,
+                          max_keys=self.keys, chunk=self.chunk, out_offset=row0, stream=ks)
+        else:
+            dev.lnl(self.table, cache, self.lnl, precision=self.precision, row0=row0,
+                    count=count, max_keys=self.keys, err=self.err, bound_keys=self.bkeys,
+                    out_offset=row0, chunk=self.chunk, stream=ks)
+
+    def _staged(self, host_chunk, S, ks, pcg):
         cs = self.copy_stream
         n_slices = (S + self.slice_rows - 1) // self.slice_rows
         for k in range(n_slices):
@@ -81,9 +97,7 @@ class HostRejection:
                 ks.wait_event(self.copied[k % 2])
                 self.cache.load(buf[: b - a], row0=a, stream=ks)
                 self.freed[k % 2].record(ks)
-                dev.lnl(self.table, self.cache, self.lnl, precision=self.precision, row0=a,
-                        count=b - a, max_keys=self.keys, err=self.err, bound_keys=self.bkeys,
-                        out_offset=a, chunk=self.chunk, stream=ks)
+                self._lnl(self.cache, a, b - a, pcg, ks)
         return self.cache
 
     def run(self, host_chunk, pcg_states):
@@ -105,15 +119,17 @@ class HostRejection:
             self.keys.t.zero_()
             if self.bkeys is not None:
                 self.bkeys.t.zero_()
+        n = self.table.n_stars
+        pcg = None
+        if self.fused:
+            with torch.cuda.stream(ks):
+                pcg = dev.pcg_table([pcg_states[s] for s in range(n)])
         if self.zero_copy:
             cache = dev.PriorCache.view(host_chunk.contiguous())
             with torch.cuda.stream(ks):
-                dev.lnl(self.table, cache, self.lnl, precision=self.precision, row0=0, count=S,
-                        max_keys=self.keys, err=self.err, bound_keys=self.bkeys,
-                        chunk=self.chunk, stream=ks)
+                self._lnl(cache, 0, S, pcg, ks)
         else:
-            cache = self._staged(host_chunk, S, ks)
-        n = self.table.n_stars
+            cache = self._staged(host_chunk, S, ks, pcg)
         segs = []
         for s in range(n):
             st, inc = pcg_states[s]
@@ -124,6 +140,10 @@ class HostRejection:
             if self.err is None:
                 dev.accept(self.lnl.view(-1), self.keys, segs, out_idx=self.out_idx,
                            counts=self.counts, stream=ks)
+            elif self.fused:
+                dev.accept_fused(self.table, cache, self.lnl.view(-1), self.err.view(-1),
+                                 self.bkeys, self.cand, self.cand_ld, segs,
+                                 out_idx=self.out_idx, counts=self.counts, stream=ks)
             else:
                 dev.accept_refined(self.table, cache, self.lnl.view(-1), self.err.view(-1),
                                    self.bkeys, segs, out_idx=self.out_idx, counts=self.counts,
