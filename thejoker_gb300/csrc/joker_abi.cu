@@ -200,6 +200,9 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
     r.maxK2 = kp[3] * kp[3];
     r.log_kscale = r.k_scaled ? std::log(r.sigK0sq) + 2.0 / 3.0 * std::log(r.P0) : 0.0;
     r.log_maxK2 = r.k_scaled ? std::log(r.maxK2) : 0.0;
+    r.log_kscale_f = (float)r.log_kscale;
+    r.log_maxK2_f = (float)r.log_maxK2;
+    r.log_lam0_f = (float)std::log(r.lam0);
     for (int j = 0; j < L; ++j) r.lam[j] = lamk[j];
     for (int j = 0; j < L; ++j)
         r.ilam[j] = lamk[j] > 0.0 ? (double)(1.0L / (long double)lamk[j]) : 0.0;

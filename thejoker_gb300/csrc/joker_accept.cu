@@ -180,59 +180,8 @@ __device__ __forceinline__ bool below_lower_bound(const AcceptArgs &a, const jok
     return v + (double)er < key_to_double(a.bound_key[2 * sg.max_slot + 1]);
 }
 
-// FP64 re-evaluation of the listed samples, one warp per sample (lanes over
-// epochs).  MODE 0 raises the FP64 maximum; MODE 1 decides the undecided
-// samples against it and their own uniforms; MODE 2 (the band refinement)
-// only writes the FP64 value back.
-template <int MODE>
-__global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
-    const int lane = threadIdx.x & 31;
-    const int64_t n = min((int64_t)a.flag_count[MODE == 1 ? 1 : 0], a.flag_cap);   // MODE 2 uses list 0
-    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t e = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); e < n;
-         e += nw) {
-        const int64_t ent = a.flag_list[e];
-        const int si = (int)(ent >> 40);
-        const int64_t i = ent & (((int64_t)1 << 40) - 1);
-        const joker_accept_seg sg = a.segs[si];
-        if (MODE == 0 && below_lower_bound(a, sg, i)) continue;     // uniform in the warp
-        const int64_t r = (sg.row0 + i) * a.stride;
-        const double v = fp64_lnl_warp(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
-                                       a.OM[r], a.M0[r], a.S[r]);
-        if (lane != 0) continue;
-        if (a.n_refined) atomicAdd(a.n_refined, 1ull);
-        if (MODE == 0) {
-            atomicMax(a.exact_key + sg.max_slot, double_to_key(v));
-            if (a.write_max) {
-                const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
-                const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
-            }
-        } else if (MODE == 2) {
-            const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
-            const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
-        } else {
-            const double mx = key_to_double(a.exact_key[sg.max_slot]);
-            double u;
-            if (a.u_source == JOKER_U_PCG64) {
-                const u128 s0 = ((u128)sg.pcg_state_hi << 64) | (u128)sg.pcg_state_lo;
-                const u128 inc = ((u128)sg.pcg_inc_hi << 64) | (u128)sg.pcg_inc_lo;
-                u = pcg_uniform(pcg_output(pcg_jump(s0, inc, (uint64_t)i + 1)));
-            } else {
-                u = a.u[sg.u_off + i];
-            }
-            // the FP64 value replaces the mixed one (exact, so its bound is 0)
-            const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
-            const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
-            if (accept_test(v - mx, u)) {
-                const int64_t gblk = seg_base(a, si) + i / ACC_BLOCK;
-                atomicOr(a.words + gblk * ACC_THREADS + (i % ACC_BLOCK) / 32, 1u << (i & 31));
-                atomicAdd((unsigned long long *)(a.blk_count + gblk), 1ull);
-            }
-        }
-    }
-}
-
-// FP64 work on the samples flagged in amb_words.  One thread covers
+// FP64 work on the samples flagged in amb_words (the lists' overflow).  One
+// thread covers
 // WORDS_PER_THREAD consecutive words (all inside one 256-word CTA block);
 // almost all words are zero.  MODE 0 raises the FP64 maximum; MODE 1 decides
 // the undecided samples against it and their own uniforms; MODE 2 writes the
@@ -240,7 +189,7 @@ __global__ void __launch_bounds__(256) accept_fp64_list_kernel(AcceptArgs a) {
 constexpr int WORDS_PER_THREAD = 16;
 
 template <int MODE>
-__global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, int64_t n_words) {
+__device__ __noinline__ void fp64_words_phase(const AcceptArgs &a, int64_t n_words) {
     if (a.total_blocks_dev) n_words = n_blocks(a) * ACC_THREADS;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
          t * WORDS_PER_THREAD < n_words; t += (int64_t)gridDim.x * blockDim.x) {
@@ -311,6 +260,62 @@ __global__ void __launch_bounds__(128) accept_fp64_words_kernel(AcceptArgs a, in
         }
     }
     }
+}
+
+// FP64 re-evaluation of the listed samples, one warp per sample (lanes over
+// epochs), then (scan_words) of the samples flagged in amb_words past the
+// list's capacity.  MODE 0 raises the FP64 maximum; MODE 1 decides the
+// undecided samples against it and their own uniforms; MODE 2 (the band
+// refinement) only writes the FP64 value back.  n_words: words of amb_words
+// (read from the device count when the pass has one).
+template <int MODE>
+__global__ void __launch_bounds__(256, 2) accept_fp64_list_kernel(AcceptArgs a, int64_t n_words,
+                                                                    int scan_words) {
+    const int lane = threadIdx.x & 31;
+    const int64_t n = min((int64_t)a.flag_count[MODE == 1 ? 1 : 0], a.flag_cap);   // MODE 2 uses list 0
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t e = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); e < n;
+         e += nw) {
+        const int64_t ent = a.flag_list[e];
+        const int si = (int)(ent >> 40);
+        const int64_t i = ent & (((int64_t)1 << 40) - 1);
+        const joker_accept_seg sg = a.segs[si];
+        if (MODE == 0 && below_lower_bound(a, sg, i)) continue;     // uniform in the warp
+        const int64_t r = (sg.row0 + i) * a.stride;
+        const double v = fp64_lnl_warp(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
+                                       a.OM[r], a.M0[r], a.S[r]);
+        if (lane != 0) continue;
+        if (a.n_refined) atomicAdd(a.n_refined, 1ull);
+        if (MODE == 0) {
+            atomicMax(a.exact_key + sg.max_slot, double_to_key(v));
+            if (a.write_max) {
+                const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
+                const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
+            }
+        } else if (MODE == 2) {
+            const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
+            const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
+        } else {
+            const double mx = key_to_double(a.exact_key[sg.max_slot]);
+            double u;
+            if (a.u_source == JOKER_U_PCG64) {
+                const u128 s0 = ((u128)sg.pcg_state_hi << 64) | (u128)sg.pcg_state_lo;
+                const u128 inc = ((u128)sg.pcg_inc_hi << 64) | (u128)sg.pcg_inc_lo;
+                u = pcg_uniform(pcg_output(pcg_jump(s0, inc, (uint64_t)i + 1)));
+            } else {
+                u = a.u[sg.u_off + i];
+            }
+            // the FP64 value replaces the mixed one (exact, so its bound is 0)
+            const_cast<double *>(a.lnl)[sg.lnl_off + i] = v;
+            const_cast<float *>(a.err)[sg.lnl_off + i] = 0.0f;
+            if (accept_test(v - mx, u)) {
+                const int64_t gblk = seg_base(a, si) + i / ACC_BLOCK;
+                atomicOr(a.words + gblk * ACC_THREADS + (i % ACC_BLOCK) / 32, 1u << (i & 31));
+                atomicAdd((unsigned long long *)(a.blk_count + gblk), 1ull);
+            }
+        }
+    }
+    if (scan_words) fp64_words_phase<MODE>(a, n_words);
 }
 
 // The band refinement's scan: flags every sample whose mixed interval reaches
@@ -737,21 +742,13 @@ cudaError_t accept_preload() {
 
 static cudaError_t launch_fp64_words(int mode, const AcceptArgs &a, int64_t total_blocks,
                                      cudaStream_t st) {
-    // the compacted list first (one warp per sample), then the words of the
-    // samples that did not fit in it (almost always none)
-    const unsigned lgrid = 152 * 4;
-    if (mode == 0) accept_fp64_list_kernel<0><<<lgrid, 256, 0, st>>>(a);
-    else if (mode == 1) accept_fp64_list_kernel<1><<<lgrid, 256, 0, st>>>(a);
-    else accept_fp64_list_kernel<2><<<lgrid, 256, 0, st>>>(a);
-    count_launch();
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    // the compacted list (one warp per sample), then the words of the samples
+    // that did not fit in it (almost always none), in one launch
+    const unsigned grid = 152 * 4;
     const int64_t n_words = total_blocks * ACC_THREADS;
-    const int64_t threads = (n_words + WORDS_PER_THREAD - 1) / WORDS_PER_THREAD;
-    const unsigned grid = (unsigned)((threads + 127) / 128);
-    if (mode == 0) accept_fp64_words_kernel<0><<<grid, 128, 0, st>>>(a, n_words);
-    else if (mode == 1) accept_fp64_words_kernel<1><<<grid, 128, 0, st>>>(a, n_words);
-    else accept_fp64_words_kernel<2><<<grid, 128, 0, st>>>(a, n_words);
+    if (mode == 0) accept_fp64_list_kernel<0><<<grid, 256, 0, st>>>(a, n_words, 1);
+    else if (mode == 1) accept_fp64_list_kernel<1><<<grid, 256, 0, st>>>(a, n_words, 1);
+    else accept_fp64_list_kernel<2><<<grid, 256, 0, st>>>(a, n_words, 1);
     count_launch();
     return cudaGetLastError();
 }
@@ -850,7 +847,7 @@ static cudaError_t accept_finish(const AcceptArgs &a, int64_t total_blocks, cuda
         accept_emit_kernel<true><<<(unsigned)total_blocks, ACC_THREADS, 0, st>>>(a);
         count_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        accept_fp64_list_kernel<2><<<152 * 4, 256, 0, st>>>(a);
+        accept_fp64_list_kernel<2><<<152 * 4, 256, 0, st>>>(a, 0, 0);
         count_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }

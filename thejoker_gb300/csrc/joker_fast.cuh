@@ -29,7 +29,8 @@
 // |d log det G| <= |tr(G^-1 dG)| + 1.34 |G^-1 dG|_F^2.  The FP32 column's own
 // error (phase rounding, FP32 Kepler; the constant err_c0 is empirical)
 // enters as in the mixed kernel.  The tail runs in float-float; the only FP64
-// arithmetic per sample is the conversion of ln L to a double.
+// instruction per sample is the addition that rounds ln L's float pair to a
+// double (both halves converted by integer operations).
 #pragma once
 #include "joker_mixed.cuh"
 
@@ -143,9 +144,9 @@ __device__ __forceinline__ void fast_tail(const StarRec &st, const AccF<L, JIT, 
     constexpr int T = L - 1;
     static_assert(!JIT || L <= 3, "the FP32-sum path takes at most three linear parameters "
                                   "with the jitter applied");
-    float log_lam0f;
-    if (st.k_scaled) log_lam0f = fminf((float)st.log_maxK2, (float)st.log_kscale + lgP);
-    else log_lam0f = (float)log(st.lam0);
+    // (the float copies of the prior's logs: no FP64 conversion per sample)
+    const float log_lam0f =
+        st.k_scaled ? fminf(st.log_maxK2_f, st.log_kscale_f + lgP) : st.log_lam0_f;
     const float ilam0 = expf(-log_lam0f);
     const float mu = st.mu0_f, amu = fabsf(mu);
     // gamma: sequential FP32 sums of N terms; per term the FP32 weight (4
@@ -344,6 +345,34 @@ __device__ __forceinline__ unsigned long long float_to_dkey(float x) {
     return key_of_bits((long long)d);
 }
 
+// The double equal to a float, from the float's bits (integer operations:
+// the conversion instruction would occupy the FP64 pipe, 1/64 of the FP32
+// rate on this GPU).  Zero, subnormal, infinite and NaN inputs convert as
+// usual.
+__device__ __forceinline__ double f2d_exact(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned ex = (b >> 23) & 0xffu;
+    if (ex - 1u < 254u)
+        return __longlong_as_double((long long)(((unsigned long long)(b & 0x80000000u) << 32) |
+                                                ((unsigned long long)(ex + 896u) << 52) |
+                                                ((unsigned long long)(b & 0x7fffffu) << 29)));
+    if ((b & 0x7fffffffu) == 0u)
+        return __longlong_as_double((long long)((unsigned long long)b << 32));   // +-0
+    return (double)x;
+}
+
+// A key's double rounded down to a float: the bit pattern directly when the
+// double is a normal float (bound keys are written from floats), else the
+// FP64 conversion.
+__device__ __forceinline__ float key_to_float_rd(unsigned long long k) {
+    const unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    const unsigned ex = (unsigned)(b >> 52) & 0x7ffu;
+    if ((b & 0x1FFFFFFFull) == 0ull && ex >= 897u && ex <= 1150u)
+        return __uint_as_float(((unsigned)(b >> 32) & 0x80000000u) | ((ex - 896u) << 23) |
+                               ((unsigned)(b >> 29) & 0x7fffffu));
+    return __double2float_rd(__longlong_as_double((long long)b));
+}
+
 __device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -369,12 +398,12 @@ __device__ __forceinline__ unsigned long long fast_store2(const LnlArgs &a, int6
                                                           unsigned long long *bk) {
     double d0 = 0.0, d1 = 0.0;
     if (act0) {
-        d0 = (double)l0.hi + (double)l0.lo;
+        d0 = f2d_exact(l0.hi) + f2d_exact(l0.lo);
         a.lnl[out0] = d0;
         if (a.err) a.err[out0] = e0;
     }
     if (act1) {
-        d1 = (double)l1.hi + (double)l1.lo;
+        d1 = f2d_exact(l1.hi) + f2d_exact(l1.lo);
         a.lnl[out1] = d1;
         if (a.err) a.err[out1] = e1;
     }
@@ -464,7 +493,7 @@ __device__ __forceinline__ void fused_pass(const LnlArgs &a, const WorkItem &w, 
         const unsigned long long gk = *((volatile const unsigned long long *)(bk + 1));
         const unsigned long long lk = gk > kd ? gk : kd;
         const bool lb_ok = lk != 0ull && lk != 0xFFFFFFFFFFFFFFFFull;   // a bound, not NaN
-        const float lbf = lb_ok ? __double2float_rd(key_to_double(lk)) : 0.0f;
+        const float lbf = lb_ok ? key_to_float_rd(lk) : 0.0f;
         float x0, x1;
         int c0 = fused_pretest(act0, l0, e0, lb_ok, lbf, x0);
         int c1 = fused_pretest(act1, l1, e1, lb_ok, lbf, x1);

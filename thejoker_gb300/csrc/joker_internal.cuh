@@ -60,6 +60,9 @@ struct alignas(16) StarRec {
     float Cn;                          // sum ivar r_c^2, rounded up
     float ivar_max;                    // max ivar, rounded up
     float Wjj[MAXL];                   // sum ivar T_j^2 (j >= 1), rounded up
+    float log_kscale_f, log_maxK2_f;   // log_kscale, log_maxK2 rounded to float
+    float log_lam0_f;                  // log lam0 rounded to float
+    float pad3;
 };
 
 // One unit of the persistent likelihood kernels: `count` samples of star
