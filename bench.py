@@ -112,7 +112,7 @@ KERNEL_NAME = {"mixed": "lnl_mixed2_kernel<L=2, jitter, VAR 0, cache form> (two 
 # candidate mask) and the DRAM bytes ncu measured per sample (read + write of
 # one 2^24-sample launch / 2^24), scaled to a launch.
 BYTES_PER_SAMPLE = 48.125
-DRAM_BYTES_PER_SAMPLE = 46.79
+DRAM_BYTES_PER_SAMPLE = 46.90
 
 
 def _hbm_peak():

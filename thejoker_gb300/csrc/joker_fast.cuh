@@ -229,16 +229,34 @@ __device__ __forceinline__ void fast_tail(const StarRec &st, const AccF<L, JIT, 
     }
     const float aK = dD + amu * dF;
     const float dC = (JIT ? gam * A.C : 0.0f) + 2.0f * amu * dD + mu * mu * dF;
+    // The second-order terms are taken in the frame scaled by D = diag(d_i),
+    // d_i^2 ~ G_ii (any positive diagonal is valid; this one makes the
+    // terms independent of the columns' units, e.g. a (t - t_ref)^2 trend
+    // column in days^2): with G~ = D^-1 G D^-1, dG~ = D^-1 dG D^-1 and
+    // r~ = D^-1 (dq' - dG theta), (dq' - dG theta)^T (G + dG)^-1 (...) =
+    // r~^T (G~ + dG~)^-1 r~ <= 2 tr(G~^-1) |r~|^2 while |dG~|_F tr(G~^-1) <= 1/2,
+    // and G^-1 dG is similar to G~^-1 dG~, whose Frobenius norm is at most
+    // |dG~|_F tr(G~^-1).  Each entry of dG~ is at most gam.
+    // (hardware reciprocals of the scales: their 2^-23 relative error is
+    // inside the bound's 1 % evaluation allowance)
+    const float dK2 = F + ilam0, idK2 = fast_rcp(dK2);
+    float dT2[MAXL], idT2[MAXL];
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        dT2[j] = fmaxf(Gjj[j] + st.ilam_hi[j + 1], 1e-30f);   // H_jj
+        idT2[j] = fast_rcp(dT2[j]);
+    }
     // first order: dC + 2 |theta|.|dq'| + |theta|^T |dG| |theta|
     float d1 = dC + 2.0f * Kh * aK + Kh * Kh * dF;
-    float eK = aK + Kh * dF, dGf2 = dF * dF;
+    float eK = aK + Kh * dF;
+    float dGs2 = (dF * idK2) * (dF * idK2);           // |dG~|_F^2
     float eT[MAXL];
 #pragma unroll
     for (int j = 0; j < T; ++j) {
         d1 += 2.0f * th[j] * (aT[j] + Kh * dg[j]);
         eK += th[j] * dg[j];
         eT[j] = aT[j] + Kh * dg[j];
-        dGf2 += 2.0f * dg[j] * dg[j];
+        dGs2 += 2.0f * (dg[j] * dg[j]) * (idK2 * idT2[j]);
     }
     if constexpr (JIT) {
 #pragma unroll
@@ -248,18 +266,19 @@ __device__ __forceinline__ void fast_tail(const StarRec &st, const AccF<L, JIT, 
                 const float dG = gam * sqrtf(Gjj[j] * Gjj[k]);
                 d1 += th[j] * th[k] * dG;
                 eT[j] += dG * th[k];
-                dGf2 += dG * dG;
+                dGs2 += (dG * dG) * (idT2[j] * idT2[k]);
             }
     }
-    // second order: 2 tr(G^-1) |dq' - dG theta|^2, valid while |dG|_F tr(G^-1) < 1/4
-    const float iS = 1.0f / sf;
-    float trGi = iS;
+    // second order: 2 tr(G~^-1) |r~|^2, valid while |dG~|_F tr(G~^-1) < 1/4;
+    // (G^-1)_KK = 1/s and (G^-1)_jj = (H^-1)_jj + v_j^2 / s
+    const float iS = fast_rcp(sf);
+    float trGi = iS * dK2;
 #pragma unroll
-    for (int j = 0; j < T; ++j) trGi += Hi[j][j].hi + v[j].hi * v[j].hi * iS;
-    float ee = eK * eK;
+    for (int j = 0; j < T; ++j) trGi += (Hi[j][j].hi + v[j].hi * v[j].hi * iS) * dT2[j];
+    float ee = eK * eK * idK2;
 #pragma unroll
-    for (int j = 0; j < T; ++j) ee += eT[j] * eT[j];
-    const float xf = sqrtf(dGf2) * trGi;
+    for (int j = 0; j < T; ++j) ee += eT[j] * eT[j] * idT2[j];
+    const float xf = sqrtf(dGs2) * trGi;
     bool ok = xf < 0.25f;
     d1 += 2.0f * trGi * ee;
     // log det G: |tr(G^-1 dG)| + 1.34 |G^-1 dG|_F^2
