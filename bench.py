@@ -13,7 +13,11 @@ resident in HBM.  ``e2e``: the same through the host-facing call -- the packed
 (S, 5) float64 chunk in pinned host memory, read by the ln L kernel over the
 host link (40 bytes per sample, no staging copy), evaluated and accepted,
 accepted indices copied back -- every step.  The plain FP64 GPU path is
-reported beside it (``fp64``) on a 2^25-sample slice of the same workload.
+reported beside it (``fp64``) on a 2^25-sample slice of the same workload,
+with ``parity`` against it on that slice.  At N = 1 the line also carries one
+pass of the other configurations: ``batched`` (4096 stars over one 2^24
+cache), ``iterative`` (1024 stars, quadratic trend, graph rounds) and
+``serving`` (a Poisson request stream, p50/p99), each beside the FP64 path.
 
 Multi-GPU (torchrun): each rank evaluates its own 2^28-sample shard of the
 cache for the same star (weak scaling); the per-star maximum is exchanged with
@@ -417,6 +421,10 @@ def run_ours(args, rank, world, dist):
         line["batched"] = batched_measure(4096, 1 << 24, warmup=1, steps=1, subset_stars=64,
                                           subset_samples=1 << 22)
         torch.cuda.empty_cache()
+        torch.cuda.empty_cache()
+        line["iterative"] = iterative_measure(1024, 1 << 22, 256, steps=1, warmup=1,
+                                              subset_stars=64, eager=False)
+        torch.cuda.empty_cache()
         line["serving"] = serving_measure(1 << 28, rates=[500.0], window=4.0, n_all=2000,
                                           slots=1024, round_budget=1 << 26, fp64_requests=64)
     return line
@@ -575,20 +583,18 @@ def run_batched(args, rank, world):
     }
 
 
-def run_iterative(args, rank, world):
-    """Iterative rejection of 1024 stars with a quadratic trend (poly_trend=3:
-    K, v0, v1, v2 with N(0, [100 km/s, 1 km/s/d, 0.01 km/s/d^2]) priors), 8-64
-    epochs each, n_requested = 256, over a 2^22-sample prior library; every
-    round on the device, rounds after the first replayed from a CUDA graph.
-    The plain FP64 path runs the same schedule on a 64-star subset."""
+def iterative_measure(n_stars, S, n_req, steps=1, warmup=1, subset_stars=64, rank=0, world=1,
+                      eager=True):
+    """Iterative rejection of ``n_stars`` stars with a quadratic trend
+    (poly_trend=3: K, v0, v1, v2 with N(0, [100 km/s, 1 km/s/d, 0.01 km/s/d^2])
+    priors), 8-64 epochs each, ``n_req`` samples requested, over an S-sample
+    prior library; every round on the device, rounds after the first replayed
+    from a CUDA graph.  The plain FP64 path runs the same schedule on a star
+    subset."""
     import torch
-    from thejoker_gb300 import build as tb
     from thejoker_gb300 import device as dev
     from thejoker_gb300.iterative import IterativeBatch
     from thejoker_gb300.synthetic import fill_prior_cache, survey_stars
-    tb.build()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-    n_stars, S, n_req = args.stars, args.samples, args.n_requested
     stars = survey_stars(n_stars * world, seed=4, n_min=8, n_max=64,
                          poly_trend=3)[rank * n_stars:(rank + 1) * n_stars]
     host = np.empty((S, 5))
@@ -598,20 +604,21 @@ def run_iterative(args, rank, world):
     seeds = lambda k: np.arange(n_stars) + 7919 * k + rank * n_stars
     it = IterativeBatch(table, cache, n_req, precision=MIXED, seeds=seeds(0))
     it.run()
-    for w in range(args.warmup):
+    for w in range(warmup):
         it.reset(seeds(w + 1)).run()
     torch.cuda.synchronize()
     evals, rounds = [], []
     with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
         t0 = time.perf_counter()
-        for k in range(args.steps):
+        for k in range(steps):
             it.reset(seeds(100 + k)).run()
             st, _, _ = it.results()
             evals.append(int(st[:, 2].sum()))
             rounds.append(int(st[:, 5].max()))
-        ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    # eager rounds (no graph) and the FP64 path on a subset, same schedule
-    sub = min(args.subset_stars, n_stars)
+        ms = (time.perf_counter() - t0) * 1e3 / steps
+    it.close()
+    # the FP64 path on a subset, same schedule
+    sub = min(subset_stars, n_stars)
     table_sub = dev.StarTable(stars[:sub])
     res = {}
     for key, prec in (("mixed", MIXED), ("fp64", "fp64")):
@@ -627,24 +634,23 @@ def run_iterative(args, rank, world):
         b.close()
     same = bool(np.array_equal(res["mixed"][1], res["fp64"][1]) and
                 all(np.array_equal(a, b) for a, b in zip(res["mixed"][2], res["fp64"][2])))
-    eager = IterativeBatch(table, cache, n_req, precision=MIXED, seeds=seeds(100))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    eager.run(use_graph=False)
-    eager_ms = (time.perf_counter() - t0) * 1e3
-    eager.close()
+    eager_ms = None
+    if eager:
+        e = IterativeBatch(table, cache, n_req, precision=MIXED, seeds=seeds(100))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e.run(use_graph=False)
+        eager_ms = (time.perf_counter() - t0) * 1e3
+        e.close()
     n_ep = np.array([len(s["t"]) for s in stars])
     ev = float(np.mean(evals))
     return {
-        "metric": "prior samples/s (lnL+accept), iterative",
-        "value": ev * world / (ms * 1e-3), "unit": "samples/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded survey, numpy prior library)",
-        "config": {"workload": f"{n_stars} stars, poly_trend=3, epochs log-uniform [8,64] "
-                               f"(mean {n_ep.mean():.1f}), n_requested={n_req}, prior library "
-                               f"2^{int(math.log2(S))}, rounds replayed from a CUDA graph",
-                   "stars_per_gpu": n_stars, "library": S, "n_requested": n_req},
+        "value": ev * world / (ms * 1e-3), "unit": "samples/s", "ms_per_step": ms,
+        "steps": steps, "warmup": warmup,
+        "workload": f"{n_stars} stars, poly_trend=3, epochs log-uniform [8,64] "
+                    f"(mean {n_ep.mean():.1f}), n_requested={n_req}, prior library "
+                    f"2^{int(math.log2(S))}, rounds replayed from a CUDA graph",
+        "stars_per_gpu": n_stars, "library": S, "n_requested": n_req,
         "stars_per_s": n_stars * world / (ms * 1e-3),
         "samples_evaluated_per_step": ev, "rounds_per_step": float(np.mean(rounds)),
         "eager_rounds_ms": eager_ms,
@@ -652,6 +658,31 @@ def run_iterative(args, rank, world):
                    "speedup_mixed_vs_fp64": res["fp64"][0] / res["mixed"][0],
                    "results_identical": same},
         "clocks": clk.summary(),
+    }
+
+
+def run_iterative(args, rank, world):
+    """The iterative configuration as its own bench line (iterative_measure)."""
+    import torch
+    from thejoker_gb300 import build as tb
+    tb.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    r = iterative_measure(args.stars, args.samples, args.n_requested, steps=args.steps,
+                          warmup=args.warmup, subset_stars=args.subset_stars, rank=rank,
+                          world=world)
+    return {
+        "metric": "prior samples/s (lnL+accept), iterative",
+        "value": r["value"], "unit": "samples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded survey, numpy prior library)",
+        "config": {"workload": r["workload"], "stars_per_gpu": r["stars_per_gpu"],
+                   "library": r["library"], "n_requested": r["n_requested"]},
+        "stars_per_s": r["stars_per_s"],
+        "samples_evaluated_per_step": r["samples_evaluated_per_step"],
+        "rounds_per_step": r["rounds_per_step"], "eager_rounds_ms": r["eager_rounds_ms"],
+        "subset": r["subset"], "clocks": r["clocks"],
     }
 
 

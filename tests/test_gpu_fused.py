@@ -186,3 +186,41 @@ def test_fused_arguments_rejected(cuda):
     with pytest.raises(JokerError):
         dev.lnl_fused(big, cache, lnl, err, bk, pcg, cand, ld)
     assert nat.lib().joker_last_error()
+
+
+@pytest.mark.parametrize("S", [1, 31, 33, 257])
+def test_fused_tiny_and_ragged(cuda, S):
+    """Caches of 1, 31, 33 and 257 samples: a partial first word, a work item
+    shorter than one pass, and a second pass with a single active sample."""
+    from thejoker_gb300 import device as dev
+    rng = np.random.default_rng(S)
+    stars = [synth_star(rng, 3, K=0.5), synth_star(rng, 12, K=5.0)]
+    cache = dev.PriorCache.from_samples(synth_chunk(rng, S, jitter=True))
+    table = dev.StarTable(stars, jitter="applied")
+    r64 = _engine(table, cache, "fp64", [5, 6], S).results()
+    rf = _engine(table, cache, "mixed_fast", [5, 6], S, chunk=128).results()
+    _same(r64, rf, 2)
+
+
+def test_fused_nan_rows_and_max_out_one(cuda):
+    """Rows with e >= 1 give NaN ln L, and a NaN maximum keeps nothing (numpy's
+    exp(lls - nan) > u is False), in both paths; with max_out = 1 the counts
+    are still those of every kept sample."""
+    from thejoker_gb300 import device as dev
+    rng = np.random.default_rng(77)
+    stars = [synth_star(rng, 6, K=1.0), synth_star(rng, 9, K=1.0)]
+    S = 5000
+    ch = synth_chunk(rng, S)
+    cache_ok = dev.PriorCache.from_samples(ch)
+    table = dev.StarTable(stars)
+    r64 = _engine(table, cache_ok, "fp64", [1, 2], 1).results()
+    rf = _engine(table, cache_ok, "mixed_fast", [1, 2], 1).results()
+    _same(r64, rf, 2)
+    assert r64[0].min() > 1 and all(len(x) == 1 for x in rf[1])
+    ch_bad = ch.copy()
+    ch_bad[1234, 1] = 1.5                                 # e >= 1: NaN ln L
+    cache_bad = dev.PriorCache.from_samples(ch_bad)
+    c64 = _engine(table, cache_bad, "fp64", [1, 2], S).results()[0]
+    cf = _engine(table, cache_bad, "mixed_fast", [1, 2], S).results()[0]
+    np.testing.assert_array_equal(cf, c64)
+    assert c64.sum() == 0

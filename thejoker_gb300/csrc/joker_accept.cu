@@ -227,10 +227,12 @@ __device__ __noinline__ void fp64_words_phase(const AcceptArgs &a, int64_t n_wor
             const int64_t i = first + b;
             if (i >= sg.n) continue;
             if (MODE == 0 && below_lower_bound(a, sg, i)) continue;
+            const bool exact = a.err[sg.lnl_off + i] == 0.0f;
             const int64_t r = (sg.row0 + i) * a.stride;
-            const double v = fp64_lnl_sample(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
-                                             a.OM[r], a.M0[r], a.S[r]);
-            if (a.n_refined) atomicAdd(a.n_refined, 1ull);
+            const double v = exact ? a.lnl[sg.lnl_off + i]
+                                   : fp64_lnl_sample(a.L, a.jit, a.stars[sg.star], a.ep64,
+                                                     a.P[r], a.E[r], a.OM[r], a.M0[r], a.S[r]);
+            if (a.n_refined && !exact) atomicAdd(a.n_refined, 1ull);
             if (MODE == 0) {
                 atomicMax(a.exact_key + sg.max_slot, double_to_key(v));
                 if (a.write_max) {
@@ -281,11 +283,14 @@ __global__ void __launch_bounds__(256, 2) accept_fp64_list_kernel(AcceptArgs a, 
         const int64_t i = ent & (((int64_t)1 << 40) - 1);
         const joker_accept_seg sg = a.segs[si];
         if (MODE == 0 && below_lower_bound(a, sg, i)) continue;     // uniform in the warp
+        // a value an earlier refinement made exact (bound 0) is not evaluated again
+        const bool exact = a.err[sg.lnl_off + i] == 0.0f;
         const int64_t r = (sg.row0 + i) * a.stride;
-        const double v = fp64_lnl_warp(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r], a.E[r],
-                                       a.OM[r], a.M0[r], a.S[r]);
+        const double v = exact ? a.lnl[sg.lnl_off + i]
+                               : fp64_lnl_warp(a.L, a.jit, a.stars[sg.star], a.ep64, a.P[r],
+                                               a.E[r], a.OM[r], a.M0[r], a.S[r]);
         if (lane != 0) continue;
-        if (a.n_refined) atomicAdd(a.n_refined, 1ull);
+        if (a.n_refined && !exact) atomicAdd(a.n_refined, 1ull);
         if (MODE == 0) {
             atomicMax(a.exact_key + sg.max_slot, double_to_key(v));
             if (a.write_max) {

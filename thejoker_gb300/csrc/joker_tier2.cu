@@ -14,9 +14,10 @@
 
 namespace joker {
 
-// Entries whose bound is already at most this are left as they are (a
-// float-float or FP64 value would not tighten them usefully).
-constexpr float TIER2_MIN_ERR = 1e-3f;
+// Entries whose bound is already at most this are left as they are (the
+// float-float bound is not smaller); entries without a bound (err >= 1e29,
+// the FP32-sum bound's validity test failed) are re-evaluated like the rest.
+constexpr float TIER2_MIN_ERR = 1e-6f;
 
 template <int L, bool JIT>
 __global__ void __launch_bounds__(128) tier2_kernel(AcceptArgs a) {
@@ -29,7 +30,7 @@ __global__ void __launch_bounds__(128) tier2_kernel(AcceptArgs a) {
         const joker_accept_seg sg = a.segs[si];
         const int64_t o = sg.lnl_off + i;
         const float er0 = a.err[o];
-        if (!(er0 > TIER2_MIN_ERR) || !(er0 < 1e29f)) continue;
+        if (!(er0 > TIER2_MIN_ERR)) continue;                // exact, tight, or NaN
         const int64_t r = (sg.row0 + i) * a.stride;
         float4 pa, pb;
         float s2;
