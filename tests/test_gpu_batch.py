@@ -93,10 +93,12 @@ def test_autotune_records_fastest_chunk(cuda, tmp_path):
     cache = dev.PriorCache.from_samples(fill_prior_cache(np.empty((1 << 18, 5)), 3))
     table = dev.StarTable(stars)
     path = str(tmp_path / "tune.json")
-    best, times = at.tune(table, cache, precision="mixed", candidates=(256, 1024, 4096), reps=1,
-                          path=path)
+    # the engines' default precision, whose tuning times the fused ln L kernel
+    best, times = at.tune(table, cache, precision="mixed_fast", candidates=(256, 1024, 4096),
+                          reps=1, path=path)
     assert best in (256, 1024, 4096) and times[best] == min(times.values())
-    assert at.chunk_for(table.n_linear, table.jitter, "mixed", table.n_epochs, path=path) == best
+    assert at.chunk_for(table.n_linear, table.jitter, "mixed_fast", table.n_epochs,
+                        path=path) == best
     # an engine built without a chunk picks the tuned size
     import os
     os.environ["JOKER_AUTOTUNE"] = path

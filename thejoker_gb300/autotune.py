@@ -83,7 +83,7 @@ def chunk_for(n_linear, jitter, precision, n_epochs, path=None):
     return int(entry["chunk"]) if entry else DEFAULT_CHUNK
 
 
-def tune(table, cache, precision="mixed", n_epochs=None, star0=0, n_sel=None, count=None,
+def tune(table, cache, precision="mixed_fast", n_epochs=None, star0=0, n_sel=None, count=None,
          candidates=CANDIDATE_CHUNKS, reps=3, path=None, write=True):
     """Time joker_lnl (joker_lnl_fused where "mixed_fast" runs the fused
     acceptance pass) over stars [star0, star0 + n_sel) x cache rows [0, count)

@@ -35,15 +35,16 @@ class BatchRejection:
     """Rejection sampling of ``stars`` (dicts as StarTable takes) against a
     PriorCache.
 
-    precision: "mixed" (default; acceptance refined to the FP64 decisions),
-    "mixed_fast" (the same decisions, with the first acceptance pass fused
-    into the ln L kernel) or "fp64".  group: stars per launch (bounded by device memory: 12 bytes per
+    precision: "mixed_fast" (default: FP32-sum ln L with the first acceptance
+    pass fused into its kernel, refined to the FP64 decisions), "mixed" (the
+    float-float kernel and separate acceptance scans, same decisions) or
+    "fp64".  group: stars per launch (bounded by device memory: 12 bytes per
     star and sample for the mixed path).  seeds: one seed per star for its
     numpy PCG64 generator (its first ``n`` uniforms are the star's ``uu``).
     chunk: samples per ln L work item (None: the autotuned size, autotune.py).
     """
 
-    def __init__(self, stars, cache, precision="mixed", jitter="reference", group=None,
+    def __init__(self, stars, cache, precision="mixed_fast", jitter="reference", group=None,
                  max_out=256, seeds=None, chunk=None, timing=False):
         self.table = stars if isinstance(stars, dev.StarTable) else dev.StarTable(stars,
                                                                                   jitter=jitter)

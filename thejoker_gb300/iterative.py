@@ -30,7 +30,7 @@ class IterativeBatch:
     the reference (defaults: growth_factor * n_requested, 128, 1, 128).
     """
 
-    def __init__(self, table, cache, n_requested, precision="mixed", lib_row0=0, lib_size=None,
+    def __init__(self, table, cache, n_requested, precision="mixed_fast", lib_row0=0, lib_size=None,
                  seeds=None, init_batch_size=None, growth_factor=128, safety_factor=1.0,
                  maxiter=128, chunk=None, round_budget=0):
         self.table, self.cache = table, cache

@@ -110,7 +110,7 @@ class ShardedRejection:
     count.
     """
 
-    def __init__(self, table, cache, row0, precision="mixed", max_out=1 << 20, group=None):
+    def __init__(self, table, cache, row0, precision="mixed_fast", max_out=1 << 20, group=None):
         from . import device as dev
         self.dev = dev
         self.table, self.cache, self.row0 = table, cache, int(row0)
@@ -166,7 +166,7 @@ class StarShardedRejection:
     star's results in star order on every rank (host objects, so any backend).
     """
 
-    def __init__(self, stars, cache, precision="mixed", jitter="reference", max_out=256,
+    def __init__(self, stars, cache, precision="mixed_fast", jitter="reference", max_out=256,
                  seeds=None, world=None, rank=None, group=None, chunk=None):
         import torch.distributed as dist
         from .batch import BatchRejection

@@ -32,7 +32,7 @@ class HostRejection:
     """Reusable buffers for rejection sampling of ``table``'s stars against
     host prior chunks of up to ``capacity`` rows."""
 
-    def __init__(self, table, capacity, precision="mixed", slice_rows=1 << 24, max_out=256,
+    def __init__(self, table, capacity, precision="mixed_fast", slice_rows=1 << 24, max_out=256,
                  zero_copy=True, chunk=None):
         self.table = table
         self.precision = precision

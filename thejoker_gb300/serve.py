@@ -91,7 +91,7 @@ class ServingEngine:
     not change."""
 
     def __init__(self, cache, n_slots=1024, max_epochs=256, n_linear=2, pool_samples=None,
-                 max_requested=512, precision="mixed", safety_factor=1.0, maxiter=128,
+                 max_requested=512, precision="mixed_fast", safety_factor=1.0, maxiter=128,
                  chunk=1024, use_graph=True, pool_fraction=0.5, round_budget=0):
         self.cache = cache
         self.n_slots = int(n_slots)
