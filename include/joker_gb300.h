@@ -477,7 +477,9 @@ int joker_rejection_sample(const joker_stars *stars, const joker_cache *cache, i
  * cudaDeviceReset of that device.
  * segs is copied to the device on `stream`: from pageable memory before the
  * call returns; from pinned memory later, so pinned segs must stay unchanged
- * until the stream has passed the call. */
+ * until the stream has passed the call.  Because every call copies from host
+ * memory (segs and a block table on the stack), no call may be captured
+ * into a CUDA graph. */
 #define JOKER_NOALLOC_MAX_SEGS 1024
 #define JOKER_NOALLOC_MAX_BLOCKS 2048
 int joker_accept_noalloc(const joker_accept_seg *segs, int n_segs, const double *d_lnl,
