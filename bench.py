@@ -131,35 +131,51 @@ def _hbm_peak():
 
 # ------------------------------------------------------------------- clocks
 class ClockSampler:
-    def __init__(self, gpu_index):
+    """SM clocks and throttle reasons sampled every 50 ms by one streaming
+    ``nvidia-smi -lms`` process while the block runs (read only; no setting
+    is changed)."""
+
+    def __init__(self, gpu_index, interval_ms=50):
         self.gpu = gpu_index
+        self.interval_ms = int(interval_ms)
         self.samples = []
-        self._stop = threading.Event()
+        self._proc = None
         self._th = None
 
-    def _run(self):
+    def _read(self):
+        for line in self._proc.stdout:
+            v = [x.strip() for x in line.strip().split(",")]
+            if len(v) >= 6:
+                self.samples.append(v)
+
+    def __enter__(self):
         q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
-                                      "--format=csv,noheader,nounits"], capture_output=True,
-                                     text=True, timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([v.strip() for v in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
-
-    def __enter__(self):
-        self._th = threading.Thread(target=self._run, daemon=True)
-        self._th.start()
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._th = threading.Thread(target=self._read, daemon=True)
+            self._th.start()
+            # let the stream start before the timed block
+            t_end = time.time() + 2.0
+            while not self.samples and time.time() < t_end:
+                time.sleep(0.02)
+            self.samples.clear()
+        except Exception:
+            self._proc = None
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._th.join(timeout=10)
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+            self._th.join(timeout=5)
 
     def summary(self):
         if not self.samples:
