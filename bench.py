@@ -293,9 +293,12 @@ def run_ours(args, rank, world, dist):
         barrier()
         launches = nat.lib().joker_launch_count() - launches0
     ms = t0.elapsed_time(t1) / args.steps
+    early = None
     if world == 1:
         lnl_ms.append(runner.lnl_ms())
         n_acc = int(runner.counts[0].item())
+        if MIXED == "mixed_fast":
+            early = early_exit_measure(runner, table, cache, S, args.steps, args.warmup)
     else:
         lnl_ms.append(float("nan"))
         n_acc = None
@@ -425,6 +428,8 @@ def run_ours(args, rank, world, dist):
         "clocks": clk.summary(),
         "parity": parity,
     }
+    if early is not None:
+        line["early_exit"] = early
     if not args.no_cpu:
         v, kind, cores, secs = cpu_baseline(star, args.cpu_samples)
         line["cpu_baseline"] = {"value": v, "unit": "samples/s", "cores": cores, "kind": kind,
@@ -444,6 +449,42 @@ def run_ours(args, rank, world, dist):
         line["serving"] = serving_measure(1 << 28, rates=[500.0], window=4.0, n_all=2000,
                                           slots=1024, round_budget=1 << 26, fp64_requests=64)
     return line
+
+
+def early_exit_measure(runner, table, cache, S, steps, warmup):
+    """The same step with the fused pass's early exit (not the headline): warps
+    whose samples the partial epoch sums put more than 746 nats below the
+    running lower bound stop evaluating epochs.  The kept rows and their ln L
+    must equal the full step's (``identical``)."""
+    import torch
+    from thejoker_gb300.batch import BatchRejection
+    c0, i0, l0 = runner.results()
+    ex = BatchRejection(table, cache, precision=MIXED, max_out=S, seeds=[1000], timing=True,
+                        early_exit=True)
+    for _ in range(max(1, warmup)):
+        ex.run()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        t0.record()
+        for _ in range(steps):
+            ex.run()
+        t1.record()
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / steps
+    c1, i1, l1 = ex.results()
+    stopped = float(torch.isinf(ex.err[0, :S]).float().mean().item())
+    same = bool(np.array_equal(c0, c1) and np.array_equal(i0[0], i1[0]) and
+                np.array_equal(l0[0], l1[0]))
+    del ex
+    torch.cuda.empty_cache()
+    return {"value": S / (ms * 1e-3), "unit": "samples/s", "ms_per_step": ms,
+            "samples_stopped_early": stopped, "identical": same,
+            "note": "opt-in (early_exit=True), not the headline: samples rejected for every "
+                    "uniform by an upper bound from their first 8..96 epochs are not evaluated "
+                    "further; kept rows and their ln L are the full step's",
+            "clocks": clk.summary()}
 
 
 def _parity_slice(table, cache, b64, S):

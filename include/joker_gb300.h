@@ -285,6 +285,15 @@ int joker_refine_band(const joker_stars *stars, const joker_cache *cache,
  * before the first call of a run); chunk a multiple of 128 and at most 8192
  * (0 = 1024).  A jittered table with more than three linear parameters
  * returns JOKER_EINVAL (use joker_lnl + joker_accept_refined).
+ * early_exit != 0 (tables with at most three linear parameters; ignored
+ * otherwise): a warp of samples stops evaluating epochs at a checkpoint
+ * (after 8, 12, 16, 24, 32, 48, 64 or 96 epochs, stars of at most 256
+ * epochs) once the partial sums bound every one of its samples' ln L more
+ * than 746 nats below the running lower bound of the maximum -- rejected for
+ * every uniform, and not the maximum.  Those samples' d_lnl holds that upper
+ * bound and d_err +infinity; joker_accept_fused keeps the same rows either
+ * way.  No counterpart in the reference, which evaluates every sample in
+ * full.
  *
  * joker_accept_fused: joker_accept_refined's output contract for segments
  * whose candidate bits segment s finds at d_cand + s * cand_ld (sample i at
@@ -299,7 +308,7 @@ int joker_lnl_fused(const joker_stars *stars, const joker_cache *cache, int star
                     int64_t row0, int64_t count, const uint64_t *d_pcg, int64_t first,
                     double *d_lnl, int64_t ld, uint64_t *d_max_key, float *d_err,
                     uint64_t *d_bound_key, uint32_t *d_cand, int64_t cand_ld, int64_t chunk,
-                    void *stream);
+                    int early_exit, void *stream);
 int joker_accept_fused(const joker_stars *stars, const joker_cache *cache,
                        const joker_accept_seg *segs, int n_segs, double *d_lnl, float *d_err,
                        const uint64_t *d_bound_key, uint64_t *d_exact_key, int n_slots,

@@ -224,3 +224,66 @@ def test_fused_nan_rows_and_max_out_one(cuda):
     cf = _engine(table, cache_bad, "mixed_fast", [1, 2], S).results()[0]
     np.testing.assert_array_equal(cf, c64)
     assert c64.sum() == 0
+
+
+EXIT_SETS = {
+    # jitter applied, K and v0; an offset column; no jitter with a linear trend
+    "jitter_L2": dict(ns=[40, 12], K=[20.0, 2.0], jitter="applied", poly=1, noff=0),
+    "jitter_L3": dict(ns=[30, 9], K=[15.0, 3.0], jitter="applied", poly=1, noff=1),
+    "plain_L3": dict(ns=[36, 20], K=[25.0, 5.0], jitter="reference", poly=2, noff=0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(EXIT_SETS))
+def test_early_exit_keeps_fp64_rows(cuda, name):
+    """With early exit the kept rows (and their ln L) are still the FP64
+    path's, on stars informative enough for most warps to stop early."""
+    from thejoker_gb300 import device as dev
+    cfg = EXIT_SETS[name]
+    rng = np.random.default_rng(len(name) * 7 + 1)
+    stars = [synth_star(rng, n, K=k, poly=cfg["poly"], noff=cfg["noff"], sig=(0.05, 0.3))
+             for n, k in zip(cfg["ns"], cfg["K"])]
+    S = 1 << 20
+    cache = dev.PriorCache.from_samples(synth_chunk(rng, S, jitter=True))
+    table = dev.StarTable(stars, jitter=cfg["jitter"])
+    seeds = [201 + k for k in range(len(stars))]
+    r64 = _engine(table, cache, "fp64", seeds, 4096).results()
+    rx = _engine(table, cache, "mixed_fast", seeds, 4096, early_exit=True).results()
+    _same(r64, rx, len(stars))
+    assert r64[0].sum() > 0
+
+
+@pytest.mark.parametrize("jitter", ["applied", "reference"])
+def test_early_exit_values_are_upper_bounds(cuda, jitter):
+    """Direct joker_lnl_fused call with early exit: every sample whose error
+    bound is infinite (its warp stopped at a checkpoint) holds a value at or
+    above its FP64 ln L, more than 746 nats below the maximum, and no
+    candidate bit; the other samples hold their usual values and bounds."""
+    from thejoker_gb300 import device as dev
+    rng = np.random.default_rng(5 if jitter == "applied" else 6)
+    st = synth_star(rng, 80, K=100.0, sig=(0.05, 0.2), base=2000.0)   # informative
+    # enough work items (512 samples each) for many waves: the warps of the
+    # first wave see no settled lower bound and run to the end
+    S = 1 << 23
+    cache = dev.PriorCache.from_samples(synth_chunk(rng, S, jitter=True))
+    table = dev.StarTable([st], jitter=jitter)
+    f64 = torch.empty((1, S), dtype=torch.float64, device="cuda")
+    dev.lnl(table, cache, f64, precision="fp64")
+    l64 = f64[0].cpu().numpy()
+    lnl = torch.empty((1, S), dtype=torch.float64, device="cuda")
+    err = torch.empty((1, S), dtype=torch.float32, device="cuda")
+    bk = dev.MaxKeys(2)
+    pcg = dev.pcg_table([dev.pcg64_state(np.random.default_rng(9))])
+    ld, cand = dev.cand_words(1, S)
+    dev.lnl_fused(table, cache, lnl, err, bk, pcg, cand, ld, chunk=512, early_exit=True)
+    v, e = lnl[0].cpu().numpy(), err[0].cpu().numpy()
+    out = np.isinf(e)
+    print(jitter, "samples stopped early", out.mean())
+    assert out.mean() > 0.2
+    assert np.all(v[out] >= l64[out] - 1e-6 * np.abs(l64[out]))
+    assert np.all(l64[out] < l64.max() - 746.0)
+    bits = np.unpackbits(cand[0].cpu().numpy().view(np.uint32).view(np.uint8),
+                         bitorder="little")[:S]
+    assert not np.any(bits[out])
+    keep = ~out
+    assert np.all(np.abs(v[keep] - l64[keep]) <= e[keep] + 1e-9 * np.abs(l64[keep]))

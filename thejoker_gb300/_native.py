@@ -92,7 +92,8 @@ _SIGS = {
     "joker_lnl": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _i64, _i64, ctypes.c_int,
                                  _vp, _i64, _vp, _vp, _vp, ctypes.c_int, _i64, _vp]),
     "joker_lnl_fused": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _i64, _i64, _vp,
-                                       _i64, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i64, _vp]),
+                                       _i64, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i64,
+                                       ctypes.c_int, _vp]),
     "joker_accept_fused": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(AcceptSeg), ctypes.c_int,
                                           _vp, _vp, _vp, _vp, ctypes.c_int, _vp, _i64, _vp, _vp,
                                           _vp, _vp, _vp, _i64, _vp]),

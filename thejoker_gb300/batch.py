@@ -42,10 +42,13 @@ class BatchRejection:
     star and sample for the mixed path).  seeds: one seed per star for its
     numpy PCG64 generator (its first ``n`` uniforms are the star's ``uu``).
     chunk: samples per ln L work item (None: the autotuned size, autotune.py).
+    early_exit (fused path, at most three linear parameters): warps whose
+    samples the partial epoch sums put out of reach stop early; the kept rows
+    and their ln L are the same.
     """
 
     def __init__(self, stars, cache, precision="mixed_fast", jitter="reference", group=None,
-                 max_out=256, seeds=None, chunk=None, timing=False):
+                 max_out=256, seeds=None, chunk=None, timing=False, early_exit=False):
         self.table = stars if isinstance(stars, dev.StarTable) else dev.StarTable(stars,
                                                                                   jitter=jitter)
         self.cache = cache
@@ -78,6 +81,7 @@ class BatchRejection:
         # "mixed_fast": the first acceptance pass runs inside the ln L kernel
         # (joker_lnl_fused), leaving one candidate bit per sample
         self.fused = dev.fused_available(self.table, precision)
+        self.early_exit = bool(early_exit)
         if self.fused:
             self.pcg_dev = dev.pcg_table(self.pcg)
             self.cand_ld, self.cand = dev.cand_words(G, S)
@@ -111,7 +115,8 @@ class BatchRejection:
                 dev.lnl_fused(self.table, self.cache, out, self.err[:n], self.bkeys,
                               self.pcg_dev[g0:g0 + n], self.cand, self.cand_ld, star0=g0,
                               n_sel=n, row0=row0, count=S, max_keys=self.keys,
-                              chunk=min(self.chunk, 8192), stream=stream)
+                              chunk=min(self.chunk, 8192), early_exit=self.early_exit,
+                              stream=stream)
             else:
                 dev.lnl(self.table, self.cache, out, precision=self.precision, star0=g0,
                         n_sel=n, row0=row0, count=S, max_keys=self.keys,

@@ -310,6 +310,48 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
         r32[18] = (float)rc;
         r32[19] = (float)(w * rc);
     }
+    // early-exit checkpoints of the fused pass (L <= 3): the partial sums'
+    // constants after the first k epochs, in the epochs' record order
+    r.n_ck = 0;
+    if (L <= 3) {
+        static const int sched[MAX_CK] = {8, 12, 16, 24, 32, 48, 64, 96};
+        long double P[2] = {0.0L, 0.0L}, Ck = 0.0L, H[4] = {0.0L, 0.0L, 0.0L, 0.0L};
+        int q = 0, i = 0;
+        for (int c = 0; c < MAX_CK; ++c) {
+            const int kend = sched[c];
+            if (kend >= n) break;
+            for (; i < kend; ++i) {
+                long double yp = rv[i];
+                for (int j = 1; j < L; ++j)
+                    yp -= (long double)muk[j] * trend_M[(size_t)i * T + (j - 1)];
+                long double rc = yp;
+                for (int j = 1; j < L; ++j)
+                    rc -= (long double)r.cC[j] * trend_M[(size_t)i * T + (j - 1)];
+                const long double w = ivar[i];
+                Ck += w * rc * rc;
+                for (int j = 0; j < T; ++j) {
+                    const long double Tj = trend_M[(size_t)i * T + j];
+                    P[j] += w * rc * Tj;
+                    for (int m = 0; m < T; ++m) H[j * T + m] += w * Tj * trend_M[(size_t)i * T + m];
+                }
+            }
+            long double Hc[4], Hinv[4] = {0.0L, 0.0L, 0.0L, 0.0L}, ldH = 0.0L;
+            for (int j = 0; j < T * T; ++j) Hc[j] = H[j];
+            for (int j = 0; j < T; ++j) Hc[j * T + j] += 1.0L / (long double)lamk[j + 1];
+            if (T > 0 && !spd_inverse(T, Hc, Hinv, ldH)) break;
+            float *ck = r.ck[q];
+            for (int j = 0; j < 8; ++j) ck[j] = 0.0f;
+            for (int j = 0; j < T; ++j)
+                ck[j] = (float)(P[j] - (long double)r.cC[j + 1] / (long double)lamk[j + 1]);
+            ck[2] = (float)(Ck + kappa);
+            if (T >= 1) ck[3] = (float)Hinv[0];
+            if (T == 2) { ck[4] = (float)Hinv[1]; ck[5] = (float)Hinv[3]; }
+            ck[6] = (float)ldH;
+            r.ck_k[q] = kend;
+            ++q;
+        }
+        r.n_ck = q;
+    }
     split_ff((double)kappa, r.kappa_hi, r.kappa_lo);
     split_ff(r.logdet_const, r.ldc_hi, r.ldc_lo);
     split_ff((double)(n * LOG2PI + slog_lam - slog_ivar), r.lnr_hi, r.lnr_lo);
@@ -808,7 +850,7 @@ extern "C" int joker_lnl_fused(const joker_stars *s, const joker_cache *c, int s
                                int64_t row0, int64_t count, const uint64_t *d_pcg, int64_t first,
                                double *d_lnl, int64_t ld, uint64_t *d_max_key, float *d_err,
                                uint64_t *d_bound_key, uint32_t *d_cand, int64_t cand_ld,
-                               int64_t chunk, void *stream) {
+                               int64_t chunk, int early_exit, void *stream) {
     if (!s || !c) return fail(JOKER_EINVAL, "joker_lnl_fused: NULL handle");
     if (star0 < 0 || n_sel < 0 || star0 + n_sel > s->n_stars)
         return fail(JOKER_EINVAL, "joker_lnl_fused: stars [%d, %d) outside [0, %d)", star0,
@@ -842,6 +884,7 @@ extern "C" int joker_lnl_fused(const joker_stars *s, const joker_cache *c, int s
     a.fa_first = first;
     a.cand_words = d_cand;
     a.cand_ld = cand_ld;
+    a.fa_exit = early_exit != 0 && s->L <= 3;
     cudaStream_t st = (cudaStream_t)stream;
     CUDA_TRY(cudaMemsetAsync(s->d_queue, 0, sizeof(int), st));
     CUDA_TRY(launch_lnl_fused(s->L, s->jitter == JOKER_JITTER_APPLIED, a, 128, st));
@@ -1193,7 +1236,7 @@ extern "C" int joker_rejection_sample(const joker_stars *s, const joker_cache *c
         uint32_t *cand = (uint32_t *)(w + lay.cand);
         CUDA_TRY(cudaMemcpyAsync(d_pcg, pcg, 32 * (size_t)n_sel, cudaMemcpyHostToDevice, st));
         int rc = joker_lnl_fused(s, c, star0, n_sel, row0, count, d_pcg, 0, lnl, count, max_key,
-                                 err, bound_key, cand, lay.cand_ld, 0, stream);
+                                 err, bound_key, cand, lay.cand_ld, 0, 0, stream);
         if (rc != JOKER_OK) return rc;
         return joker_accept_fused(s, c, segs.data(), n_sel, lnl, err, bound_key, exact_key,
                                   n_sel, cand, lay.cand_ld, d_out_idx, d_out_lnl, d_count,

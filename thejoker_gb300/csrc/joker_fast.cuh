@@ -502,6 +502,19 @@ __device__ __forceinline__ int fused_utest(int c, float x, uint64_t m) {
     return x < __logf(u53_to_float(m)) ? 0 : 1;
 }
 
+// The warp's two candidate words of a pass (lanes on j0 = base + t and on
+// j1 = j0 + 128), written by lane 0 for the words inside the item.
+__device__ __forceinline__ void fused_write_words(const LnlArgs &a, const WorkItem &w, int base,
+                                                  unsigned b0, unsigned b1) {
+    if ((threadIdx.x & 31) == 0) {
+        const int wo = base + (int)(threadIdx.x & ~31u);          // the warp's first j0
+        const int64_t q = a.fa_first + (w.row0 - a.row0) + wo;    // its stream position
+        uint32_t *cw = a.cand_words + (int64_t)w.max_slot * a.cand_ld + (q >> 5);
+        if (wo < w.count) cw[0] = b0;
+        if (wo + 128 < w.count) cw[4] = b1;
+    }
+}
+
 template <bool FUSED>
 __device__ __forceinline__ void fused_pass(const LnlArgs &a, const WorkItem &w, int base,
                                            const unsigned long long *s, unsigned long long kd,
@@ -530,14 +543,117 @@ __device__ __forceinline__ void fused_pass(const LnlArgs &a, const WorkItem &w, 
         }
         const unsigned b0 = __ballot_sync(0xffffffffu, c0 == 1);
         const unsigned b1 = __ballot_sync(0xffffffffu, c1 == 1);
-        if ((threadIdx.x & 31) == 0) {
-            const int wo = base + (int)(threadIdx.x & ~31u);          // the warp's first j0
-            const int64_t q = a.fa_first + (w.row0 - a.row0) + wo;    // its stream position
-            uint32_t *cw = a.cand_words + (int64_t)w.max_slot * a.cand_ld + (q >> 5);
-            if (wo < w.count) cw[0] = b0;
-            if (wo + 128 < w.count) cw[4] = b1;
+        fused_write_words(a, w, base, b0, b1);
+    }
+}
+
+// ---- early exit of the fused pass (L <= 3, stars of one epoch tile)
+// ln L over all N epochs is at most the same expression over the first k
+// epochs, with the unseen epochs' log weights taken at their largest,
+// log ivar: chi2 over k epochs minimised over the linear parameters is at
+// most chi2 over all of them (terms are only added), and log det G only grows
+// as epochs are added (G_N - G_k is positive semi-definite).  With the
+// re-centred sums the k-epoch chi2 is C_k + kappa - q'_k^T G_k^-1 q'_k (the
+// substitution r = r_c + T^T beta0 holds on any subset of epochs), where
+// q'_T = P_k - s^2 Q_k - mu0 g_k and P_k (per checkpoint, from the host)
+// carries sum_{i<k} ivar r_c T - Lambda_T^-1 beta0; without jitter the
+// trend block's inverse and log det come from the host as well.  Returns
+// -1/2 of the k-epoch expression and in mag the magnitude of its terms.
+template <int L, bool JIT>
+__device__ __forceinline__ float fast_upper(const StarRec &st, const AccF<L, JIT, float> &A,
+                                            const float *ck, float lgP, float s2, float &mag,
+                                            bool &valid) {
+    constexpr int T = L - 1;
+    static_assert(L <= 3, "early exit takes at most three linear parameters");
+    const float log_lam0f =
+        st.k_scaled ? fminf(st.log_maxK2_f, st.log_kscale_f + lgP) : st.log_lam0_f;
+    const float ilam0 = __expf(-log_lam0f);
+    const float mu = st.mu0_f;
+    float Hi[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}}, ldH = 0.0f;
+    valid = true;
+    if constexpr (!JIT) {
+        if (T >= 1) Hi[0][0] = ck[3];
+        if (T == 2) { Hi[0][1] = Hi[1][0] = ck[4]; Hi[1][1] = ck[5]; }
+        ldH = ck[6];
+    } else if constexpr (T == 1) {
+        const float H11 = A.G[1][1] + st.ilam_hi[1];
+        Hi[0][0] = 1.0f / H11;
+        ldH = __logf(H11);
+        valid = H11 > 0.0f;
+    } else if constexpr (T == 2) {
+        const float H11 = A.G[1][1] + st.ilam_hi[1], H21 = A.G[2][1];
+        const float H22 = A.G[2][2] + st.ilam_hi[2];
+        const float det = H11 * H22 - H21 * H21;
+        const float idet = 1.0f / det;
+        Hi[0][0] = H22 * idet; Hi[1][1] = H11 * idet; Hi[0][1] = Hi[1][0] = -H21 * idet;
+        ldH = __logf(det);
+        valid = det > 0.0f && H11 > 0.0f;
+    }
+    float g[2] = {0.0f, 0.0f}, qT[2] = {0.0f, 0.0f};
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        g[j] = A.g[j + 1];
+        qT[j] = ck[j] - (JIT ? s2 * A.Q[j + 1] : 0.0f) - mu * g[j];
+    }
+    float gv = 0.0f, gz = 0.0f, qz = 0.0f;
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+        float vj = 0.0f, zj = 0.0f;
+#pragma unroll
+        for (int m = 0; m < T; ++m) {
+            vj += Hi[j][m] * g[m];
+            zj += Hi[j][m] * qT[m];
+        }
+        gv += g[j] * vj;
+        gz += g[j] * zj;
+        qz += qT[j] * zj;
+    }
+    const float sK = A.F - gv + ilam0;
+    const float tK = A.D - mu * A.F - gz;
+    float Ceff = JIT ? A.C + st.kappa_hi : ck[2];
+    if (mu != 0.0f) Ceff += mu * (mu * A.F - 2.0f * A.D);
+    const float q2 = tK * tK / sK;
+    const float chi2 = Ceff - qz - q2;
+    const float lnr = st.lnr_hi;
+    float t = chi2 + lnr + ldH + log_lam0f + __logf(sK);
+    if (JIT) t += 0.6931472f * A.LG;
+    mag = fabsf(Ceff) + fabsf(qz) + fabsf(q2) + fabsf(lnr) + fabsf(ldH) + fabsf(log_lam0f) +
+          fabsf(__logf(sK)) + (JIT ? 0.6931472f * fabsf(A.LG) : 0.0f);
+    valid = valid && sK > 0.0f && (t == t) && (mag < 1e30f);
+    return -0.5f * t;
+}
+
+// Whether every active sample of the warp is out of reach after the first
+// ck_k[c] epochs: its k-epoch upper bound, with a margin of 1e-3 of the
+// magnitudes of its terms plus 4 (far above the FP32 error of the sums and of
+// this evaluation), lies more than 746 nats below the running lower bound of
+// the maximum.  Such a sample is rejected for every uniform, 0 included,
+// and cannot be the maximum.  ub0 and ub1 receive the lanes' bounds.
+template <int L, bool JIT>
+__device__ __forceinline__ bool fused_out_of_reach(const StarRec &st,
+                                                   const AccF<L, JIT, float2> &A,
+                                                   const float *ck, float lgP0, float lgP1,
+                                                   float s20, float s21, bool act0, bool act1,
+                                                   const unsigned long long *bk, float &ub0,
+                                                   float &ub1) {
+    const unsigned long long gk = *((volatile const unsigned long long *)(bk + 1));
+    const bool lb_ok = gk != 0ull && gk != 0xFFFFFFFFFFFFFFFFull;
+    bool h0 = !act0, h1 = !act1;
+    ub0 = ub1 = 0.0f;
+    if (__any_sync(0xffffffffu, lb_ok)) {
+        const float lim = (lb_ok ? key_to_float_rd(gk) : 0.0f) - 746.0f;
+        float mag;
+        bool ok;
+        if (act0) {
+            ub0 = fast_upper<L, JIT>(st, accf_lane(A, 0), ck, lgP0, s20, mag, ok);
+            h0 = lb_ok && ok && ub0 + (1e-3f * mag + 4.0f) < lim;
+        }
+        if (act1) {
+            ub1 = fast_upper<L, JIT>(st, accf_lane(A, 1), ck, lgP1, s21, mag, ok);
+            h1 = lb_ok && ok && ub1 + (1e-3f * mag + 4.0f) < lim;
         }
     }
+    return __all_sync(0xffffffffu, h0 && h1);
 }
 
 // Resident CTAs per SM the FP32-sum kernel is compiled for: 8 (64 registers,
@@ -550,9 +666,10 @@ __device__ __forceinline__ void fused_pass(const LnlArgs &a, const WorkItem &w, 
 // FUSED: also the first acceptance pass (implicit work items, chunks of at
 // most FUSED_MAX_CHUNK samples): each sample's uniform from its slot's PCG64
 // stream and its candidate bit.
-template <int L, bool JIT, bool PACKED, bool FUSED>
+template <int L, bool JIT, bool PACKED, bool FUSED, bool EXIT = false>
 __global__ void __launch_bounds__(128, JOKER_FAST_MINB)
 lnl_fast2_kernel(LnlArgs a) {
+    static_assert(!EXIT || (FUSED && L <= 3), "early exit is part of the fused pass, L <= 3");
     __shared__ __align__(16) float sm[TILE * REC32];
     __shared__ double smr[PACKED ? PACK_ROWS * 5 : 1];
     __shared__ unsigned long long s_pcg[FUSED ? 2 * FUSED_PASSES + 4 : 1];
@@ -590,18 +707,69 @@ lnl_fast2_kernel(LnlArgs a) {
             const MixC<float2> c = mix_pair(c0, c1);
             AccF<L, JIT, float2> A;
             A.zero();
-            for (int t0 = 0; t0 < N; t0 += TILE) {
-                const int nt = min(TILE, N - t0);
-                if (!single) {
-                    __syncthreads();
-                    stage_epochs<float, REC32>(sm, a.ep32 + ((size_t)st.epoch_off + t0) * REC32, nt);
-                    staged_star = -1;
-                    __syncthreads();
-                }
-                if (act0) {
+            bool exited = false;
+            float ub0 = 0.0f, ub1 = 0.0f;
+            // every epoch, staged a tile at a time for long stars
+            auto all_epochs = [&]() {
+                for (int t0 = 0; t0 < N; t0 += TILE) {
+                    const int nt = min(TILE, N - t0);
+                    if (!single) {
+                        __syncthreads();
+                        stage_epochs<float, REC32>(sm, a.ep32 + ((size_t)st.epoch_off + t0) * REC32,
+                                                   nt);
+                        staged_star = -1;
+                        __syncthreads();
+                    }
+                    if (act0) {
 #pragma unroll 2
-                    for (int i = 0; i < nt; ++i) fast_epoch<L, JIT, false>(sm + i * REC32, c, A);
+                        for (int i = 0; i < nt; ++i)
+                            fast_epoch<L, JIT, false>(sm + i * REC32, c, A);
+                    }
                 }
+            };
+            if constexpr (EXIT) {
+                if (single) {
+                    // the epochs in segments ending at the star's checkpoints;
+                    // the warp stops once all its samples are out of reach
+                    int i0 = 0;
+                    for (int q = 0; q < st.n_ck; ++q) {
+                        const int kend = st.ck_k[q];
+                        if (act0) {
+#pragma unroll 2
+                            for (int i = i0; i < kend; ++i)
+                                fast_epoch<L, JIT, false>(sm + i * REC32, c, A);
+                        }
+                        i0 = kend;
+                        if (fused_out_of_reach<L, JIT>(st, A, st.ck[q], pb0.w, pb1.w, s20, s21,
+                                                       act0, act1, bk, ub0, ub1)) {
+                            exited = true;
+                            break;
+                        }
+                    }
+                    if (!exited && act0) {
+#pragma unroll 2
+                        for (int i = i0; i < N; ++i)
+                            fast_epoch<L, JIT, false>(sm + i * REC32, c, A);
+                    }
+                } else {
+                    all_epochs();
+                }
+            } else {
+                all_epochs();
+            }
+            if (EXIT && exited) {
+                // ln L of these samples is left at their upper bound, with an
+                // infinite error bound; they carry no candidate bit and no key
+                if (act0) {
+                    a.lnl[w.out_off + j0] = (double)ub0;
+                    a.err[w.out_off + j0] = __int_as_float(0x7f800000);
+                }
+                if (act1) {
+                    a.lnl[w.out_off + j1] = (double)ub1;
+                    a.err[w.out_off + j1] = __int_as_float(0x7f800000);
+                }
+                fused_write_words(a, w, base, 0u, 0u);
+                continue;
             }
             ff l0 = ffv(0.0f), l1 = ffv(0.0f);
             float err0 = 0.0f, err1 = 0.0f;
@@ -622,6 +790,13 @@ lnl_fast2_kernel(LnlArgs a) {
 // with it.
 template <bool FUSED, int L, bool JIT>
 static cudaError_t launch_fast_LJ(const LnlArgs &a, int block, cudaStream_t st) {
+    if constexpr (FUSED && L <= 3) {
+        if (a.fa_exit) {
+            if (a.mx_a == nullptr)
+                return launch_persistent(lnl_fast2_kernel<L, JIT, true, true, true>, a, block, st);
+            return launch_persistent(lnl_fast2_kernel<L, JIT, false, true, true>, a, block, st);
+        }
+    }
     if (a.mx_a == nullptr)
         return launch_persistent(lnl_fast2_kernel<L, JIT, true, FUSED>, a, block, st);
     return launch_persistent(lnl_fast2_kernel<L, JIT, false, FUSED>, a, block, st);

@@ -14,6 +14,7 @@ void count_launch();
 constexpr int TILE = 256;          // epochs staged in shared memory at a time
 constexpr int REC32 = 20;          // floats per epoch record of the mixed kernel
 constexpr int REC64 = 8;           // doubles per epoch record of the FP64 kernel
+constexpr int MAX_CK = 8;          // early-exit checkpoints per star (fused pass)
 
 // Per-star constants, built on the host in FP64 (joker_abi.cu).  Index 0 of
 // the linear parameters is K; 1.. are v0, the offsets and the trend terms.
@@ -62,7 +63,14 @@ struct alignas(16) StarRec {
     float Wjj[MAXL];                   // sum ivar T_j^2 (j >= 1), rounded up
     float log_kscale_f, log_maxK2_f;   // log_kscale, log_maxK2 rounded to float
     float log_lam0_f;                  // log lam0 rounded to float
-    float pad3;
+    // Early exit of the fused pass (L <= 3): after the first ck_k[c] epochs
+    // the partial sums bound ln L from above.  Per checkpoint: P_j = sum over
+    // those epochs of ivar r_c T_j minus (Lambda_T^-1 beta0)_j (j = 1, 2);
+    // without jitter also C + kappa over those epochs, the inverse of the
+    // partial trend block H (11, 12, 22) and log det H.
+    int32_t n_ck;
+    int32_t ck_k[MAX_CK];
+    float ck[MAX_CK][8];          // P1, P2, C + kappa, Hi11, Hi12, Hi22, log det H, 0
 };
 
 // One unit of the persistent likelihood kernels: `count` samples of star
@@ -116,6 +124,10 @@ struct LnlArgs {
     int64_t fa_first;
     uint32_t *cand_words;
     int64_t cand_ld;
+    // early exit (L <= 3): a warp stops evaluating epochs once the partial
+    // sums put all its samples out of reach; their ln L is left at that upper
+    // bound with an infinite error bound, and they get no candidate bit
+    int fa_exit;
 };
 
 // Largest work item (samples) of the fused pass: its per-pass generator

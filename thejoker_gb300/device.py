@@ -449,11 +449,15 @@ def cand_words(n_sel, n_samples):
 
 
 def lnl_fused(stars, cache, out, err, bound_keys, pcg, cand, cand_ld, star0=0, n_sel=None,
-              row0=0, count=None, first=0, max_keys=None, chunk=0, out_offset=0, stream=None):
+              row0=0, count=None, first=0, max_keys=None, chunk=0, out_offset=0,
+              early_exit=False, stream=None):
     """ln L at "mixed_fast" with the first acceptance pass fused in
     (joker_lnl_fused): as ``lnl``, plus each sample's candidate bit in
     ``cand`` (from cand_words).  ``pcg``: pcg_table of the n_sel stars' streams;
-    row row0 + j is number first + j of each stream."""
+    row row0 + j is number first + j of each stream.  ``early_exit``: warps
+    whose samples the partial sums put out of reach stop early; those samples'
+    ``out`` holds an upper bound and ``err`` infinity (the kept rows are the
+    same)."""
     n_sel = stars.n_stars - star0 if n_sel is None else n_sel
     count = cache.size - row0 if count is None else count
     if out.dtype != torch.float64 or out.dim() != 2 or out.shape[0] < n_sel or \
@@ -467,8 +471,8 @@ def lnl_fused(stars, cache, out, err, bound_keys, pcg, cand, cand_ld, star0=0, n
         ctypes.c_void_p(out.data_ptr() + 8 * int(out_offset)), out.shape[1],
         max_keys.ptr() if max_keys is not None else None,
         ctypes.c_void_p(err.data_ptr() + 4 * int(out_offset)), bound_keys.ptr(),
-        ctypes.c_void_p(cand.data_ptr()), int(cand_ld), int(chunk), stream_handle(stream)),
-        "joker_lnl_fused")
+        ctypes.c_void_p(cand.data_ptr()), int(cand_ld), int(chunk), int(bool(early_exit)),
+        stream_handle(stream)), "joker_lnl_fused")
     return out
 
 
