@@ -557,37 +557,51 @@ __device__ __forceinline__ void fused_pass(const LnlArgs &a, const WorkItem &w, 
 // substitution r = r_c + T^T beta0 holds on any subset of epochs), where
 // q'_T = P_k - s^2 Q_k - mu0 g_k and P_k (per checkpoint, from the host)
 // carries sum_{i<k} ivar r_c T - Lambda_T^-1 beta0; without jitter the
-// trend block's inverse and log det come from the host as well.  Returns
-// -1/2 of the k-epoch expression and in mag the magnitude of its terms.
+// trend block's inverse and log det come from the host as well.
+//
+// Returns -1/2 of the k-epoch expression and in dub a margin for its error:
+// 1e-3 of its terms' magnitudes (over 100 times the rounding of FP32 sums of
+// at most 103 terms, which covers the cross sums' Cauchy-Schwarz factors in
+// practice) plus the amplification of the sums' rounding through an
+// ill-conditioned Schur complement s or trend block H (t^2 / s and
+// q'^T H^-1 q' move by their relative errors), and 2 nats; valid = false
+// when s or det H lies within four times its error of zero (a long-period
+// sample nearly collinear with the constant column, say).
 template <int L, bool JIT>
 __device__ __forceinline__ float fast_upper(const StarRec &st, const AccF<L, JIT, float> &A,
-                                            const float *ck, float lgP, float s2, float &mag,
+                                            const float *ck, float lgP, float s2, float &dub,
                                             bool &valid) {
     constexpr int T = L - 1;
+    constexpr float g1 = 2e-5f;   // three times the rounding bound of a sum of <= 103 terms
     static_assert(L <= 3, "early exit takes at most three linear parameters");
     const float log_lam0f =
         st.k_scaled ? fminf(st.log_maxK2_f, st.log_kscale_f + lgP) : st.log_lam0_f;
     const float ilam0 = __expf(-log_lam0f);
     const float mu = st.mu0_f;
-    float Hi[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}}, ldH = 0.0f;
+    float Hi[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}}, ldH = 0.0f, rH = 0.0f;
     valid = true;
     if constexpr (!JIT) {
+        // host-computed: only the float rounding of the entries
         if (T >= 1) Hi[0][0] = ck[3];
         if (T == 2) { Hi[0][1] = Hi[1][0] = ck[4]; Hi[1][1] = ck[5]; }
         ldH = ck[6];
+        rH = 1e-6f;
     } else if constexpr (T == 1) {
         const float H11 = A.G[1][1] + st.ilam_hi[1];
         Hi[0][0] = 1.0f / H11;
         ldH = __logf(H11);
+        rH = 2.0f * g1;
         valid = H11 > 0.0f;
     } else if constexpr (T == 2) {
         const float H11 = A.G[1][1] + st.ilam_hi[1], H21 = A.G[2][1];
         const float H22 = A.G[2][2] + st.ilam_hi[2];
         const float det = H11 * H22 - H21 * H21;
+        const float ddet = 2.0f * g1 * (H11 * H22 + H21 * H21);
         const float idet = 1.0f / det;
         Hi[0][0] = H22 * idet; Hi[1][1] = H11 * idet; Hi[0][1] = Hi[1][0] = -H21 * idet;
         ldH = __logf(det);
-        valid = det > 0.0f && H11 > 0.0f;
+        rH = ddet / (det - ddet) + g1;
+        valid = det > 4.0f * ddet && H11 > 0.0f;
     }
     float g[2] = {0.0f, 0.0f}, qT[2] = {0.0f, 0.0f};
 #pragma unroll
@@ -609,26 +623,29 @@ __device__ __forceinline__ float fast_upper(const StarRec &st, const AccF<L, JIT
         qz += qT[j] * zj;
     }
     const float sK = A.F - gv + ilam0;
+    const float ds = g1 * (A.F + ilam0 + fabsf(gv)) + rH * fabsf(gv);
     const float tK = A.D - mu * A.F - gz;
     float Ceff = JIT ? A.C + st.kappa_hi : ck[2];
     if (mu != 0.0f) Ceff += mu * (mu * A.F - 2.0f * A.D);
     const float q2 = tK * tK / sK;
     const float chi2 = Ceff - qz - q2;
     const float lnr = st.lnr_hi;
-    float t = chi2 + lnr + ldH + log_lam0f + __logf(sK);
+    const float lsK = __logf(sK);
+    float t = chi2 + lnr + ldH + log_lam0f + lsK;
     if (JIT) t += 0.6931472f * A.LG;
-    mag = fabsf(Ceff) + fabsf(qz) + fabsf(q2) + fabsf(lnr) + fabsf(ldH) + fabsf(log_lam0f) +
-          fabsf(__logf(sK)) + (JIT ? 0.6931472f * fabsf(A.LG) : 0.0f);
-    valid = valid && sK > 0.0f && (t == t) && (mag < 1e30f);
+    const float mag = fabsf(Ceff) + fabsf(qz) + q2 + fabsf(lnr) + fabsf(ldH) +
+                      fabsf(log_lam0f) + fabsf(lsK) + (JIT ? 0.6931472f * A.LG : 0.0f);
+    valid = valid && sK > 4.0f * ds && (t == t) && mag < 1e30f;
+    const float cond = q2 * ds / (sK - ds) + fabsf(qz) * rH + ds / (sK - ds) + rH * (float)T;
+    dub = 0.5f * (1e-3f * mag + 2.0f * cond) + 2.0f;
     return -0.5f * t;
 }
 
 // Whether every active sample of the warp is out of reach after the first
-// ck_k[c] epochs: its k-epoch upper bound, with a margin of 1e-3 of the
-// magnitudes of its terms plus 4 (far above the FP32 error of the sums and of
-// this evaluation), lies more than 746 nats below the running lower bound of
-// the maximum.  Such a sample is rejected for every uniform, 0 included,
-// and cannot be the maximum.  ub0 and ub1 receive the lanes' bounds.
+// ck_k[c] epochs: its k-epoch upper bound plus its margin lies more than 746
+// nats below the running lower bound of the maximum.  Such a sample is
+// rejected for every uniform, 0 included, and cannot be the maximum.  ub0
+// and ub1 receive the lanes' bounds.
 template <int L, bool JIT>
 __device__ __forceinline__ bool fused_out_of_reach(const StarRec &st,
                                                    const AccF<L, JIT, float2> &A,
@@ -642,15 +659,15 @@ __device__ __forceinline__ bool fused_out_of_reach(const StarRec &st,
     ub0 = ub1 = 0.0f;
     if (__any_sync(0xffffffffu, lb_ok)) {
         const float lim = (lb_ok ? key_to_float_rd(gk) : 0.0f) - 746.0f;
-        float mag;
+        float dub;
         bool ok;
         if (act0) {
-            ub0 = fast_upper<L, JIT>(st, accf_lane(A, 0), ck, lgP0, s20, mag, ok);
-            h0 = lb_ok && ok && ub0 + (1e-3f * mag + 4.0f) < lim;
+            ub0 = fast_upper<L, JIT>(st, accf_lane(A, 0), ck, lgP0, s20, dub, ok);
+            h0 = lb_ok && ok && ub0 + dub < lim;
         }
         if (act1) {
-            ub1 = fast_upper<L, JIT>(st, accf_lane(A, 1), ck, lgP1, s21, mag, ok);
-            h1 = lb_ok && ok && ub1 + (1e-3f * mag + 4.0f) < lim;
+            ub1 = fast_upper<L, JIT>(st, accf_lane(A, 1), ck, lgP1, s21, dub, ok);
+            h1 = lb_ok && ok && ub1 + dub < lim;
         }
     }
     return __all_sync(0xffffffffu, h0 && h1);
