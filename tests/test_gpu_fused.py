@@ -258,14 +258,19 @@ def test_early_exit_values_are_upper_bounds(cuda, jitter):
     """Direct joker_lnl_fused call with early exit: every sample whose error
     bound is infinite (its warp stopped at a checkpoint) holds a value at or
     above its FP64 ln L, more than 746 nats below the maximum, and no
-    candidate bit; the other samples hold their usual values and bounds."""
+    candidate bit; the other samples hold their usual values and bounds.  An
+    eighth of the orbits (a contiguous block, so that whole warps hold them)
+    have e in [0.9, 0.995], where the FP32 column's own error is largest."""
     from thejoker_gb300 import device as dev
     rng = np.random.default_rng(5 if jitter == "applied" else 6)
     st = synth_star(rng, 80, K=100.0, sig=(0.05, 0.2), base=2000.0)   # informative
     # enough work items (512 samples each) for many waves: the warps of the
     # first wave see no settled lower bound and run to the end
     S = 1 << 23
-    cache = dev.PriorCache.from_samples(synth_chunk(rng, S, jitter=True))
+    ch = synth_chunk(rng, S, jitter=True)
+    ecc = slice(S // 2, S // 2 + S // 8)                  # eccentric orbits: large column error
+    ch[ecc, 1] = rng.uniform(0.9, 0.995, S // 8)
+    cache = dev.PriorCache.from_samples(ch)
     table = dev.StarTable([st], jitter=jitter)
     f64 = torch.empty((1, S), dtype=torch.float64, device="cuda")
     dev.lnl(table, cache, f64, precision="fp64")

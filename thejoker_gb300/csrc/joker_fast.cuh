@@ -562,15 +562,17 @@ __device__ __forceinline__ void fused_pass(const LnlArgs &a, const WorkItem &w, 
 // Returns -1/2 of the k-epoch expression and in dub a margin for its error:
 // 1e-3 of its terms' magnitudes (over 100 times the rounding of FP32 sums of
 // at most 103 terms, which covers the cross sums' Cauchy-Schwarz factors in
-// practice) plus the amplification of the sums' rounding through an
+// practice), plus the amplification of the sums' rounding through an
 // ill-conditioned Schur complement s or trend block H (t^2 / s and
-// q'^T H^-1 q' move by their relative errors), and 2 nats; valid = false
-// when s or det H lies within four times its error of zero (a long-period
-// sample nearly collinear with the constant column, say).
+// q'^T H^-1 q' move by their relative errors), plus twice the FP32 column's
+// own error term of the full bound (err_c0 (1 + e) / (1 - e)^2 per epoch,
+// large for eccentric orbits), and 2 nats; valid = false when s or det H
+// lies within four times its error of zero (a long-period sample nearly
+// collinear with the constant column, say).
 template <int L, bool JIT>
 __device__ __forceinline__ float fast_upper(const StarRec &st, const AccF<L, JIT, float> &A,
-                                            const float *ck, float lgP, float s2, float &dub,
-                                            bool &valid) {
+                                            const float *ck, float lgP, float s2, float e,
+                                            float ome, float err_c0, float &dub, bool &valid) {
     constexpr int T = L - 1;
     constexpr float g1 = 2e-5f;   // three times the rounding bound of a sum of <= 103 terms
     static_assert(L <= 3, "early exit takes at most three linear parameters");
@@ -635,9 +637,16 @@ __device__ __forceinline__ float fast_upper(const StarRec &st, const AccF<L, JIT
     if (JIT) t += 0.6931472f * A.LG;
     const float mag = fabsf(Ceff) + fabsf(qz) + q2 + fabsf(lnr) + fabsf(ldH) +
                       fabsf(log_lam0f) + fabsf(lsK) + (JIT ? 0.6931472f * A.LG : 0.0f);
-    valid = valid && sK > 4.0f * ds && (t == t) && mag < 1e30f;
+    // the FP32 column's own error (err_c0, as in the full bound): chi2 moves
+    // by at most 2 |theta_K| Dcol sqrt(W chi2) + theta_K^2 Dcol^2 W, s by dsc
+    const float Dcol = err_c0 * (1.0f + e) / (ome * ome);
+    const float Wsum = st.sum_ivar, Kh = fabsf(tK / sK), c2 = fmaxf(chi2, 0.0f);
+    const float dsc = 2.0f * Dcol * sqrtf(Wsum * fmaxf(A.F - gv, 0.0f)) + Wsum * Dcol * Dcol;
+    valid = valid && sK > 4.0f * ds && dsc < 0.5f * sK && (t == t) && mag < 1e30f;
+    const float col = 2.0f * Kh * Dcol * sqrtf(Wsum * c2) + Kh * Kh * Dcol * Dcol * Wsum +
+                      dsc / (sK - dsc);
     const float cond = q2 * ds / (sK - ds) + fabsf(qz) * rH + ds / (sK - ds) + rH * (float)T;
-    dub = 0.5f * (1e-3f * mag + 2.0f * cond) + 2.0f;
+    dub = 0.5f * (1e-3f * mag + 2.0f * cond + 2.0f * col) + 2.0f;
     return -0.5f * t;
 }
 
@@ -649,10 +658,11 @@ __device__ __forceinline__ float fast_upper(const StarRec &st, const AccF<L, JIT
 template <int L, bool JIT>
 __device__ __forceinline__ bool fused_out_of_reach(const StarRec &st,
                                                    const AccF<L, JIT, float2> &A,
-                                                   const float *ck, float lgP0, float lgP1,
-                                                   float s20, float s21, bool act0, bool act1,
-                                                   const unsigned long long *bk, float &ub0,
-                                                   float &ub1) {
+                                                   const float *ck, float e0, float ome0,
+                                                   float e1, float ome1, float lgP0, float lgP1,
+                                                   float s20, float s21, float err_c0, bool act0,
+                                                   bool act1, const unsigned long long *bk,
+                                                   float &ub0, float &ub1) {
     const unsigned long long gk = *((volatile const unsigned long long *)(bk + 1));
     const bool lb_ok = gk != 0ull && gk != 0xFFFFFFFFFFFFFFFFull;
     bool h0 = !act0, h1 = !act1;
@@ -662,11 +672,13 @@ __device__ __forceinline__ bool fused_out_of_reach(const StarRec &st,
         float dub;
         bool ok;
         if (act0) {
-            ub0 = fast_upper<L, JIT>(st, accf_lane(A, 0), ck, lgP0, s20, dub, ok);
+            ub0 = fast_upper<L, JIT>(st, accf_lane(A, 0), ck, lgP0, s20, e0, ome0, err_c0,
+                                     dub, ok);
             h0 = lb_ok && ok && ub0 + dub < lim;
         }
         if (act1) {
-            ub1 = fast_upper<L, JIT>(st, accf_lane(A, 1), ck, lgP1, s21, dub, ok);
+            ub1 = fast_upper<L, JIT>(st, accf_lane(A, 1), ck, lgP1, s21, e1, ome1, err_c0,
+                                     dub, ok);
             h1 = lb_ok && ok && ub1 + dub < lim;
         }
     }
@@ -757,7 +769,8 @@ lnl_fast2_kernel(LnlArgs a) {
                                 fast_epoch<L, JIT, false>(sm + i * REC32, c, A);
                         }
                         i0 = kend;
-                        if (fused_out_of_reach<L, JIT>(st, A, st.ck[q], pb0.w, pb1.w, s20, s21,
+                        if (fused_out_of_reach<L, JIT>(st, A, st.ck[q], c0.e, c0.ome, c1.e,
+                                                       c1.ome, pb0.w, pb1.w, s20, s21, a.err_c0,
                                                        act0, act1, bk, ub0, ub1)) {
                             exited = true;
                             break;
