@@ -290,10 +290,12 @@ int joker_refine_band(const joker_stars *stars, const joker_cache *cache,
  * (after 8, 12, 16, 24, 32, 48, 64 or 96 epochs, stars of at most 256
  * epochs) once the partial sums bound every one of its samples' ln L more
  * than 746 nats below the running lower bound of the maximum -- rejected for
- * every uniform, and not the maximum.  Those samples' d_lnl holds that upper
- * bound and d_err +infinity; joker_accept_fused keeps the same rows either
- * way.  No counterpart in the reference, which evaluates every sample in
- * full.
+ * every uniform, and not the maximum -- and, after the last epoch, skips the
+ * float-float tail and error bound of warps whose samples are all that far
+ * below.  Those samples' d_lnl holds that upper bound (after the last epoch
+ * ln L in FP32) and d_err +infinity; joker_accept_fused keeps the same rows
+ * either way.  No counterpart in the reference, which evaluates every sample
+ * in full.
  *
  * joker_accept_fused: joker_accept_refined's output contract for segments
  * whose candidate bits segment s finds at d_cand + s * cand_ld (sample i at

@@ -256,9 +256,11 @@ def test_early_exit_keeps_fp64_rows(cuda, name):
 @pytest.mark.parametrize("jitter", ["applied", "reference"])
 def test_early_exit_values_are_upper_bounds(cuda, jitter):
     """Direct joker_lnl_fused call with early exit: every sample whose error
-    bound is infinite (its warp stopped at a checkpoint) holds a value at or
-    above its FP64 ln L, more than 746 nats below the maximum, and no
-    candidate bit; the other samples hold their usual values and bounds.  An
+    bound is infinite (its warp stopped at a checkpoint, or was out of reach
+    after its last epoch) holds a value at or above its FP64 ln L (up to
+    FP32 rounding after the last epoch), lies more than 746 nats below the
+    maximum, and has no candidate bit; the other samples hold their usual
+    values and bounds.  An
     eighth of the orbits (a contiguous block, so that whole warps hold them)
     have e in [0.9, 0.995], where the FP32 column's own error is largest."""
     from thejoker_gb300 import device as dev
@@ -285,8 +287,12 @@ def test_early_exit_values_are_upper_bounds(cuda, jitter):
     out = np.isinf(e)
     print(jitter, "samples stopped early", out.mean())
     assert out.mean() > 0.2
-    assert np.all(v[out] >= l64[out] - 1e-6 * np.abs(l64[out]))
+    # none of them can be kept or be the maximum
     assert np.all(l64[out] < l64.max() - 746.0)
+    # an upper bound from the first epochs, or ln L itself in FP32 after the
+    # last (whose rounding scales with the cancelling chi2 terms, up to 1e8
+    # here, not with ln L)
+    assert np.all(v[out] >= l64[out] - 1e-4 * np.abs(l64[out]) - 100.0)
     bits = np.unpackbits(cand[0].cpu().numpy().view(np.uint32).view(np.uint8),
                          bitorder="little")[:S]
     assert not np.any(bits[out])

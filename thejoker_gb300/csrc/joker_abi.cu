@@ -351,6 +351,13 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
             ++q;
         }
         r.n_ck = q;
+        // all epochs: P = 0 (T W0 r_c = Lambda_T^-1 beta0), C + kappa = chi2_0,
+        // H = C (the folded trend block)
+        for (int j = 0; j < 8; ++j) r.ck_full[j] = 0.0f;
+        r.ck_full[2] = (float)(Cn + kappa);
+        if (T >= 1) r.ck_full[3] = (float)Cinv[0];
+        if (T == 2) { r.ck_full[4] = (float)Cinv[1]; r.ck_full[5] = (float)Cinv[3]; }
+        r.ck_full[6] = (float)logdetC;
     }
     split_ff((double)kappa, r.kappa_hi, r.kappa_lo);
     split_ff(r.logdet_const, r.ldc_hi, r.ldc_lo);

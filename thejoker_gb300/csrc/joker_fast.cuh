@@ -776,10 +776,17 @@ lnl_fast2_kernel(LnlArgs a) {
                             break;
                         }
                     }
-                    if (!exited && act0) {
+                    if (!exited) {
+                        if (act0) {
 #pragma unroll 2
-                        for (int i = i0; i < N; ++i)
-                            fast_epoch<L, JIT, false>(sm + i * REC32, c, A);
+                            for (int i = i0; i < N; ++i)
+                                fast_epoch<L, JIT, false>(sm + i * REC32, c, A);
+                        }
+                        // all epochs: the same test on the full sums spares the
+                        // float-float tail and its bound (ub is then ln L in FP32)
+                        exited = fused_out_of_reach<L, JIT>(st, A, st.ck_full, c0.e, c0.ome, c1.e,
+                                                            c1.ome, pb0.w, pb1.w, s20, s21,
+                                                            a.err_c0, act0, act1, bk, ub0, ub1);
                     }
                 } else {
                     all_epochs();
@@ -788,8 +795,9 @@ lnl_fast2_kernel(LnlArgs a) {
                 all_epochs();
             }
             if (EXIT && exited) {
-                // ln L of these samples is left at their upper bound, with an
-                // infinite error bound; they carry no candidate bit and no key
+                // ln L of these samples is left at their upper bound (or, after
+                // the last epoch, at its FP32 value), with an infinite error
+                // bound; they carry no candidate bit and no key
                 if (act0) {
                     a.lnl[w.out_off + j0] = (double)ub0;
                     a.err[w.out_off + j0] = __int_as_float(0x7f800000);

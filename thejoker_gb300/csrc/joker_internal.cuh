@@ -71,6 +71,7 @@ struct alignas(16) StarRec {
     int32_t n_ck;
     int32_t ck_k[MAX_CK];
     float ck[MAX_CK][8];          // P1, P2, C + kappa, Hi11, Hi12, Hi22, log det H, 0
+    float ck_full[8];             // the same over all epochs (P = 0, C + kappa = chi2_0)
 };
 
 // One unit of the persistent likelihood kernels: `count` samples of star
