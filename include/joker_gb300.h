@@ -285,17 +285,18 @@ int joker_refine_band(const joker_stars *stars, const joker_cache *cache,
  * before the first call of a run); chunk a multiple of 128 and at most 8192
  * (0 = 1024).  A jittered table with more than three linear parameters
  * returns JOKER_EINVAL (use joker_lnl + joker_accept_refined).
- * early_exit != 0 (tables with at most three linear parameters; ignored
- * otherwise): a warp of samples stops evaluating epochs at a checkpoint
- * (after 8, 12, 16, 24, 32, 48, 64 or 96 epochs, stars of at most 256
- * epochs) once the partial sums bound every one of its samples' ln L more
- * than 746 nats below the running lower bound of the maximum -- rejected for
- * every uniform, and not the maximum -- and, after the last epoch, skips the
- * float-float tail and error bound of warps whose samples are all that far
- * below.  Those samples' d_lnl holds that upper bound (after the last epoch
- * ln L in FP32) and d_err +infinity; joker_accept_fused keeps the same rows
- * either way.  No counterpart in the reference, which evaluates every sample
- * in full.
+ * With at most three linear parameters, a warp of 64 samples whose ln L all
+ * lie more than 746 nats below the running lower bound of the maximum after
+ * the last epoch (rejected for every uniform, and none the maximum) keeps
+ * their ln L in FP32 with d_err +infinity, skipping the float-float tail and
+ * its bound; every other sample gets its usual value and bound.
+ * early_exit != 0 (at most three linear parameters; ignored otherwise): a
+ * warp also stops evaluating epochs at a checkpoint (after 8, 12, 16, 24,
+ * 32, 48, 64 or 96 epochs, stars of at most 256 epochs) once the partial
+ * sums put every one of its samples that far below; those samples' d_lnl
+ * holds that upper bound and d_err +infinity.  joker_accept_fused keeps the
+ * same rows either way.  No counterpart in the reference, which evaluates
+ * every sample in full.
  *
  * joker_accept_fused: joker_accept_refined's output contract for segments
  * whose candidate bits segment s finds at d_cand + s * cand_ld (sample i at

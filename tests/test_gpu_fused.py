@@ -231,6 +231,9 @@ EXIT_SETS = {
     "jitter_L2": dict(ns=[40, 12], K=[20.0, 2.0], jitter="applied", poly=1, noff=0),
     "jitter_L3": dict(ns=[30, 9], K=[15.0, 3.0], jitter="applied", poly=1, noff=1),
     "plain_L3": dict(ns=[36, 20], K=[25.0, 5.0], jitter="reference", poly=2, noff=0),
+    # a star above the 256-epoch tile (no checkpoints) beside one with fewer
+    # epochs than the first checkpoint (only the test after the last epoch)
+    "long_short": dict(ns=[300, 6], K=[20.0, 30.0], jitter="applied", poly=1, noff=0),
 }
 
 

@@ -790,11 +790,22 @@ lnl_fast2_kernel(LnlArgs a) {
                     }
                 } else {
                     all_epochs();
+                    exited = fused_out_of_reach<L, JIT>(st, A, st.ck_full, c0.e, c0.ome, c1.e,
+                                                        c1.ome, pb0.w, pb1.w, s20, s21,
+                                                        a.err_c0, act0, act1, bk, ub0, ub1);
                 }
             } else {
                 all_epochs();
+                if constexpr (FUSED && L <= 3) {
+                    // every epoch evaluated: a warp whose samples are all out of
+                    // reach (rejected for every uniform, not the maximum) keeps
+                    // their ln L in FP32 and skips the float-float tail and bound
+                    exited = fused_out_of_reach<L, JIT>(st, A, st.ck_full, c0.e, c0.ome, c1.e,
+                                                        c1.ome, pb0.w, pb1.w, s20, s21,
+                                                        a.err_c0, act0, act1, bk, ub0, ub1);
+                }
             }
-            if (EXIT && exited) {
+            if ((EXIT || (FUSED && L <= 3)) && exited) {
                 // ln L of these samples is left at their upper bound (or, after
                 // the last epoch, at its FP32 value), with an infinite error
                 // bound; they carry no candidate bit and no key
