@@ -232,6 +232,25 @@ def test_mixed_bound_holds_on_many_samples(cuda, n_ep, poly, noff, jitter):
 
 
 @pytest.mark.parametrize("jitter", ["reference", "applied"])
+def test_mixed_bound_holds_over_long_spans(cuda, jitter):
+    """Epochs over 20000 d and periods down to 0.5 d (up to 4e4 cycles from
+    the reference epoch): the FP32-sum path's split phase rounds to about
+    2^-34 dt/P cycles, and its bound grows with 1/P and the star's span to
+    cover that; both mixed paths stay within their per-sample bounds."""
+    rng = np.random.default_rng(77)
+    st = synth_star(rng, 40, base=20000.0)
+    chunk = synth_chunk(rng, 1 << 18, P_min=0.5, P_max=20.0, jitter=True)
+    chunk[:4000, 1] = rng.uniform(0.9, 0.99, 4000)
+    table = _table([st], jitter=jitter)
+    ref64 = _lnl(table, chunk, "fp64")[0]
+    for prec in ("mixed", "mixed_fast"):
+        got, err = _lnl(table, chunk, prec, with_err=True)
+        ok, ratio = within_bound(got[0], err[0], ref64)
+        print(jitter, prec, "max |d|/bound", ratio)
+        assert ok, ratio
+
+
+@pytest.mark.parametrize("jitter", ["reference", "applied"])
 def test_fp64_extreme_elements(cuda, jitter):
     """Periods over 2 d .. 1e7 d (P / P0 across 22 binary exponents of the
     scaled K prior's (P / P0)^(-2/3)), omega and M0 well outside [0, 2 pi),

@@ -280,7 +280,7 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
     r.sum_log_ivar = (double)slog_ivar;
     // FP32-sum path: the residual of the trend-only fit r_c = y' - T^T beta0
     // (beta0 = C^-1 c, as stored in cC) and the magnitudes its bound needs
-    long double Cn = 0.0L, ivmax = 0.0L, Wjj[MAXL] = {0.0L}, kappa = 0.0L;
+    long double Cn = 0.0L, ivmax = 0.0L, Wjj[MAXL] = {0.0L}, kappa = 0.0L, dtmax = 0.0L;
     for (int j = 1; j < L; ++j) kappa += (long double)r.cC[j] * r.cC[j] / (long double)lamk[j];
     for (int i = 0; i < n; ++i) {
         long double yp = rv[i];
@@ -294,6 +294,7 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
             const long double Tj = trend_M[(size_t)i * T + (j - 1)];
             Wjj[j] += w * Tj * Tj;
         }
+        dtmax = std::max(dtmax, (long double)std::fabs(t[i] - t_ref));
         float *r32 = rec32 + (size_t)i * REC32;
         // dt split for the FP32-sum kernel's phase: dth with 12 significant
         // bits (exact in a float), dtl the rest.  Words 16 and 17 are free in
@@ -364,6 +365,8 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
     split_ff((double)(n * LOG2PI + slog_lam - slog_ivar), r.lnr_hi, r.lnr_lo);
     r.Cn = (float)(Cn * (1.0L + 1e-6L));
     r.ivar_max = (float)(ivmax * (1.0L + 1e-6L));
+    r.phase_c = (float)(dtmax * (2.0L * 3.141592653589793238462643383279502884L * 0x1p-33L *
+                                 (1.0L + 1e-6L)));
     for (int j = 1; j < L; ++j) r.Wjj[j] = (float)(Wjj[j] * (1.0L + 1e-6L));
     return JOKER_OK;
 }

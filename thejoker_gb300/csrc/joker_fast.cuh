@@ -27,8 +27,9 @@
 // bounded term by term, the last by 2 tr(G^-1) |dq' - dG theta|^2 while
 // |dG|_F tr(G^-1) < 1/4 (else err = 1e30: no bound, always refined); and
 // |d log det G| <= |tr(G^-1 dG)| + 1.34 |G^-1 dG|_F^2.  The FP32 column's own
-// error (phase rounding, FP32 Kepler; the constant err_c0 is empirical)
-// enters as in the mixed kernel.  The tail runs in float-float; the only FP64
+// error (FP32 Kepler and the phase's constant rounding: the empirical
+// constant err_c0; the split phase's rounding, at most 2^-34 |dt| / P cycles,
+// as 2 pi 2^-33 max|dt| / P radians on top) enters as in the mixed kernel.  The tail runs in float-float; the only FP64
 // instruction per sample is the addition that rounds ln L's float pair to a
 // double (both halves converted by integer operations).
 #pragma once
@@ -60,16 +61,17 @@ template <int L, bool JIT, class T> struct AccF {
 // exact in FP32 and so is its fractional part; |dth il| + |dtl / P| is below
 // 2^-10 dt/P cycles, and its FP32 rounding leaves about 2^-34 dt/P cycles
 // (1.2e-7 cycles at dt/P = 2000: a 4000-day baseline at P = 2 d; the
-// float-float phase of unit_rv_column gets 3e-8).  Both are inside the column
-// error that err_c0 bounds.  The reciprocal of the velocity's denominator is
+// float-float phase of unit_rv_column gets 3e-8).  The bound adds twice that
+// term, per sample from 1/P and the star's largest |dt|, to the constant
+// column error err_c0.  The reciprocal of the velocity's denominator is
 // the hardware one (within 2^-23 relative, no Newton step).
 template <class T>
 __device__ __forceinline__ T unit_rv_column_split(T dth, T dtl, const MixC<T> &c) {
     const T p = vmul(dth, c.ih);                                          // exact
-    const T fr = vsub(p, vmap([](float v) { return rintf(v); }, p));      // exact
+    const T fr = vsub(p, vrint(p));                                       // exact
     const T sm = vfma(dth, c.il, vmul(dtl, c.iph));
     const T f0 = vadd(vsub(fr, c.mch), vsub(sm, c.mcl));
-    const T f = vsub(f0, vmap([](float v) { return rintf(v); }, f0));     // [-0.5, 0.5]
+    const T f = vsub(f0, vrint(f0));                                      // [-0.5, 0.5]
     const T M = vfma(f, vsplat<T>(TWO_PI_HI_F), vmul(f, vsplat<T>(TWO_PI_LO_F)));
     T sE, cE;
     vkepler<false>(M, c.e, c.ne, c.ome, c.ome3, c.a1, sE, cE);
@@ -293,8 +295,8 @@ __device__ __forceinline__ void fast_tail(const StarRec &st, const AccF<L, JIT, 
                 dl += fabsf(Hi[j][k].hi + v[j].hi * v[k].hi * iS) * gam * sqrtf(Gjj[j] * Gjj[k]);
     }
     float dlog = dl + 1.34f * xf * xf;
-    // ---- the FP32 column's own error (err_c0 empirical, as in the mixed
-    // kernel): chi2 is a minimum over the linear parameters, so it moves by
+    // ---- the FP32 column's own error (err_c0: the empirical constant plus
+    // the phase term of this sample, as in the mixed kernel): chi2 is a minimum over the linear parameters, so it moves by
     // -2 K sum w res dm; s moves directly
     const float Dcol = err_c0 * (1.0f + e) / (ome * ome);
     const float Wsum = st.sum_ivar;
@@ -660,7 +662,8 @@ __device__ __forceinline__ bool fused_out_of_reach(const StarRec &st,
                                                    const AccF<L, JIT, float2> &A,
                                                    const float *ck, float e0, float ome0,
                                                    float e1, float ome1, float lgP0, float lgP1,
-                                                   float s20, float s21, float err_c0, bool act0,
+                                                   float s20, float s21, float ec0, float ec1,
+                                                   bool act0,
                                                    bool act1, const unsigned long long *bk,
                                                    float &ub0, float &ub1) {
     const unsigned long long gk = *((volatile const unsigned long long *)(bk + 1));
@@ -672,12 +675,12 @@ __device__ __forceinline__ bool fused_out_of_reach(const StarRec &st,
         float dub;
         bool ok;
         if (act0) {
-            ub0 = fast_upper<L, JIT>(st, accf_lane(A, 0), ck, lgP0, s20, e0, ome0, err_c0,
+            ub0 = fast_upper<L, JIT>(st, accf_lane(A, 0), ck, lgP0, s20, e0, ome0, ec0,
                                      dub, ok);
             h0 = lb_ok && ok && ub0 + dub < lim;
         }
         if (act1) {
-            ub1 = fast_upper<L, JIT>(st, accf_lane(A, 1), ck, lgP1, s21, e1, ome1, err_c0,
+            ub1 = fast_upper<L, JIT>(st, accf_lane(A, 1), ck, lgP1, s21, e1, ome1, ec1,
                                      dub, ok);
             h1 = lb_ok && ok && ub1 + dub < lim;
         }
@@ -738,6 +741,9 @@ lnl_fast2_kernel(LnlArgs a) {
             A.zero();
             bool exited = false;
             float ub0 = 0.0f, ub1 = 0.0f;
+            // column-error constant of a sample with 1/P = iph: the empirical
+            // part plus the split phase's rounding over the star's span
+            auto col_c0 = [&](float iph) { return fmaf(st.phase_c, iph, a.err_c0); };
             // every epoch, staged a tile at a time for long stars
             auto all_epochs = [&]() {
                 for (int t0 = 0; t0 < N; t0 += TILE) {
@@ -770,8 +776,9 @@ lnl_fast2_kernel(LnlArgs a) {
                         }
                         i0 = kend;
                         if (fused_out_of_reach<L, JIT>(st, A, st.ck[q], c0.e, c0.ome, c1.e,
-                                                       c1.ome, pb0.w, pb1.w, s20, s21, a.err_c0,
-                                                       act0, act1, bk, ub0, ub1)) {
+                                                       c1.ome, pb0.w, pb1.w, s20, s21,
+                                                       col_c0(c.iph.x), col_c0(c.iph.y), act0,
+                                                       act1, bk, ub0, ub1)) {
                             exited = true;
                             break;
                         }
@@ -786,13 +793,15 @@ lnl_fast2_kernel(LnlArgs a) {
                         // float-float tail and its bound (ub is then ln L in FP32)
                         exited = fused_out_of_reach<L, JIT>(st, A, st.ck_full, c0.e, c0.ome, c1.e,
                                                             c1.ome, pb0.w, pb1.w, s20, s21,
-                                                            a.err_c0, act0, act1, bk, ub0, ub1);
+                                                            col_c0(c.iph.x), col_c0(c.iph.y),
+                                                            act0, act1, bk, ub0, ub1);
                     }
                 } else {
                     all_epochs();
                     exited = fused_out_of_reach<L, JIT>(st, A, st.ck_full, c0.e, c0.ome, c1.e,
                                                         c1.ome, pb0.w, pb1.w, s20, s21,
-                                                        a.err_c0, act0, act1, bk, ub0, ub1);
+                                                        col_c0(c.iph.x), col_c0(c.iph.y),
+                                                        act0, act1, bk, ub0, ub1);
                 }
             } else {
                 all_epochs();
@@ -802,7 +811,8 @@ lnl_fast2_kernel(LnlArgs a) {
                     // their ln L in FP32 and skips the float-float tail and bound
                     exited = fused_out_of_reach<L, JIT>(st, A, st.ck_full, c0.e, c0.ome, c1.e,
                                                         c1.ome, pb0.w, pb1.w, s20, s21,
-                                                        a.err_c0, act0, act1, bk, ub0, ub1);
+                                                        col_c0(c.iph.x), col_c0(c.iph.y),
+                                                        act0, act1, bk, ub0, ub1);
                 }
             }
             if ((EXIT || (FUSED && L <= 3)) && exited) {
@@ -823,9 +833,11 @@ lnl_fast2_kernel(LnlArgs a) {
             ff l0 = ffv(0.0f), l1 = ffv(0.0f);
             float err0 = 0.0f, err1 = 0.0f;
             if (act0)
-                fast_tail<L, JIT>(st, accf_lane(A, 0), c0.e, c0.ome, pb0.w, s20, N, a.err_c0, l0, err0);
+                fast_tail<L, JIT>(st, accf_lane(A, 0), c0.e, c0.ome, pb0.w, s20, N,
+                                  col_c0(c.iph.x), l0, err0);
             if (act1)
-                fast_tail<L, JIT>(st, accf_lane(A, 1), c1.e, c1.ome, pb1.w, s21, N, a.err_c0, l1, err1);
+                fast_tail<L, JIT>(st, accf_lane(A, 1), c1.e, c1.ome, pb1.w, s21, N,
+                                  col_c0(c.iph.y), l1, err1);
             const unsigned long long kd =
                 fast_store2(a, w.out_off + j0, act0, l0, err0, w.out_off + j1, act1, l1, err1, mk,
                             bk);

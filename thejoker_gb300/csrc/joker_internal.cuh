@@ -63,6 +63,8 @@ struct alignas(16) StarRec {
     float Wjj[MAXL];                   // sum ivar T_j^2 (j >= 1), rounded up
     float log_kscale_f, log_maxK2_f;   // log_kscale, log_maxK2 rounded to float
     float log_lam0_f;                  // log lam0 rounded to float
+    float phase_c;                     // 2 pi 2^-33 max |t - t_ref|, rounded up: the split
+                                       // phase's rounding per unit of 1/P (radians)
     // Early exit of the fused pass (L <= 3): after the first ck_k[c] epochs
     // the partial sums bound ln L from above.  Per checkpoint: P_j = sum over
     // those epochs of ivar r_c T_j minus (Lambda_T^-1 beta0)_j (j = 1, 2);
