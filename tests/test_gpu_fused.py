@@ -256,14 +256,16 @@ def test_early_exit_keeps_fp64_rows(cuda, name):
     assert r64[0].sum() > 0
 
 
+@pytest.mark.parametrize("early_exit", [True, False])
 @pytest.mark.parametrize("jitter", ["applied", "reference"])
-def test_early_exit_values_are_upper_bounds(cuda, jitter):
-    """Direct joker_lnl_fused call with early exit: every sample whose error
-    bound is infinite (its warp stopped at a checkpoint, or was out of reach
-    after its last epoch) holds a value at or above its FP64 ln L (up to
-    FP32 rounding after the last epoch), lies more than 746 nats below the
-    maximum, and has no candidate bit; the other samples hold their usual
-    values and bounds.  An
+def test_early_exit_values_are_upper_bounds(cuda, jitter, early_exit):
+    """Direct joker_lnl_fused call: every sample whose error bound is
+    infinite (with early exit, its warp stopped at a checkpoint; with or
+    without it, its warp was out of reach after its last epoch) holds a
+    value at or above its FP64 ln L (up to FP32 rounding after the last
+    epoch; without early exit that FP32 ln L itself), lies more than 746
+    nats below the maximum, and has no candidate bit; the other samples hold
+    their usual values and bounds.  An
     eighth of the orbits (a contiguous block, so that whole warps hold them)
     have e in [0.9, 0.995], where the FP32 column's own error is largest."""
     from thejoker_gb300 import device as dev
@@ -285,11 +287,14 @@ def test_early_exit_values_are_upper_bounds(cuda, jitter):
     bk = dev.MaxKeys(2)
     pcg = dev.pcg_table([dev.pcg64_state(np.random.default_rng(9))])
     ld, cand = dev.cand_words(1, S)
-    dev.lnl_fused(table, cache, lnl, err, bk, pcg, cand, ld, chunk=512, early_exit=True)
+    dev.lnl_fused(table, cache, lnl, err, bk, pcg, cand, ld, chunk=512, early_exit=early_exit)
     v, e = lnl[0].cpu().numpy(), err[0].cpu().numpy()
     out = np.isinf(e)
-    print(jitter, "samples stopped early", out.mean())
+    print(jitter, early_exit, "samples with an infinite bound", out.mean())
     assert out.mean() > 0.2
+    if not early_exit:
+        # every epoch evaluated: the stored value is ln L in FP32
+        assert np.all(np.abs(v[out] - l64[out]) <= 1e-4 * np.abs(l64[out]) + 100.0)
     # none of them can be kept or be the maximum
     assert np.all(l64[out] < l64.max() - 746.0)
     # an upper bound from the first epochs, or ln L itself in FP32 after the
