@@ -280,7 +280,8 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
     r.sum_log_ivar = (double)slog_ivar;
     // FP32-sum path: the residual of the trend-only fit r_c = y' - T^T beta0
     // (beta0 = C^-1 c, as stored in cC) and the magnitudes its bound needs
-    long double Cn = 0.0L, ivmax = 0.0L, Wjj[MAXL] = {0.0L}, kappa = 0.0L, dtmax = 0.0L;
+    long double Cn = 0.0L, ivmax = 0.0L, Wjj[MAXL] = {0.0L}, kappa = 0.0L, dtmax = 0.0L,
+                swdt2 = 0.0L;
     for (int j = 1; j < L; ++j) kappa += (long double)r.cC[j] * r.cC[j] / (long double)lamk[j];
     for (int i = 0; i < n; ++i) {
         long double yp = rv[i];
@@ -294,7 +295,9 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
             const long double Tj = trend_M[(size_t)i * T + (j - 1)];
             Wjj[j] += w * Tj * Tj;
         }
-        dtmax = std::max(dtmax, (long double)std::fabs(t[i] - t_ref));
+        const long double adt = std::fabs(t[i] - t_ref);
+        dtmax = std::max(dtmax, adt);
+        swdt2 += (long double)ivar[i] * adt * adt;
         float *r32 = rec32 + (size_t)i * REC32;
         // dt split for the FP32-sum kernel's phase: dth with 12 significant
         // bits (exact in a float), dtl the rest.  Words 16 and 17 are free in
@@ -352,12 +355,21 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
             ++q;
         }
         r.n_ck = q;
-        // all epochs: P = 0 (T W0 r_c = Lambda_T^-1 beta0), C + kappa = chi2_0,
-        // H = C (the folded trend block)
-        for (int j = 0; j < 8; ++j) r.ck_full[j] = 0.0f;
+    }
+    // all epochs (L <= 4): P = 0 (T W0 r_c = Lambda_T^-1 beta0), C + kappa =
+    // chi2_0, H = C (the folded trend block).  With three trend columns the
+    // free P slots hold the third row of C^-1: {Hi13, Hi23, C + kappa, Hi11,
+    // Hi12, Hi22, log det C, Hi33}
+    for (int j = 0; j < 8; ++j) r.ck_full[j] = 0.0f;
+    if (L <= 4) {
         r.ck_full[2] = (float)(Cn + kappa);
         if (T >= 1) r.ck_full[3] = (float)Cinv[0];
-        if (T == 2) { r.ck_full[4] = (float)Cinv[1]; r.ck_full[5] = (float)Cinv[3]; }
+        if (T >= 2) { r.ck_full[4] = (float)Cinv[1]; r.ck_full[5] = (float)Cinv[T + 1]; }
+        if (T == 3) {
+            r.ck_full[0] = (float)Cinv[2];
+            r.ck_full[1] = (float)Cinv[5];
+            r.ck_full[7] = (float)Cinv[8];
+        }
         r.ck_full[6] = (float)logdetC;
     }
     split_ff((double)kappa, r.kappa_hi, r.kappa_lo);
@@ -365,8 +377,14 @@ static int prep_star(int k, int L, int jitter_mode, int n, const double *t, cons
     split_ff((double)(n * LOG2PI + slog_lam - slog_ivar), r.lnr_hi, r.lnr_lo);
     r.Cn = (float)(Cn * (1.0L + 1e-6L));
     r.ivar_max = (float)(ivmax * (1.0L + 1e-6L));
-    r.phase_c = (float)(dtmax * (2.0L * 3.141592653589793238462643383279502884L * 0x1p-33L *
-                                 (1.0L + 1e-6L)));
+    // the split phase rounds to at most 2.5 2^-34 |dt| / P cycles; the bound
+    // takes the column error through its ivar-weighted norm, so the
+    // ivar-weighted RMS of |dt| stands for |dt| (the largest |dt| when the
+    // weights are not finite)
+    long double rms = sw > 0.0L ? sqrtl(swdt2 / sw) : dtmax;
+    if (!(rms <= dtmax)) rms = dtmax;
+    r.phase_c = (float)(rms * (2.0L * 3.141592653589793238462643383279502884L * 2.5L *
+                               0x1p-34L * (1.0L + 1e-6L)));
     for (int j = 1; j < L; ++j) r.Wjj[j] = (float)(Wjj[j] * (1.0L + 1e-6L));
     return JOKER_OK;
 }

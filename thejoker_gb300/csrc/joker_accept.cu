@@ -103,6 +103,14 @@ __device__ __forceinline__ bool dbl_to_float_trunc(double x, float &f) {
     return true;
 }
 
+// +infinity as a sample's bound: the ln L kernel found it out of reach, its
+// ln L (upper bound) more than 746 nats below a lower bound of the maximum:
+// exp(lnL - max) underflows to 0, so no uniform keeps it, and it is not the
+// maximum.  (A tail without a bound writes 1e30, never +infinity.)
+__device__ __forceinline__ bool out_of_reach(float er) {
+    return __float_as_int(er) == 0x7f800000;
+}
+
 // Decision of exp(v + [-er, er] - mx) > u from float approximations:
 // 1 keep, 0 reject, 2 undecided here (use the FP64 test).  uf = float u
 // (> 0, truncated), vf, mxf = float approximations of v, mx.
@@ -154,7 +162,9 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_candidates_kernel(AcceptAr
             const double v = a.lnl[sg.lnl_off + i];
             const float er = a.err[sg.lnl_off + i];
             float vf;
-            if (fast && er < 1e29f && dbl_to_float_trunc(v, vf) &&
+            if (out_of_reach(er)) {
+                cand = false;
+            } else if (fast && er < 1e29f && dbl_to_float_trunc(v, vf) &&
                 vf + er + (1e-6f + 5e-7f * (fabsf(vf) + fabsf(lbf) + er)) < lbf) {
                 cand = false;                        // certainly below the largest lower bound
             } else {
@@ -347,7 +357,9 @@ __global__ void __launch_bounds__(ACC_THREADS) band_flag_kernel(AcceptArgs a, do
             const double v = a.lnl[sg.lnl_off + i];
             const float er = a.err[sg.lnl_off + i];
             float vf;
-            if (!(er < 1e29f) || !(v == v)) {
+            if (out_of_reach(er)) {
+                flag = band >= 746.0;                // more than 746 below the maximum
+            } else if (!(er < 1e29f) || !(v == v)) {
                 flag = true;                         // no bound, or no value
             } else if (er <= tol) {
                 flag = false;                        // already within the tolerance
@@ -423,7 +435,9 @@ __global__ void __launch_bounds__(ACC_THREADS) accept_mark_kernel(AcceptArgs a) 
             const float er = refine ? a.err[sg.lnl_off + i] : 0.0f;
             float vf;
             int dec = 2;
-            if (fast && uf_ok && er < 1e29f && dbl_to_float_trunc(v, vf))
+            if (refine && out_of_reach(er))
+                dec = 0;
+            else if (fast && uf_ok && er < 1e29f && dbl_to_float_trunc(v, vf))
                 dec = fast_decide(vf, er, mxf, uf);
             if (dec == 2) {
                 const double u = a.u_source == JOKER_U_PCG64 ? (double)m * 0x1.0p-53 : ua;

@@ -28,8 +28,10 @@
 // |dG|_F tr(G^-1) < 1/4 (else err = 1e30: no bound, always refined); and
 // |d log det G| <= |tr(G^-1 dG)| + 1.34 |G^-1 dG|_F^2.  The FP32 column's own
 // error (FP32 Kepler and the phase's constant rounding: the empirical
-// constant err_c0; the split phase's rounding, at most 2^-34 |dt| / P cycles,
-// as 2 pi 2^-33 max|dt| / P radians on top) enters as in the mixed kernel.  The tail runs in float-float; the only FP64
+// constant err_c0; the split phase's rounding, at most 2.5 2^-34 |dt| / P
+// cycles, on top) enters as in the mixed kernel through its ivar-weighted
+// norm, which by Minkowski's inequality takes the ivar-weighted RMS of |dt|
+// in place of each epoch's |dt|.  The tail runs in float-float; the only FP64
 // instruction per sample is the addition that rounds ln L's float pair to a
 // double (both halves converted by integer operations).
 #pragma once
@@ -59,11 +61,12 @@ template <int L, bool JIT, class T> struct AccF {
 // The unit-K RV column with a split phase: dt = dth + dtl with dth carrying
 // 12 significant bits and 1/P = ih + il with ih carrying 12, so dth ih is
 // exact in FP32 and so is its fractional part; |dth il| + |dtl / P| is below
-// 2^-10 dt/P cycles, and its FP32 rounding leaves about 2^-34 dt/P cycles
-// (1.2e-7 cycles at dt/P = 2000: a 4000-day baseline at P = 2 d; the
-// float-float phase of unit_rv_column gets 3e-8).  The bound adds twice that
-// term, per sample from 1/P and the star's largest |dt|, to the constant
-// column error err_c0.  The reciprocal of the velocity's denominator is
+// 2^-11 dt/P cycles, and the roundings of dtl, il, dtl 1/P, the FMA and the
+// two additions of the phase leave at most 2.5 2^-34 dt/P cycles (1.2e-7
+// cycles typically at dt/P = 2000: a 4000-day baseline at P = 2 d; the
+// float-float phase of unit_rv_column gets 3e-8).  The bound adds that term,
+// per sample from 1/P and the star's ivar-weighted RMS of |dt|, to the
+// constant column error err_c0.  The reciprocal of the velocity's denominator is
 // the hardware one (within 2^-23 relative, no Newton step).
 template <class T>
 __device__ __forceinline__ T unit_rv_column_split(T dth, T dtl, const MixC<T> &c) {
@@ -330,7 +333,8 @@ __device__ __forceinline__ void fast_tail(const StarRec &st, const AccF<L, JIT, 
     // of each epoch's jitter term (2e-7 N), the float-float tail (its terms'
     // magnitude times 2^-40), and 1 % for the FP32 evaluation of the bound
     err = 1.01f * (0.5f * (dchi + dlog) + 2e-6f + 2e-7f * (float)N + 1e-12f * tailmag);
-    if (!ok || !(err == err) || !(lnl.hi == lnl.hi)) err = 1e30f;
+    // no bound: 1e30 (+infinity is reserved for samples out of reach)
+    if (!ok || !(err < 1e30f) || !(lnl.hi == lnl.hi)) err = 1e30f;
 }
 
 template <int L, bool JIT>
@@ -564,7 +568,7 @@ __device__ __forceinline__ void fused_pass(const LnlArgs &a, const WorkItem &w, 
 // Returns -1/2 of the k-epoch expression and in dub a margin for its error:
 // 1e-3 of its terms' magnitudes (over 100 times the rounding of FP32 sums of
 // at most 103 terms, which covers the cross sums' Cauchy-Schwarz factors in
-// practice), plus the amplification of the sums' rounding through an
+// practice; 100 (k + 3) 2^-24 for longer sums), plus the amplification of the sums' rounding through an
 // ill-conditioned Schur complement s or trend block H (t^2 / s and
 // q'^T H^-1 q' move by their relative errors), plus twice the FP32 column's
 // own error term of the full bound (err_c0 (1 + e) / (1 - e)^2 per epoch,
@@ -573,21 +577,38 @@ __device__ __forceinline__ void fused_pass(const LnlArgs &a, const WorkItem &w, 
 // collinear with the constant column, say).
 template <int L, bool JIT>
 __device__ __forceinline__ float fast_upper(const StarRec &st, const AccF<L, JIT, float> &A,
-                                            const float *ck, float lgP, float s2, float e,
-                                            float ome, float err_c0, float &dub, bool &valid) {
+                                            const float *ck, int nsum, float lgP, float s2,
+                                            float e, float ome, float err_c0, float &dub,
+                                            bool &valid) {
     constexpr int T = L - 1;
-    constexpr float g1 = 2e-5f;   // three times the rounding bound of a sum of <= 103 terms
-    static_assert(L <= 3, "early exit takes at most three linear parameters");
+    constexpr int TT = T > 0 ? T : 1;
+    static_assert(L <= 3 || (L == 4 && !JIT),
+                  "the upper bound takes at most three linear parameters, four without jitter");
+    // g1: three times the rounding bound of an FP32 sum of nsum terms (at
+    // least that of 103 terms); fm: over 100 times that bound
+    const float nu = (float)(nsum + 3) * U32;
+    const float g1 = fmaxf(2e-5f, 3.0f * nu);
+    const float fm = fmaxf(1e-3f, 100.0f * nu);
     const float log_lam0f =
         st.k_scaled ? fminf(st.log_maxK2_f, st.log_kscale_f + lgP) : st.log_lam0_f;
     const float ilam0 = __expf(-log_lam0f);
     const float mu = st.mu0_f;
-    float Hi[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}}, ldH = 0.0f, rH = 0.0f;
+    float Hi[TT][TT], ldH = 0.0f, rH = 0.0f;
+#pragma unroll
+    for (int j = 0; j < TT; ++j)
+#pragma unroll
+        for (int m = 0; m < TT; ++m) Hi[j][m] = 0.0f;
     valid = true;
     if constexpr (!JIT) {
-        // host-computed: only the float rounding of the entries
+        // host-computed: only the float rounding of the entries (three trend
+        // columns: all epochs only, the third row of C^-1 in the P slots)
         if (T >= 1) Hi[0][0] = ck[3];
-        if (T == 2) { Hi[0][1] = Hi[1][0] = ck[4]; Hi[1][1] = ck[5]; }
+        if (T >= 2) { Hi[0][1] = Hi[1][0] = ck[4]; Hi[1][1] = ck[5]; }
+        if (T == 3) {
+            Hi[0][2] = Hi[2][0] = ck[0];
+            Hi[1][2] = Hi[2][1] = ck[1];
+            Hi[2][2] = ck[7];
+        }
         ldH = ck[6];
         rH = 1e-6f;
     } else if constexpr (T == 1) {
@@ -607,11 +628,11 @@ __device__ __forceinline__ float fast_upper(const StarRec &st, const AccF<L, JIT
         rH = ddet / (det - ddet) + g1;
         valid = det > 4.0f * ddet && H11 > 0.0f;
     }
-    float g[2] = {0.0f, 0.0f}, qT[2] = {0.0f, 0.0f};
+    float g[TT], qT[TT];
 #pragma unroll
     for (int j = 0; j < T; ++j) {
         g[j] = A.g[j + 1];
-        qT[j] = ck[j] - (JIT ? s2 * A.Q[j + 1] : 0.0f) - mu * g[j];
+        qT[j] = (T == 3 ? 0.0f : ck[j]) - (JIT ? s2 * A.Q[j + 1] : 0.0f) - mu * g[j];
     }
     float gv = 0.0f, gz = 0.0f, qz = 0.0f;
 #pragma unroll
@@ -648,19 +669,21 @@ __device__ __forceinline__ float fast_upper(const StarRec &st, const AccF<L, JIT
     const float col = 2.0f * Kh * Dcol * sqrtf(Wsum * c2) + Kh * Kh * Dcol * Dcol * Wsum +
                       dsc / (sK - dsc);
     const float cond = q2 * ds / (sK - ds) + fabsf(qz) * rH + ds / (sK - ds) + rH * (float)T;
-    dub = 0.5f * (1e-3f * mag + 2.0f * cond + 2.0f * col) + 2.0f;
+    dub = 0.5f * (fm * mag + 2.0f * cond + 2.0f * col) + 2.0f;
     return -0.5f * t;
 }
 
 // Whether every active sample of the warp is out of reach after the first
-// ck_k[c] epochs: its k-epoch upper bound plus its margin lies more than 746
-// nats below the running lower bound of the maximum.  Such a sample is
+// nsum epochs (ck: that checkpoint's constants, or ck_full after all of them):
+// its upper bound plus its margin lies more than 746 nats below the running
+// lower bound of the maximum.  Such a sample is
 // rejected for every uniform, 0 included, and cannot be the maximum.  ub0
 // and ub1 receive the lanes' bounds.
 template <int L, bool JIT>
 __device__ __forceinline__ bool fused_out_of_reach(const StarRec &st,
                                                    const AccF<L, JIT, float2> &A,
-                                                   const float *ck, float e0, float ome0,
+                                                   const float *ck, int nsum, float e0,
+                                                   float ome0,
                                                    float e1, float ome1, float lgP0, float lgP1,
                                                    float s20, float s21, float ec0, float ec1,
                                                    bool act0,
@@ -675,12 +698,12 @@ __device__ __forceinline__ bool fused_out_of_reach(const StarRec &st,
         float dub;
         bool ok;
         if (act0) {
-            ub0 = fast_upper<L, JIT>(st, accf_lane(A, 0), ck, lgP0, s20, e0, ome0, ec0,
+            ub0 = fast_upper<L, JIT>(st, accf_lane(A, 0), ck, nsum, lgP0, s20, e0, ome0, ec0,
                                      dub, ok);
             h0 = lb_ok && ok && ub0 + dub < lim;
         }
         if (act1) {
-            ub1 = fast_upper<L, JIT>(st, accf_lane(A, 1), ck, lgP1, s21, e1, ome1, ec1,
+            ub1 = fast_upper<L, JIT>(st, accf_lane(A, 1), ck, nsum, lgP1, s21, e1, ome1, ec1,
                                      dub, ok);
             h1 = lb_ok && ok && ub1 + dub < lim;
         }
@@ -702,6 +725,10 @@ template <int L, bool JIT, bool PACKED, bool FUSED, bool EXIT = false>
 __global__ void __launch_bounds__(128, JOKER_FAST_MINB)
 lnl_fast2_kernel(LnlArgs a) {
     static_assert(!EXIT || (FUSED && L <= 3), "early exit is part of the fused pass, L <= 3");
+    // the out-of-reach test after the last epoch: always in the fused pass
+    // (L <= 3), on request (oor_tail) in the plain form (L <= 3, or 4 without
+    // jitter)
+    constexpr bool OOR = FUSED ? (L <= 3) : (L <= 3 || (L == 4 && !JIT));
     __shared__ __align__(16) float sm[TILE * REC32];
     __shared__ double smr[PACKED ? PACK_ROWS * 5 : 1];
     __shared__ unsigned long long s_pcg[FUSED ? 2 * FUSED_PASSES + 4 : 1];
@@ -775,7 +802,7 @@ lnl_fast2_kernel(LnlArgs a) {
                                 fast_epoch<L, JIT, false>(sm + i * REC32, c, A);
                         }
                         i0 = kend;
-                        if (fused_out_of_reach<L, JIT>(st, A, st.ck[q], c0.e, c0.ome, c1.e,
+                        if (fused_out_of_reach<L, JIT>(st, A, st.ck[q], kend, c0.e, c0.ome, c1.e,
                                                        c1.ome, pb0.w, pb1.w, s20, s21,
                                                        col_c0(c.iph.x), col_c0(c.iph.y), act0,
                                                        act1, bk, ub0, ub1)) {
@@ -791,31 +818,30 @@ lnl_fast2_kernel(LnlArgs a) {
                         }
                         // all epochs: the same test on the full sums spares the
                         // float-float tail and its bound (ub is then ln L in FP32)
-                        exited = fused_out_of_reach<L, JIT>(st, A, st.ck_full, c0.e, c0.ome, c1.e,
-                                                            c1.ome, pb0.w, pb1.w, s20, s21,
-                                                            col_c0(c.iph.x), col_c0(c.iph.y),
-                                                            act0, act1, bk, ub0, ub1);
+                        exited = fused_out_of_reach<L, JIT>(
+                            st, A, st.ck_full, N, c0.e, c0.ome, c1.e, c1.ome, pb0.w, pb1.w, s20,
+                            s21, col_c0(c.iph.x), col_c0(c.iph.y), act0, act1, bk, ub0, ub1);
                     }
                 } else {
                     all_epochs();
-                    exited = fused_out_of_reach<L, JIT>(st, A, st.ck_full, c0.e, c0.ome, c1.e,
-                                                        c1.ome, pb0.w, pb1.w, s20, s21,
-                                                        col_c0(c.iph.x), col_c0(c.iph.y),
-                                                        act0, act1, bk, ub0, ub1);
+                    exited = fused_out_of_reach<L, JIT>(
+                        st, A, st.ck_full, N, c0.e, c0.ome, c1.e, c1.ome, pb0.w, pb1.w, s20, s21,
+                        col_c0(c.iph.x), col_c0(c.iph.y), act0, act1, bk, ub0, ub1);
                 }
             } else {
                 all_epochs();
-                if constexpr (FUSED && L <= 3) {
+                if constexpr (OOR) {
                     // every epoch evaluated: a warp whose samples are all out of
                     // reach (rejected for every uniform, not the maximum) keeps
-                    // their ln L in FP32 and skips the float-float tail and bound
-                    exited = fused_out_of_reach<L, JIT>(st, A, st.ck_full, c0.e, c0.ome, c1.e,
-                                                        c1.ome, pb0.w, pb1.w, s20, s21,
-                                                        col_c0(c.iph.x), col_c0(c.iph.y),
-                                                        act0, act1, bk, ub0, ub1);
+                    // their ln L in FP32 and skips the float-float tail and
+                    // bound (the fused pass, or on request)
+                    if (FUSED || (a.oor_tail && bk))
+                        exited = fused_out_of_reach<L, JIT>(
+                            st, A, st.ck_full, N, c0.e, c0.ome, c1.e, c1.ome, pb0.w, pb1.w, s20,
+                            s21, col_c0(c.iph.x), col_c0(c.iph.y), act0, act1, bk, ub0, ub1);
                 }
             }
-            if ((EXIT || (FUSED && L <= 3)) && exited) {
+            if ((EXIT || OOR) && exited) {
                 // ln L of these samples is left at their upper bound (or, after
                 // the last epoch, at its FP32 value), with an infinite error
                 // bound; they carry no candidate bit and no key
@@ -827,7 +853,7 @@ lnl_fast2_kernel(LnlArgs a) {
                     a.lnl[w.out_off + j1] = (double)ub1;
                     a.err[w.out_off + j1] = __int_as_float(0x7f800000);
                 }
-                fused_write_words(a, w, base, 0u, 0u);
+                if constexpr (FUSED) fused_write_words(a, w, base, 0u, 0u);
                 continue;
             }
             ff l0 = ffv(0.0f), l1 = ffv(0.0f);

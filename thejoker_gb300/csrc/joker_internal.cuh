@@ -63,8 +63,9 @@ struct alignas(16) StarRec {
     float Wjj[MAXL];                   // sum ivar T_j^2 (j >= 1), rounded up
     float log_kscale_f, log_maxK2_f;   // log_kscale, log_maxK2 rounded to float
     float log_lam0_f;                  // log lam0 rounded to float
-    float phase_c;                     // 2 pi 2^-33 max |t - t_ref|, rounded up: the split
-                                       // phase's rounding per unit of 1/P (radians)
+    float phase_c;                     // 2 pi 2.5 2^-34 rms |t - t_ref| (ivar-weighted),
+                                       // rounded up: the split phase's rounding per
+                                       // unit of 1/P (radians), in the bound's norm
     // Early exit of the fused pass (L <= 3): after the first ck_k[c] epochs
     // the partial sums bound ln L from above.  Per checkpoint: P_j = sum over
     // those epochs of ivar r_c T_j minus (Lambda_T^-1 beta0)_j (j = 1, 2);
@@ -131,6 +132,12 @@ struct LnlArgs {
     // sums put all its samples out of reach; their ln L is left at that upper
     // bound with an infinite error bound, and they get no candidate bit
     int fa_exit;
+    // plain FP32-sum kernel only (L <= 3, or 4 without jitter): after the last
+    // epoch a warp whose samples are all out of reach of the running lower
+    // bound of the maximum (bound_key) stores their ln L in FP32 with an
+    // infinite error bound, skipping the float-float tail; the acceptance
+    // kernels reject such samples for every uniform
+    int oor_tail;
 };
 
 // Largest work item (samples) of the fused pass: its per-pass generator

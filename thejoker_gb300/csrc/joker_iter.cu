@@ -529,6 +529,10 @@ extern "C" int joker_iter_round(joker_iter *it, void *stream) {
         a.err = it->err;
         a.bound_key = it->bound_key;
         a.err_c0 = mixed_err_c0();
+        // samples out of reach of the maximum after their last epoch keep an
+        // FP32 ln L and an infinite bound (the acceptance rejects them); the
+        // maximum only grows over the rounds, so they stay out of reach
+        a.oor_tail = it->precision == JOKER_MIXED_FAST;
     }
     if ((e = cudaMemsetAsync(it->queue, 0, sizeof(int), st)) != cudaSuccess ||
         (e = launch_lnl(it->precision, L, jit != 0, a, 128, st)) != cudaSuccess)

@@ -520,7 +520,8 @@ __device__ __forceinline__ void mixed_tail(const StarRec &st, const Acc32<L, JIT
     const float dlogs = (room > 1e-3f * s_f) ? ds / room : 1e30f;
     err = 0.5f * (dchi + dlogs) + 2e-6f + 2e-7f * (float)N +
           1e-12f * (fabsf(chi2f) + fabsf(quadf)) + (JIT ? 2e-7f * c2 : 0.f);
-    if (!(err == err)) err = 1e30f;      // NaN inputs: no bound
+    if (!(err < 1e30f)) err = 1e30f;     // NaN inputs or overflow: no bound
+                                         // (+infinity marks samples out of reach)
 }
 
 template <int L, bool JIT>
