@@ -68,13 +68,13 @@ template <int L, bool JIT, class T> struct AccF {
 // per sample from 1/P and the star's ivar-weighted RMS of |dt|, to the
 // constant column error err_c0.  The reciprocal of the velocity's denominator is
 // the hardware one (within 2^-23 relative, no Newton step).
-template <class T>
+template <bool SHIFT, class T>
 __device__ __forceinline__ T unit_rv_column_split(T dth, T dtl, const MixC<T> &c) {
     const T p = vmul(dth, c.ih);                                          // exact
-    const T fr = vsub(p, vrint(p));                                       // exact
+    const T fr = vsub(p, vrint<SHIFT>(p));                                // exact
     const T sm = vfma(dth, c.il, vmul(dtl, c.iph));
     const T f0 = vadd(vsub(fr, c.mch), vsub(sm, c.mcl));
-    const T f = vsub(f0, vrint(f0));                                      // [-0.5, 0.5]
+    const T f = vsub(f0, vrint<SHIFT>(f0));                               // [-0.5, 0.5]
     const T M = vfma(f, vsplat<T>(TWO_PI_HI_F), vmul(f, vsplat<T>(TWO_PI_LO_F)));
     T sE, cE;
     vkepler<false>(M, c.e, c.ne, c.ome, c.ome3, c.a1, sE, cE);
@@ -89,7 +89,7 @@ __device__ __forceinline__ T unit_rv_column_split(T dth, T dtl, const MixC<T> &c
 template <int L, bool JIT, bool ACCURATE, class T>
 __device__ __forceinline__ void fast_epoch(const float *recf, const MixC<T> &c,
                                            AccF<L, JIT, T> &A) {
-    const T m = unit_rv_column_split(vsplat<T>(recf[16]), vsplat<T>(recf[17]), c);
+    const T m = unit_rv_column_split<JIT>(vsplat<T>(recf[16]), vsplat<T>(recf[17]), c);
     const T iv = vsplat<T>(recf[2]);
     if constexpr (!JIT) {
         const T ivm = vmul(iv, m);
