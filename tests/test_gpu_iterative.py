@@ -33,7 +33,9 @@ def reference_iterative(lls_all, seed, n_req, init, n_total, safety=1.0, maxiter
 
 @pytest.mark.parametrize("precision,use_graph,budget", [("fp64", False, 0), ("fp64", True, 0),
                                                         ("mixed", True, 0),
-                                                        ("mixed", True, 20000)])
+                                                        ("mixed", True, 20000),
+                                                        ("mixed_fast", True, 0),
+                                                        ("mixed_fast", False, 20000)])
 def test_iterative_matches_reference_loop(cuda, precision, use_graph, budget):
     from thejoker_gb300 import device as dev
     from thejoker_gb300.iterative import IterativeBatch

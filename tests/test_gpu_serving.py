@@ -37,7 +37,7 @@ def served():
     return stars, chunk, cache
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_fast"])
 def test_alone_equals_mix(cuda, served, precision):
     from thejoker_gb300.serve import ServingEngine
     stars, chunk, cache = served
