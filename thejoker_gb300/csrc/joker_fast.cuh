@@ -680,15 +680,14 @@ __device__ __forceinline__ float fast_upper(const StarRec &st, const AccF<L, JIT
 // rejected for every uniform, 0 included, and cannot be the maximum.  ub0
 // and ub1 receive the lanes' bounds.
 template <int L, bool JIT>
-__device__ __forceinline__ bool fused_out_of_reach(const StarRec &st,
-                                                   const AccF<L, JIT, float2> &A,
-                                                   const float *ck, int nsum, float e0,
-                                                   float ome0,
-                                                   float e1, float ome1, float lgP0, float lgP1,
-                                                   float s20, float s21, float ec0, float ec1,
-                                                   bool act0,
-                                                   bool act1, const unsigned long long *bk,
-                                                   float &ub0, float &ub1) {
+__device__ __forceinline__ bool warp_out_of_reach(const StarRec &st,
+                                                  const AccF<L, JIT, float2> &A,
+                                                  const float *ck, int nsum, float e0,
+                                                  float ome0, float e1, float ome1, float lgP0,
+                                                  float lgP1, float s20, float s21, float ec0,
+                                                  float ec1, bool act0, bool act1,
+                                                  const unsigned long long *bk, float &ub0,
+                                                  float &ub1) {
     const unsigned long long gk = *((volatile const unsigned long long *)(bk + 1));
     const bool lb_ok = gk != 0ull && gk != 0xFFFFFFFFFFFFFFFFull;
     bool h0 = !act0, h1 = !act1;
@@ -802,10 +801,10 @@ lnl_fast2_kernel(LnlArgs a) {
                                 fast_epoch<L, JIT, false>(sm + i * REC32, c, A);
                         }
                         i0 = kend;
-                        if (fused_out_of_reach<L, JIT>(st, A, st.ck[q], kend, c0.e, c0.ome, c1.e,
-                                                       c1.ome, pb0.w, pb1.w, s20, s21,
-                                                       col_c0(c.iph.x), col_c0(c.iph.y), act0,
-                                                       act1, bk, ub0, ub1)) {
+                        if (warp_out_of_reach<L, JIT>(st, A, st.ck[q], kend, c0.e, c0.ome, c1.e,
+                                                      c1.ome, pb0.w, pb1.w, s20, s21,
+                                                      col_c0(c.iph.x), col_c0(c.iph.y), act0,
+                                                      act1, bk, ub0, ub1)) {
                             exited = true;
                             break;
                         }
@@ -818,13 +817,13 @@ lnl_fast2_kernel(LnlArgs a) {
                         }
                         // all epochs: the same test on the full sums spares the
                         // float-float tail and its bound (ub is then ln L in FP32)
-                        exited = fused_out_of_reach<L, JIT>(
+                        exited = warp_out_of_reach<L, JIT>(
                             st, A, st.ck_full, N, c0.e, c0.ome, c1.e, c1.ome, pb0.w, pb1.w, s20,
                             s21, col_c0(c.iph.x), col_c0(c.iph.y), act0, act1, bk, ub0, ub1);
                     }
                 } else {
                     all_epochs();
-                    exited = fused_out_of_reach<L, JIT>(
+                    exited = warp_out_of_reach<L, JIT>(
                         st, A, st.ck_full, N, c0.e, c0.ome, c1.e, c1.ome, pb0.w, pb1.w, s20, s21,
                         col_c0(c.iph.x), col_c0(c.iph.y), act0, act1, bk, ub0, ub1);
                 }
@@ -836,7 +835,7 @@ lnl_fast2_kernel(LnlArgs a) {
                     // their ln L in FP32 and skips the float-float tail and
                     // bound (the fused pass, or on request)
                     if (FUSED || (a.oor_tail && bk))
-                        exited = fused_out_of_reach<L, JIT>(
+                        exited = warp_out_of_reach<L, JIT>(
                             st, A, st.ck_full, N, c0.e, c0.ome, c1.e, c1.ome, pb0.w, pb1.w, s20,
                             s21, col_c0(c.iph.x), col_c0(c.iph.y), act0, act1, bk, ub0, ub1);
                 }
