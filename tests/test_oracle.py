@@ -102,6 +102,21 @@ def test_accept_mask_rule():
     np.testing.assert_array_equal(oracle.accept_mask(lls, uu), [True, True, True, False])
 
 
+def test_out_of_reach_threshold_rejects_for_every_uniform():
+    """The kernels leave a sample without a bound (+inf) once its ln L lies
+    more than 746 nats below a lower bound of the maximum: exp(lnL - max)
+    then underflows to 0 in FP64, so the rule rejects it for every uniform,
+    0 included (numpy's uniforms lie in [0, 1)), while a sample 745 below
+    can still be kept with u = 0."""
+    d = -746.0 - np.array([0.0, 1e-9, 1.0, 1e3, np.inf])
+    assert np.all(np.exp(d) == 0.0)
+    lls = np.concatenate([[0.0], d])
+    uu = np.zeros(len(lls))
+    np.testing.assert_array_equal(oracle.accept_mask(lls, uu), [True] + [False] * len(d))
+    assert np.exp(-745.0) > 0.0
+    assert oracle.accept_mask(np.array([0.0, -745.0]), np.zeros(2))[1]
+
+
 @pytest.mark.skipif(not ref_cython.available(), reason="reference Cython module not built here")
 def test_reference_module_reproduces_fixture(golden_dir):
     """Re-running the compiled reference gives the committed fixture bit-for-bit."""
